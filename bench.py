@@ -1,0 +1,427 @@
+"""Benchmark of the CAPE/CIN hot path on the pressure-level workload.
+
+Workload (one "step"): calc_cape on 721 x 1440 = 1,038,240 columns x 37
+pressure levels (1000..100 hPa, float32, ps ~ U(700, 1030) hPa so the valid
+level count is ragged), once with source='most-unstable' and once with
+source='mixed-layer' (ml_depth 500 m), pseudo-liquid adiabat, pinc 500 Pa.
+value = columns per second (both sources computed for every column).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--guess plain|learned] [--workload cape|srh]
+
+--impl reference times the reference algorithm on the host cores (the CPU
+restatement of the Fortran in oracle/, all host threads, a bounded sample of
+the same workload per step).  Under torchrun every rank processes its own
+equal share of columns (weak scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID_SHAPE = (721, 1440)
+NLEV = 37
+SOURCES = (("most-unstable", 2), ("mixed-layer", 3))
+PINC = 500.0
+ML_DEPTH = 500.0
+ADIABAT = 1
+METRIC = "CAPE/CIN columns/s at 1M×37 lev: learned-guess vs plain CUDA, |ΔCAPE|≤1 J/kg"
+SRH_METRIC = "SRH columns/s at 1M×50 lev (calc_srh, depth 1000+3000 m)"
+CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
+REF_SAMPLE = 32768       # columns per --impl reference step
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--guess", default="plain", choices=["plain", "learned"])
+    ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (one process per GPU)
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def shard(n, world, rank):
+    """Contiguous, near-equal share [lo, hi) of n columns for `rank`."""
+    base, rem = divmod(n, world)
+    lo = rank * base + min(rank, rem)
+    return lo, lo + base + (1 if rank < rem else 0)
+
+
+def init_dist(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workloads
+
+def cape_inputs(lo, hi):
+    from xcape_gb300 import synthetic as S
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=GRID_SHAPE, nlev=NLEV)
+    n2 = ps.size
+    t, td = t.reshape(n2, NLEV)[lo:hi], td.reshape(n2, NLEV)[lo:hi]
+    ps, ts, tds = (a.reshape(n2)[lo:hi] for a in (ps, ts, tds))
+    return plev, t, td, ps, ts, tds
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_cape(sample, nthreads):
+    """Times the oracle (FP32 restatement of the Fortran) on `sample` columns
+    per source with `nthreads` OpenMP threads; returns columns/s."""
+    import oracle as O
+    plev, t, td, ps, ts, tds = cape_inputs(0, sample)
+    start = O.pres_lev_pos(plev, ps)
+    O.loopcape(plev, t[:64], td[:64], ps[:64], ts[:64], tds[:64], PINC, 2, ML_DEPTH, ADIABAT,
+               start=start[:64], p_is_1d=True, nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _, src in SOURCES:
+        O.loopcape(plev, t, td, ps, ts, tds, PINC, src, ML_DEPTH, ADIABAT, start=start,
+                   p_is_1d=True, nthreads=nthreads)
+    return sample / (time.perf_counter() - t0)
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle as O
+    nthreads = os.cpu_count() or 1
+    plev, t, td, ps, ts, tds = cape_inputs(0, REF_SAMPLE)
+    start = O.pres_lev_pos(plev, ps)
+
+    def step():
+        for _, src in SOURCES:
+            O.loopcape(plev, t, td, ps, ts, tds, PINC, src, ML_DEPTH, ADIABAT, start=start,
+                       p_is_1d=True, nthreads=nthreads)
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    value = REF_SAMPLE / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": "calc_cape pressure levels 721x1440 cols x 37 lev, sources "
+                   "most-unstable + mixed-layer(500 m), pseudo-liquid, pinc 500 Pa",
+                   "columns": GRID_SHAPE[0] * GRID_SHAPE[1], "levels": NLEV},
+        "cpu_baseline": {"value": value, "unit": "columns/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{REF_SAMPLE} of the 1,038,240 columns per step, both "
+                                   "sources, OpenMP over columns"},
+        "e2e": {"value": value, "unit": "columns/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    dev = torch.device("cuda", local)
+    from xcape_gb300 import _lib
+    L = _lib.lib()
+    guess = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED}[args.guess]
+
+    n_total = GRID_SHAPE[0] * GRID_SHAPE[1]
+    lo, hi = shard(n_total, world, rank)
+    plev, t, td, ps, ts, tds = cape_inputs(lo, hi)
+    n2 = hi - lo
+    P, T, TD, PS, TS, TDS = (torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                             for a in (plev, t, td, ps, ts, tds))
+    outs = {src: [torch.empty(n2, dtype=torch.float32, device=dev) for _ in range(3)] +
+            [torch.empty(n2, dtype=torch.int32, device=dev)] for src, _ in SOURCES}
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def launch(src_code, o, counters=None):
+        cape, cin, zout, mulvl = o
+        _lib.check(L.xc_loopcape_ex(2, P.data_ptr(), T.data_ptr(), TD.data_ptr(), PS.data_ptr(),
+                                    TS.data_ptr(), TDS.data_ptr(), _lib.XC_F32, PINC, src_code,
+                                    ML_DEPTH, ADIABAT, None, NLEV, n2, guess, cape.data_ptr(),
+                                    cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), None,
+                                    counters, sptr))
+
+    def step():
+        for src, code in SOURCES:
+            launch(code, outs[src])
+
+    # work accounting (untimed): sub-steps and iterations per source
+    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+    work = {}
+    for src, code in SOURCES:
+        cnt.zero_()
+        launch(code, outs[src], cnt.data_ptr())
+        torch.cuda.synchronize()
+        work[src] = [int(x) for x in cnt.cpu()]
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms_max = max_over_ranks(dist, ms, dev)
+
+    # per-kernel (per-source) average durations, for the roofline
+    per_src_ms = {}
+    for src, code in SOURCES:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            launch(code, outs[src])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_src_ms[src] = e0.elapsed_time(e1) / args.steps
+
+    # end to end through the public API from pinned host memory
+    import xcape_gb300 as X
+    pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in
+              (plev, t, td, ps, ts, tds)]
+    host = [x.numpy() for x in pinned]
+    h2d = sum(a.nbytes for a in host) * len(SOURCES)
+    d2h = 4 * 4 * n2 * len(SOURCES)
+
+    def e2e_step():
+        r = []
+        for src, _ in SOURCES:
+            r.append(X.calc_cape(*host, source=src, ml_depth=ML_DEPTH, adiabat="pseudo-liquid",
+                                 pinc=PINC, vertical_lev="pressure", guess=args.guess))
+        return r
+    e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_dt = max_over_ranks(dist, (time.perf_counter() - t0) / e2e_steps, dev)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    cols_all = n_total if world > 1 else n2
+    value = cols_all / (ms_max / 1e3)
+    hbm_peak, peak_kind = measured_peaks()
+    # algorithmic bytes of one launch: t, td (nk per column) + ps, ts, tds
+    # in, cape/cin/z_out/mulvl out, p1d once.
+    bytes_per_launch = n2 * (2 * NLEV * 4 + 3 * 4 + 4 * 4) + NLEV * 4
+    top = max(per_src_ms, key=per_src_ms.get)
+    achieved = bytes_per_launch / (per_src_ms[top] / 1e3) / 1e9
+    clocks = clk.summary()
+    # FP32 work: 60 ops per fixed-point iteration, 10 per sub-step, 40 per
+    # level (counted from CAPE_CODE_model_lev.f90:232-248, 417-547, each
+    # exp/log/pow/divide as one op), against the nominal FP32 lane rate.
+    nsub, niter = work[top]
+    flops = 60.0 * niter + 10.0 * nsub + 40.0 * n2 * NLEV
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_ach = flops / (per_src_ms[top] / 1e3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "calc_cape pressure levels 721x1440 cols x 37 lev (1000..100 hPa), "
+                               "ps~U(700,1030) ragged, sources most-unstable + mixed-layer(500 m), "
+                               "pseudo-liquid, pinc 500 Pa",
+                   "columns": cols_all, "levels": NLEV, "guess": args.guess,
+                   "l2": "inputs (307 MB) larger than L2 (129 MB), no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "kernel": f"cape_kernel ({top})", "peak_kind": peak_kind,
+                     "note": "compute-bound kernel: see fp32 entry"},
+        "fp32": {"achieved_tflops": fp32_ach, "peak_tflops_nominal": fp32_peak,
+                 "frac": fp32_ach / fp32_peak, "iterations": niter, "substeps": nsub},
+        "per_source_ms": per_src_ms,
+        "work": {k: {"substeps": v[0], "iterations": v[1]} for k, v in work.items()},
+        "e2e": {"value": cols_all / e2e_dt, "unit": "columns/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "api": "xcape_gb300.calc_cape(numpy, pinned)"},
+        "gpu_launches": args.steps * len(SOURCES),
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        import oracle  # noqa: F401
+        nth = os.cpu_count() or 1
+        v = cpu_cape(CPU_SAMPLE, nth)
+        line["cpu_baseline"] = {"value": v, "unit": "columns/s", "cores": nth, "kind": "port",
+                                "sample": f"first {CPU_SAMPLE} columns, both sources, FP32 "
+                                          "oracle (C restatement of the Fortran), OpenMP"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_srh(args):
+    """Secondary workload: calc_srh on 1024x1024 columns x 50 model levels."""
+    import torch
+    from xcape_gb300 import _lib
+    from xcape_gb300 import synthetic as S
+    L = _lib.lib()
+    a = S.srh_c2()
+    n2 = 1024 * 1024
+    d = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in a]
+    srm, slm = (torch.empty(n2, dtype=torch.float64, device="cuda") for _ in range(2))
+    rm, lm, mean = (torch.empty(2 * n2, dtype=torch.float32, device="cuda") for _ in range(3))
+    s = torch.cuda.current_stream().cuda_stream
+
+    def step():
+        for depth in (1000.0, 3000.0):
+            _lib.check(L.xc_calc_srh(1, *[x.data_ptr() for x in d], _lib.XC_F32, None, depth, 2.0,
+                                     50, n2, srm.data_ptr(), slm.data_ptr(), rm.data_ptr(),
+                                     lm.data_ptr(), mean.data_ptr(), s))
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    hbm_peak, kind = measured_peaks()
+    bytes_launch = n2 * (5 * 50 * 4 + 5 * 4 + 2 * 8 + 6 * 4)
+    ach = bytes_launch / (ms / 2 / 1e3) / 1e9
+    print(json.dumps({"metric": SRH_METRIC, "value": n2 / (ms / 1e3), "unit": "columns/s",
+                      "n_gpus": 1, "steps": args.steps, "ms_per_step": ms, "dtype": "f64+f32",
+                      "higher_is_better": True, "data": "synthetic",
+                      "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak,
+                                   "unit": "GB/s", "frac": ach / hbm_peak, "peak_kind": kind},
+                      "clocks": clk.summary()}), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.workload == "srh":
+        return run_srh(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,214 @@
+/*
+ * xcape_gb300.h -- C ABI of libxcape_gb300.so, the GB300 (sm_103a) column
+ * kernels behind xcape's calc_cape / calc_srh.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (XC_OK == 0).  No entry point aborts the process:
+ * where the reference Fortran executes `stop` (unknown source / adiabat) the
+ * call returns XC_ERR_INVALID instead.
+ *
+ * Array layout is the one the reference's f2py interfaces bind: a Fortran
+ * (nk, n2) array, which is the C array [n2][nk] -- the levels of one column
+ * are contiguous, exactly as a user's (..., nlev) numpy array is laid out.
+ * Outputs declared (2, n2) in Fortran are [n2][2] here.
+ *
+ * Two families of entry points:
+ *   xc_*          DEVICE pointers; asynchronous on `stream` (a cudaStream_t,
+ *                 NULL = the legacy default stream).  Nothing is allocated.
+ *   xc_*_host     HOST pointers (pageable or pinned); the library stages the
+ *                 arrays through a device workspace that it owns (grown on
+ *                 demand, released by xc_release_workspace), runs the same
+ *                 kernels and returns when the outputs are back in host memory.
+ *
+ * Input element type: `dtype` selects XC_F32 or XC_F64 for every
+ * floating-point input of a call.  The CAPE kernels round f64 inputs to f32
+ * on load, which is what f2py does when it passes a float64 array to a
+ * `real` argument.
+ */
+#ifndef XCAPE_GB300_H
+#define XCAPE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes. */
+#define XC_OK 0
+#define XC_ERR_INVALID 1  /* bad argument: sizes, option codes, dtype, NULL   */
+#define XC_ERR_CUDA 2     /* a CUDA runtime call failed (see xc_last_error)    */
+#define XC_ERR_NOMEM 3    /* device workspace could not be allocated           */
+#define XC_ERR_NODEVICE 4 /* no CUDA device                                    */
+
+/* Input element types. */
+#define XC_F32 0
+#define XC_F64 1
+
+/* Option codes, identical to the reference's integer encodings
+ * (src/xcape/core.py:302-311). */
+#define XC_SOURCE_SURFACE 1
+#define XC_SOURCE_MOST_UNSTABLE 2
+#define XC_SOURCE_MIXED_LAYER 3
+#define XC_ADIABAT_PSEUDO_LIQUID 1
+#define XC_ADIABAT_REVERSIBLE_LIQUID 2
+#define XC_ADIABAT_PSEUDO_ICE 3
+#define XC_ADIABAT_REVERSIBLE_ICE 4
+
+/* Per-column status bits (optional `status` output). */
+#define XC_COL_NOCONV 1   /* moist-adiabat iteration passed 100 steps: cape=cin=0 */
+#define XC_COL_BADSTART 2 /* start_3d outside 1..nk: outputs zero              */
+
+/* First guess of the moist-adiabat iteration (xc_loopcape_*_ex). */
+#define XC_GUESS_PLAIN 0   /* thlast = th1, exactly as the reference            */
+#define XC_GUESS_LEARNED 1 /* the loaded guess network (xc_guess_load)          */
+
+/* Largest supported level count of one column (without the surface). */
+#define XC_MAX_LEVELS 4096
+
+/* ---------------------------------------------------------------------- */
+/* CAPE / CIN                                                             */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces loopcape_ml: CAPE_CODE_model_lev.pyf:6-24,
+ * CAPE_CODE_model_lev.f90:4-91 (+ getcape_ml :97-564).
+ * p3d/t3d/td3d [n2][nk] (hPa, degC, degC), ps/ts/tds [n2].
+ * Outputs [n2]: cape, cin (J/kg), mulvl (1-based level of the most-unstable
+ * parcel, surface = 1; -999999 unless source == 2), z_out (height of the last
+ * level reached, m).  status may be NULL. */
+int xc_loopcape_ml(const void *p3d, const void *t3d, const void *td3d, const void *ps,
+                   const void *ts, const void *tds, int dtype, float pinc, int source,
+                   float ml_depth, int adiabat, int nk, int n2, float *cape, float *cin,
+                   int *mulvl, float *z_out, int *status, void *stream);
+
+/* Replaces loopcape_pl1d: CAPE_CODE_pressure_lev.pyf:26-45 (the routine named
+ * loopcape_pl1d there), CAPE_CODE_pressure_lev.f90:88-169.  p1d [nk] is shared
+ * by all columns.  start_3d [n2] is the 1-based first level at or above the
+ * surface; when start_3d is NULL it is derived in the kernel with the
+ * reference's rule (src/xcape/core.py:286-289: masked argmin of ps - p). */
+int xc_loopcape_pl1d(const void *t3d, const void *td3d, const void *p1d, const void *ps,
+                     const void *ts, const void *tds, int dtype, float pinc, int source,
+                     float ml_depth, int adiabat, const int *start_3d, int nk, int n2,
+                     float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                     void *stream);
+
+/* Replaces loopcape_pl: CAPE_CODE_pressure_lev.pyf:6-25,
+ * CAPE_CODE_pressure_lev.f90:4-84 (per-column pressure, per-column start;
+ * start_3d must not be NULL). */
+int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const void *ps,
+                   const void *ts, const void *tds, int dtype, float pinc, int source,
+                   float ml_depth, int adiabat, const int *start_3d, int nk, int n2,
+                   float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                   void *stream);
+
+/* Generalised CAPE entry point used by the Python layer: one call for the
+ * three grid kinds.  grid: 1 = sigma/model (p3d per column), 2 = pressure
+ * with shared p1d (start_3d optional), 3 = pressure with per-column p3d
+ * (start_3d required).  guess: XC_GUESS_*.  counters (nullable, 2 x int64 on
+ * the device) receives the total sub-steps and iterations, atomically added. */
+int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                   const void *ts, const void *tds, int dtype, float pinc, int source,
+                   float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
+                   float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                   long long *counters, void *stream);
+
+/* Host-pointer form of xc_loopcape_ex (see the family note above). */
+int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
+                        const void *ps, const void *ts, const void *tds, int dtype, float pinc,
+                        int source, float ml_depth, int adiabat, const int *start_3d, int nk,
+                        int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
+                        int *status, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Storm-relative helicity                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Fused replacement of src/xcape/core.py:_calc_srh_numpy :473-542, i.e. the
+ * chain loop_stdheight_{ml,pl1d} -> bunkers_loop_{ml,pl} -> loop_sreh_{ml,pl}
+ * in one pass per column.  grid: 1 = sigma/model (p [n2][nk]), 2 = pressure
+ * with shared p [nk] (start_3d optional as for xc_loopcape_pl1d).
+ * depth (m) is `top` of loop_sreh; aglh0 is the surface height (2 m in the
+ * reference, core.py:519).  srh_rm/srh_lm [n2] (f64, like loop_sreh);
+ * rm/lm/mean6 [n2][2] (f32, like bunkers_loop) may be NULL. */
+int xc_calc_srh(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
+                const void *v3d, const void *ps, const void *ts, const void *tds,
+                const void *us, const void *vs, int dtype, const int *start_3d, double depth,
+                double aglh0, int nk, int n2, double *srh_rm, double *srh_lm, float *rm,
+                float *lm, float *mean6, void *stream);
+
+/* Host-pointer form of xc_calc_srh. */
+int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
+                     const void *u3d, const void *v3d, const void *ps, const void *ts,
+                     const void *tds, const void *us, const void *vs, int dtype,
+                     const int *start_3d, double depth, double aglh0, int nk, int n2,
+                     double *srh_rm, double *srh_lm, float *rm, float *lm, float *mean6,
+                     void *stream);
+
+/* Replaces loop_stdheight_ml: stdheight_2D_model_lev.pyf:6-19,
+ * stdheight_2D_model_lev.f90:4-34 (+ stdheight_ml :74-160).  All f64. */
+int xc_loop_stdheight_ml(const double *P, const double *T, const double *Td, const double *Ps,
+                         const double *Ts, const double *Tds, const double *Hin, int NK, int NX,
+                         double *H, double *Hs, void *stream);
+
+/* Replaces loop_stdheight_pl1d: stdheight_2D_pressure_lev.pyf:20-33,
+ * stdheight_2D_pressure_lev.f90:65-93.  Levels below start get -999999. */
+int xc_loop_stdheight_pl1d(const double *T, const double *Td, const double *P, const double *Ps,
+                           const double *Ts, const double *Tds, const double *Hin,
+                           const int *start_3d, int NK, int NX, double *H, double *Hs,
+                           void *stream);
+
+/* Replaces loop_stdheight_pl: stdheight_2D_pressure_lev.pyf:6-19,
+ * stdheight_2D_pressure_lev.f90:5-47. */
+int xc_loop_stdheight_pl(const double *P, const double *T, const double *Td, const double *Ps,
+                         const double *Ts, const double *Tds, const double *Hin,
+                         const int *start_3d, int NK, int NX, double *H, double *Hs,
+                         void *stream);
+
+/* Replaces bunkers_loop_ml: Bunkers_model_lev.pyf:8-21,
+ * Bunkers_model_lev.f90:4-69 (+ bunkers_calc_ml :75-180, DINTERP2DZ :188-236).
+ * All f32; RM/LM/Mean6kmwind [n2][2]. */
+int xc_bunkers_loop_ml(const float *U3d, const float *V3d, const float *AGLH3d, const float *Us,
+                       const float *Vs, const float *AGLHs, int nk, int n2, float *RM, float *LM,
+                       float *Mean6kmwind, void *stream);
+
+/* Replaces bunkers_loop_pl: Bunkers_pressure_lev.pyf:7-21,
+ * Bunkers_pressure_lev.f90:4-78. */
+int xc_bunkers_loop_pl(const float *U3d, const float *V3d, const float *AGLH3d, const float *Us,
+                       const float *Vs, const float *AGLHs, const int *start_3d, int nk, int n2,
+                       float *RM, float *LM, float *Mean6kmwind, void *stream);
+
+/* Replaces loop_sreh_ml: SREH_model_lev.pyf:6-23, SREH_model_lev.f90:4-55
+ * (+ DCALRELHL_ml :61-118, INTERP1 :123-129).  All f64. */
+int xc_loop_sreh_ml(const double *u, const double *v, const double *aglh, const double *us,
+                    const double *vs, const double *aglhs, const double *cu_rm,
+                    const double *cv_rm, const double *cu_lm, const double *cv_lm, double top,
+                    int nk, int n2, double *sreh_rm, double *sreh_lm, void *stream);
+
+/* Replaces loop_sreh_pl: SREH_pressure_lev.pyf:6-24, SREH_pressure_lev.f90:4-63. */
+int xc_loop_sreh_pl(const double *u, const double *v, const double *aglh, const double *us,
+                    const double *vs, const double *aglhs, const double *cu_rm,
+                    const double *cv_rm, const double *cu_lm, const double *cv_lm, double top,
+                    const int *start_3d, int nk, int n2, double *sreh_rm, double *sreh_lm,
+                    void *stream);
+
+/* Derives start_3d [n2] for a shared 1-D pressure axis with the reference's
+ * rule (core.py:286-289).  No counterpart entry point in the reference: there
+ * it is host numpy code. */
+int xc_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, int n2, int *start_3d,
+                    void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Library services                                                       */
+/* ---------------------------------------------------------------------- */
+
+/* Frees the device workspace of the *_host entry points (all devices). */
+int xc_release_workspace(void);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char *xc_last_error(void);
+
+/* Library version string. */
+const char *xc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XCAPE_GB300_H */

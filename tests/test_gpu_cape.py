@@ -1,0 +1,260 @@
+"""GPU parity tests of the CAPE/CIN kernels against the CPU oracle and the
+reference's golden vectors.
+
+Mirrors test/test_core.py:68-170 of the reference (sigma and pressure golden
+tests) and extends them to every source x adiabat on seeded synthetic
+soundings, the three grid kinds, the ragged pressure-level start, edge cases
+and the full 1,038,240-column pressure-level workload (through size-
+independent properties plus a random sample checked column by column).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import xcape_gb300 as X
+from xcape_gb300 import _lib
+from xcape_gb300 import synthetic as S
+
+from gpu_util import (ADIABATS, SOURCES, cape_device, compare_cape, thetae_f64, to_dev,
+                      torch_cuda)
+
+pytestmark = pytest.mark.gpu
+
+SIGMA_GOLDEN = [
+    ("surface", 100, ("SB_CAPE_pinc100", "SB_CIN_pinc100")),
+    ("mixed-layer", 1000, ("ML_CAPE_pinc1000_mldepth500", "ML_CIN_pinc1000_mldepth500")),
+    ("most-unstable", 100, ("MU_CAPE_pinc100", "MU_CIN_pinc100", "MU_lv_pinc100", "MU_z_pinc100")),
+]
+PRESSURE_GOLDEN = [
+    ("surface", ("sfc_capesp500", "sfc_cinsp500")),
+    ("mixed-layer", ("sfc_capeml300p500", "sfc_cinml300p500")),
+    ("most-unstable", ("sfc_capemup500", "sfc_cinmup500")),
+]
+
+
+def _close(got, want):
+    np.testing.assert_almost_equal(got, want, 0)
+    w = np.asarray(want, np.float64)
+    assert np.all(np.abs(np.asarray(got, np.float64) - w) <= np.maximum(1.0, 1e-3 * np.abs(w)))
+
+
+@pytest.mark.parametrize("use_torch", [False, True])
+@pytest.mark.parametrize("source,pinc,keys", SIGMA_GOLDEN)
+def test_cape_sigma_golden(soundings, source, pinc, keys, use_torch):
+    s = soundings
+    P, T, TD = s["pressure"], s["temperature"], s["dewpoint"]
+    args = (P[:, 1:], T[:, 1:], TD[:, 1:], P[:, 0], T[:, 0], TD[:, 0])
+    if use_torch:
+        args = to_dev(*args)
+    res = X.calc_cape(*args, source=source, ml_depth=500.0, adiabat="pseudo-liquid", pinc=pinc,
+                      method="cuda", vertical_lev="sigma")
+    assert len(res) == len(keys)
+    res = [r.cpu().numpy() if use_torch else r for r in res]
+    for got, key in zip(res, keys):
+        if key.startswith("MU_lv"):
+            assert got.dtype == np.int32
+            np.testing.assert_array_equal(got, s[key].astype(np.int32))
+        elif key.startswith("MU_z"):
+            np.testing.assert_almost_equal(got, s[key], 0)
+        else:
+            assert got.dtype == np.float32
+            _close(got, s[key])
+
+
+@pytest.mark.parametrize("use_torch", [False, True])
+@pytest.mark.parametrize("source,keys", PRESSURE_GOLDEN)
+def test_cape_pressure_golden(era5, source, keys, use_torch):
+    e = era5
+    args = (e["lev_level"], e["lev_t"], e["lev_td"], e["sfc_p"], e["sfc_t"], e["sfc_td"])
+    if use_torch:
+        args = to_dev(*args)
+    res = X.calc_cape(*args, source=source, ml_depth=300, adiabat="pseudo-liquid", pinc=500,
+                      method="cuda", vertical_lev="pressure")
+    res = [r.cpu().numpy() if use_torch else r for r in res]
+    for got, key in zip(res, keys):
+        _close(got, e[key])
+
+
+def _oracle_cols(grid, p, t, td, ps, ts, tds, source, adiabat, pinc, ml_depth, start=None):
+    n2 = int(np.prod(np.shape(t)[:-1]))
+    nk = np.shape(t)[-1]
+    t2, td2 = np.reshape(t, (n2, nk)), np.reshape(td, (n2, nk))
+    sf = [np.ravel(a) for a in (ps, ts, tds)]
+    src, adi = SOURCES[source], ADIABATS[adiabat]
+    if grid == 1:
+        return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi,
+                          stats=True)
+    if grid == 2:
+        st = O.pres_lev_pos(p, sf[0]) if start is None else start
+        return O.loopcape(np.ravel(p), t2, td2, *sf, pinc, src, ml_depth, adi, start=st,
+                          p_is_1d=True, stats=True)
+    return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, start=start,
+                      stats=True)
+
+
+def _check_mulvl(got, want, p, t, td, ps, ts, tds, grid, start=None):
+    same = got["mulvl"] == want["mulvl"]
+    flip = ((got["status"] ^ want["status"]) & _lib.COL_NOCONV) != 0
+    bad = np.nonzero(~same & ~flip)[0]
+    if bad.size == 0:
+        return
+    # Near-ties: theta-e of the two chosen levels within 1e-3 K.
+    nk = np.shape(t)[-1]
+    t2, td2 = np.reshape(t, (-1, nk)), np.reshape(td, (-1, nk))
+    for c in bad:
+        def level(j):
+            if j == 1:
+                return np.ravel(ps)[c], np.ravel(ts)[c], np.ravel(tds)[c]
+            m = (start[c] if start is not None else 1) - 2 + j
+            pj = p[m] if grid == 2 else np.reshape(p, (-1, nk))[c, m]
+            return pj, t2[c, m], td2[c, m]
+        a = thetae_f64(*level(got["mulvl"][c]))
+        b = thetae_f64(*level(want["mulvl"][c]))
+        assert abs(a - b) < 1e-3, f"column {c}: MU level {got['mulvl'][c]} vs {want['mulvl'][c]}"
+    assert bad.size <= max(2, 1e-3 * same.size)
+
+
+@pytest.mark.parametrize("adiabat", list(ADIABATS))
+@pytest.mark.parametrize("source", list(SOURCES))
+def test_cape_sigma_synthetic_vs_oracle(source, adiabat):
+    """64x64 columns x 40 sigma levels, float64 input (the small CPU case)."""
+    p, t, td, ps, ts, tds = S.sigma_c0()
+    got = cape_device(1, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0)
+    want = _oracle_cols(1, p, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0)
+    compare_cape(got, want, what=f"sigma {source} {adiabat}")
+    if source == "most-unstable":
+        _check_mulvl(got, want, p, t, td, ps, ts, tds, 1)
+    else:
+        assert np.all(got["mulvl"][ts.ravel() > 0] == -999999)
+
+
+@pytest.mark.parametrize("adiabat", ["pseudo-liquid", "reversible-ice"])
+@pytest.mark.parametrize("source", list(SOURCES))
+def test_cape_pressure_synthetic_vs_oracle(source, adiabat):
+    """Ragged pressure levels: 128x128 columns of the 1000..100 hPa workload,
+    start level derived on the GPU."""
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(128, 128))
+    got = cape_device(2, plev, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0)
+    want = _oracle_cols(2, plev, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0)
+    compare_cape(got, want, what=f"pressure {source} {adiabat}")
+    if source == "most-unstable":
+        st = O.pres_lev_pos(plev, ps.ravel())
+        _check_mulvl(got, want, plev, t, td, ps, ts, tds, 2, start=st)
+
+
+def test_cape_pressure_3d_grid_vs_oracle():
+    """loopcape_pl: per-column pressure plus a given start level."""
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(32, 64))
+    n2 = 32 * 64
+    p3 = np.broadcast_to(plev, (n2, plev.size)).copy() * np.float32(1.0)
+    p3 += np.random.default_rng(3).normal(0, 0.5, p3.shape).astype(np.float32)
+    st = O.pres_lev_pos(plev, ps.ravel())
+    got = cape_device(3, p3, t, td, ps, ts, tds, "mixed-layer", "pseudo-liquid", start=st)
+    want = _oracle_cols(3, p3, t, td, ps, ts, tds, "mixed-layer", "pseudo-liquid", 500.0, 500.0,
+                        start=st)
+    compare_cape(got, want, what="pressure 3-D")
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_pres_lev_pos_kernel_matches_numpy(dtype):
+    torch = torch_cuda()
+    rng = np.random.default_rng(11)
+    plev = np.array([1000, 975, 950, 950, 900, 850, 700, 500, 300, 100], dtype)
+    ps = rng.uniform(800, 1050, 4096).astype(dtype)
+    ps[:4] = [1000, 950, 899.99, 80]  # exact hit, tie, between, every level masked
+    ps[4] = np.nan
+    want = O.pres_lev_pos(plev, ps)
+    P, PS = to_dev(plev, ps)
+    st = torch.empty(ps.size, dtype=torch.int32, device="cuda")
+    _lib.call("xc_pres_lev_pos", P.data_ptr(), PS.data_ptr(),
+              _lib.XC_F64 if dtype == np.float64 else _lib.XC_F32, plev.size, ps.size,
+              st.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(st.cpu().numpy(), want)
+
+
+def test_cape_edge_cases():
+    """Cold surface gate, short columns, MU above 500 hPa, single level,
+    bad start, NaN input, one column."""
+    p, t, td, ps, ts, tds = (np.array(a) for a in S.sigma_c0(shape=(1, 12), nlev=40, seed=4))
+    p, t, td = p[0], t[0], td[0]
+    ps, ts, tds = ps[0], ts[0], tds[0]
+    ts[0] = -1.0          # ts <= 0: zeros, MU level 0 (CAPE_CODE_model_lev.f90:77-88)
+    ts[1] = 0.0
+    p[2] *= 0.45          # whole column above 500 hPa
+    ps[2] *= 0.45
+    t[3, :] = np.nan      # NaN column must finish with some status, not fault
+    for source in SOURCES:
+        got = cape_device(1, p, t, td, ps, ts, tds, source, "pseudo-liquid")
+        want = _oracle_cols(1, p, t, td, ps, ts, tds, source, "pseudo-liquid", 500.0, 500.0)
+        ok = np.ones(12, bool)
+        ok[3] = False
+        for key in ("cape", "cin", "mulvl"):
+            np.testing.assert_allclose(got[key][ok], want[key][ok], rtol=1e-3, atol=1.0)
+        assert got["cape"][0] == 0 and got["mulvl"][0] == 0 and got["z_out"][0] == 0
+        assert got["cape"][1] == 0 and got["mulvl"][1] == 0
+        if source == "most-unstable":
+            assert got["mulvl"][2] == -999999
+    # mixed layer deeper than the column: ascent never starts, sentinels stay
+    got = cape_device(1, p[4:6, :2], t[4:6, :2], td[4:6, :2], ps[4:6], ts[4:6], tds[4:6],
+                      "mixed-layer", "pseudo-liquid", ml_depth=5000.0)
+    want = _oracle_cols(1, p[4:6, :2], t[4:6, :2], td[4:6, :2], ps[4:6], ts[4:6], tds[4:6],
+                        "mixed-layer", "pseudo-liquid", 500.0, 5000.0)
+    np.testing.assert_array_equal(got["cape"], want["cape"])
+    np.testing.assert_array_equal(got["z_out"], want["z_out"])
+    assert np.all(got["z_out"] == -999999.0)
+    # a single 3-D level
+    got = cape_device(1, p[:, :1], t[:, :1], td[:, :1], ps, ts, tds, "surface", "pseudo-liquid")
+    want = _oracle_cols(1, p[:, :1], t[:, :1], td[:, :1], ps, ts, tds, "surface",
+                        "pseudo-liquid", 500.0, 500.0)
+    np.testing.assert_allclose(got["cape"][ok], want["cape"][ok], atol=1.0)
+    # start outside 1..nk on the 3-D pressure grid: flagged, zeros
+    st = np.array([0, 41] + [1] * 10, np.int32)
+    got = cape_device(3, p, t, td, ps, ts, tds, "surface", "pseudo-liquid", start=st)
+    assert got["status"][0] & _lib.COL_BADSTART and got["status"][1] & _lib.COL_BADSTART
+    assert got["cape"][0] == 0 and got["cape"][1] == 0
+
+
+def test_host_and_device_paths_agree():
+    torch = torch_cuda()
+    p, t, td, ps, ts, tds = S.pressure_c1(shape=(48, 48))
+    host = X.calc_cape(p, t, td, ps, ts, tds, source="most-unstable", vertical_lev="pressure")
+    dev = X.calc_cape(*to_dev(p, t, td, ps, ts, tds), source="most-unstable",
+                      vertical_lev="pressure")
+    torch.cuda.synchronize()
+    for h, d in zip(host, dev):
+        np.testing.assert_array_equal(h, d.cpu().numpy())
+        assert h.shape == (48, 48)
+
+
+def test_work_counters_match_oracle():
+    p, t, td, ps, ts, tds = S.sigma_c0(shape=(16, 64))
+    got = cape_device(1, p, t, td, ps, ts, tds, "surface", "pseudo-liquid", counters=True)
+    want = _oracle_cols(1, p, t, td, ps, ts, tds, "surface", "pseudo-liquid", 500.0, 500.0)
+    assert got["nsub_total"] == int(want["nsub"].sum())
+    assert abs(got["niter_total"] - int(want["niter"].sum())) <= 0.01 * want["niter"].sum()
+
+
+def test_cape_full_size_pressure_workload():
+    """1,038,240 columns x 37 levels (the benchmark workload): determinism,
+    column-permutation invariance, and a random sample against the oracle."""
+    torch = torch_cuda()
+    plev, t, td, ps, ts, tds = S.pressure_c1()
+    n2 = ps.size
+    a = cape_device(2, plev, t, td, ps, ts, tds, "most-unstable", "pseudo-liquid")
+    b = cape_device(2, plev, t, td, ps, ts, tds, "most-unstable", "pseudo-liquid")
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+    perm = np.random.default_rng(5).permutation(n2)
+    t2, td2 = t.reshape(n2, -1)[perm], td.reshape(n2, -1)[perm]
+    c = cape_device(2, plev, t2, td2, ps.ravel()[perm], ts.ravel()[perm], tds.ravel()[perm],
+                    "most-unstable", "pseudo-liquid")
+    for k in a:
+        np.testing.assert_array_equal(a[k][perm], c[k])
+    idx = np.sort(np.random.default_rng(6).choice(n2, 4096, replace=False))
+    want = _oracle_cols(2, plev, t.reshape(n2, -1)[idx], td.reshape(n2, -1)[idx],
+                        ps.ravel()[idx], ts.ravel()[idx], tds.ravel()[idx], "most-unstable",
+                        "pseudo-liquid", 500.0, 500.0)
+    compare_cape({k: v[idx] for k, v in a.items()}, want, what="full-size sample")
+    assert np.all(a["cape"] >= 0) and np.all(a["cin"] >= 0)
+    del torch

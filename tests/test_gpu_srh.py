@@ -1,0 +1,201 @@
+"""GPU parity tests of storm-relative helicity and its stages.
+
+Mirrors test/test_core.py:173-286 of the reference (sigma and pressure SRH
+goldens, decimal=5) and checks the Bunkers vectors, the individual stage
+entry points (stdheight, Bunkers, SREH) and seeded synthetic workloads
+against the CPU oracle.  SRH is double precision in the reference and here,
+so the bar is 1e-5 m^2/s^2 on the goldens and a relative 1e-9 on synthetic
+columns; the FP32 Bunkers vectors must agree to 1e-4 m/s.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import xcape_gb300 as X
+from xcape_gb300 import _lib
+from xcape_gb300 import synthetic as S
+
+from gpu_util import to_dev, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+
+def _snd_args(s):
+    P, T, TD, U, V = s["pressure"], s["temperature"], s["dewpoint"], s["u_wind_ms"], s["v_wind_ms"]
+    return (P[:, 1:], T[:, 1:], TD[:, 1:], U[:, 1:], V[:, 1:], P[:, 0], T[:, 0], TD[:, 0],
+            U[:, 0], V[:, 0])
+
+
+def _era_args(e):
+    return (e["lev_level"], e["lev_t"], e["lev_td"], e["lev_u"], e["lev_v"], e["sfc_p"],
+            e["sfc_t"], e["sfc_td"], e["sfc_u"], e["sfc_v"])
+
+
+def _check_all(got, want, srh_atol):
+    np.testing.assert_allclose(got[0], want[0], rtol=1e-9, atol=srh_atol)
+    np.testing.assert_allclose(got[1], want[1], rtol=1e-9, atol=srh_atol)
+    for g, w in zip(got[2:], want[2:]):
+        assert g.dtype == np.float32
+        np.testing.assert_allclose(g, w, rtol=0, atol=1e-4)
+
+
+@pytest.mark.parametrize("use_torch", [False, True])
+@pytest.mark.parametrize("output_var,n", [("srh", 2), ("all", 8)])
+def test_srh_sigma_golden(soundings, output_var, n, use_torch):
+    s = soundings
+    args = _snd_args(s)
+    if use_torch:
+        args = to_dev(*args)
+    res = X.calc_srh(*args, depth=3000, vertical_lev="sigma", output_var=output_var)
+    assert len(res) == n
+    res = [r.cpu().numpy() if use_torch else r for r in res]
+    np.testing.assert_almost_equal(res[0], s["SRH03_model_lev_rm"], 5)
+    np.testing.assert_almost_equal(res[1], s["SRH03_model_lev_lm"], 5)
+    if output_var == "all":
+        want = O.calc_srh(*_snd_args(s), depth=3000, vertical_lev="sigma", output_var="all")
+        _check_all(res, want, 1e-6)
+
+
+@pytest.mark.parametrize("output_var,n", [("srh", 2), ("all", 8)])
+def test_srh_pressure_golden(era5, output_var, n):
+    e = era5
+    res = X.calc_srh(*_era_args(e), depth=3000, vertical_lev="pressure", output_var=output_var)
+    assert len(res) == n
+    np.testing.assert_almost_equal(res[0], e["sfc_srh_rm"], 5)
+    np.testing.assert_almost_equal(res[1], e["sfc_srh_lm"], 5)
+    if output_var == "all":
+        want = O.calc_srh(*_era_args(e), depth=3000, vertical_lev="pressure", output_var="all")
+        _check_all(res, want, 1e-6)
+
+
+@pytest.mark.parametrize("depth", [1000, 3000])
+def test_srh_model_levels_synthetic(depth):
+    """256x256 columns x 50 model levels, float32, veering jet
+    (vertical_lev='model' aliases 'sigma')."""
+    args = S.srh_c2(shape=(256, 256))
+    got = X.calc_srh(*args, depth=depth, vertical_lev="model", output_var="all")
+    want = O.calc_srh(*args, depth=depth, vertical_lev="model", output_var="all")
+    _check_all(got, want, 1e-6)
+    assert np.mean(got[0]) > 0  # veering hodograph: positive right-mover helicity
+
+
+def test_srh_pressure_synthetic():
+    args = S.pressure_srh(shape=(96, 96))
+    got = X.calc_srh(*args, depth=3000, vertical_lev="pressure", output_var="all")
+    want = O.calc_srh(*args, depth=3000, vertical_lev="pressure", output_var="all")
+    _check_all(got, want, 1e-6)
+
+
+def test_srh_decreasing_height_columns():
+    """Columns whose heights fall with level index take DINTERP2DZ's other
+    scan rule (Bunkers_model_lev.f90:210-215)."""
+    p, t, td, u, v, ps, ts, tds, us, vs = (np.array(a, np.float64) for a in
+                                           S.srh_c2(shape=(4, 8), nlev=50, seed=9))
+    p = p[..., ::-1].copy()
+    t = t[..., ::-1].copy()
+    td = td[..., ::-1].copy()
+    ps = p[..., 0] * 1.2
+    got = X.calc_srh(p, t, td, u, v, ps, ts, tds, us, vs, depth=3000, output_var="all")
+    want = O.calc_srh(p, t, td, u, v, ps, ts, tds, us, vs, depth=3000, output_var="all")
+    _check_all(got, want, 1e-6)
+
+
+def test_srh_stage_entry_points(soundings):
+    """loop_stdheight_ml, bunkers_loop_ml and loop_sreh_ml bound one by one."""
+    torch = torch_cuda()
+    P, T, TD, U, V, ps, ts, tds, us, vs = (np.ascontiguousarray(a, np.float64)
+                                           for a in _snd_args(soundings))
+    n2, nk = T.shape
+    hin = np.full(n2, 2.0)
+    H_w, Hs_w = O.loop_stdheight(P, T, TD, ps, ts, tds, hin)
+    d = to_dev(P, T, TD, ps, ts, tds, hin)
+    H = torch.empty((n2, nk), dtype=torch.float64, device="cuda")
+    Hs = torch.empty(n2, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    _lib.call("xc_loop_stdheight_ml", *[x.data_ptr() for x in d], nk, n2, H.data_ptr(),
+              Hs.data_ptr(), st)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(H.cpu().numpy(), H_w, rtol=1e-12)
+    np.testing.assert_array_equal(Hs.cpu().numpy(), Hs_w)
+
+    f32 = [np.ascontiguousarray(a, np.float32) for a in (U, V, H_w, us, vs, Hs_w)]
+    rm_w, lm_w, mean_w = O.bunkers_loop(*f32)
+    d = to_dev(*f32)
+    RM, LM, MEAN = (torch.empty((n2, 2), dtype=torch.float32, device="cuda") for _ in range(3))
+    _lib.call("xc_bunkers_loop_ml", *[x.data_ptr() for x in d], nk, n2, RM.data_ptr(),
+              LM.data_ptr(), MEAN.data_ptr(), st)
+    torch.cuda.synchronize()
+    for g, w in ((RM, rm_w), (LM, lm_w), (MEAN, mean_w)):
+        np.testing.assert_allclose(g.cpu().numpy(), w, rtol=0, atol=1e-5)
+
+    srm_w, slm_w = O.loop_sreh(U, V, H_w, us, vs, Hs_w, rm_w[:, 0], rm_w[:, 1], lm_w[:, 0],
+                               lm_w[:, 1], 3000.0)
+    d = to_dev(U, V, H_w, us, vs, Hs_w, *(np.ascontiguousarray(a, np.float64) for a in
+                                          (rm_w[:, 0], rm_w[:, 1], lm_w[:, 0], lm_w[:, 1])))
+    SRM = torch.empty(n2, dtype=torch.float64, device="cuda")
+    SLM = torch.empty_like(SRM)
+    _lib.call("xc_loop_sreh_ml", *[x.data_ptr() for x in d], 3000.0, nk, n2, SRM.data_ptr(),
+              SLM.data_ptr(), st)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(SRM.cpu().numpy(), srm_w, rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(SLM.cpu().numpy(), slm_w, rtol=1e-12, atol=1e-9)
+
+
+def test_srh_pressure_stage_entry_points(era5):
+    """loop_stdheight_pl1d, bunkers_loop_pl and loop_sreh_pl with start_3d."""
+    torch = torch_cuda()
+    e = era5
+    plev = np.ascontiguousarray(e["lev_level"], np.float64)
+    T, TD, U, V = (np.ascontiguousarray(e[k], np.float64) for k in ("lev_t", "lev_td", "lev_u",
+                                                                      "lev_v"))
+    ps, ts, tds, us, vs = (np.ascontiguousarray(e[k], np.float64) for k in
+                           ("sfc_p", "sfc_t", "sfc_td", "sfc_u", "sfc_v"))
+    n2, nk = T.shape
+    start = O.pres_lev_pos(plev, ps)
+    hin = np.full(n2, 2.0)
+    H_w, Hs_w = O.loop_stdheight(plev, T, TD, ps, ts, tds, hin, start=start, p_is_1d=True)
+    st = torch.cuda.current_stream().cuda_stream
+    d = to_dev(T, TD, plev, ps, ts, tds, hin)
+    S_ = to_dev(start)[0]
+    H = torch.empty((n2, nk), dtype=torch.float64, device="cuda")
+    Hs = torch.empty(n2, dtype=torch.float64, device="cuda")
+    _lib.call("xc_loop_stdheight_pl1d", *[x.data_ptr() for x in d], S_.data_ptr(), nk, n2,
+              H.data_ptr(), Hs.data_ptr(), st)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(H.cpu().numpy(), H_w, rtol=1e-12)
+    f32 = [np.ascontiguousarray(a, np.float32) for a in (U, V, H_w, us, vs, Hs_w)]
+    rm_w, lm_w, mean_w = O.bunkers_loop(*f32, start=start)
+    d = to_dev(*f32)
+    RM, LM, MEAN = (torch.empty((n2, 2), dtype=torch.float32, device="cuda") for _ in range(3))
+    _lib.call("xc_bunkers_loop_pl", *[x.data_ptr() for x in d], S_.data_ptr(), nk, n2,
+              RM.data_ptr(), LM.data_ptr(), MEAN.data_ptr(), st)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(RM.cpu().numpy(), rm_w, atol=1e-5)
+    srm_w, _ = O.loop_sreh(U, V, H_w, us, vs, Hs_w, rm_w[:, 0], rm_w[:, 1], lm_w[:, 0],
+                           lm_w[:, 1], 3000.0, start=start)
+    d = to_dev(U, V, H_w, us, vs, Hs_w, *(np.ascontiguousarray(a, np.float64) for a in
+                                          (rm_w[:, 0], rm_w[:, 1], lm_w[:, 0], lm_w[:, 1])))
+    SRM = torch.empty(n2, dtype=torch.float64, device="cuda")
+    SLM = torch.empty_like(SRM)
+    _lib.call("xc_loop_sreh_pl", *[x.data_ptr() for x in d], 3000.0, S_.data_ptr(), nk, n2,
+              SRM.data_ptr(), SLM.data_ptr(), st)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(SRM.cpu().numpy(), srm_w, rtol=1e-12, atol=1e-9)
+
+
+def test_srh_full_size_workload():
+    """1024x1024 columns x 50 levels: determinism and a sample vs the oracle."""
+    torch = torch_cuda()
+    args = S.srh_c2()
+    dev = to_dev(*args)
+    a = X.calc_srh(*dev, depth=3000, vertical_lev="model", output_var="all")
+    b = X.calc_srh(*dev, depth=3000, vertical_lev="model", output_var="all")
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    n2 = 1024 * 1024
+    idx = np.sort(np.random.default_rng(8).choice(n2, 8192, replace=False))
+    sub = [np.reshape(x, (n2, -1))[idx] for x in args[:5]] + [np.ravel(x)[idx] for x in args[5:]]
+    want = O.calc_srh(*sub, depth=3000, vertical_lev="model", output_var="all")
+    got = [x.reshape(-1).cpu().numpy()[idx] for x in a]
+    _check_all(got, want, 1e-6)

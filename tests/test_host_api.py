@@ -1,0 +1,148 @@
+"""CPU tests of the host side: shapes, argument errors, and the C ABI surface.
+
+The shape tests mirror the reference's test_calc_cape_shape_3d
+(test/test_core.py:39-58), which drives the 'dummy' backend.  The ABI tests
+load libxcape_gb300.so and check that every entry point declared in
+include/xcape_gb300.h is exported; calls whose arguments are rejected return
+before any CUDA work, so they run without a GPU.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import xcape_gb300 as X
+from xcape_gb300 import _lib
+from xcape_gb300.core import calc_cape, calc_srh
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def p_t_td_3d():
+    rng = np.random.default_rng(0)
+    return tuple(rng.random((5, 10, 20)) for _ in range(3))
+
+
+@pytest.fixture(scope="module")
+def p_t_td_surface():
+    rng = np.random.default_rng(1)
+    return tuple(rng.random((5, 10)) for _ in range(3))
+
+
+@pytest.mark.parametrize("sourcein,n_returns", [("surface", 2), ("most-unstable", 4)])
+@pytest.mark.parametrize("vertical_levin", ["sigma", "pressure", "model"])
+def test_calc_cape_shape_3d(p_t_td_3d, p_t_td_surface, sourcein, n_returns, vertical_levin):
+    p, t, td = p_t_td_3d
+    ps, ts, tds = p_t_td_surface
+    if vertical_levin == "pressure":
+        args = (np.ones(t.shape[-1]), t, td, ps, ts, tds)
+    else:
+        args = (p, t, td, ps, ts, tds)
+    result = calc_cape(*args, source=sourcein, vertical_lev=vertical_levin, method="dummy")
+    assert len(result) == n_returns
+    for data in result:
+        assert data.shape == p.shape[:-1]
+
+
+def test_calc_cape_argument_errors(p_t_td_3d, p_t_td_surface):
+    p, t, td = p_t_td_3d
+    ps, ts, tds = p_t_td_surface
+    with pytest.raises(ValueError, match="Too few"):
+        calc_cape(p, t, td, ps, ts)
+    with pytest.raises(ValueError, match="Too many"):
+        calc_cape(p, t, td, ps, ts, tds, ps)
+    with pytest.raises(ValueError, match="vertical_lev"):
+        calc_cape(p, t, td, ps, ts, tds, vertical_lev="height")
+    with pytest.raises(ValueError, match="P should be 1d"):
+        calc_cape(p, t, td, ps, ts, tds, vertical_lev="pressure", method="dummy")
+    with pytest.raises(ValueError, match="invalid method"):
+        calc_cape(p, t, td, ps, ts, tds, vertical_lev="sigma", method="numba")
+    with pytest.raises(ValueError, match="source"):
+        calc_cape(p, t, td, ps, ts, tds, source="lifted", method="dummy")
+    with pytest.raises(ValueError, match="adiabat"):
+        calc_cape(p, t, td, ps, ts, tds, adiabat="dry", method="dummy")
+    with pytest.raises(ValueError, match="same shape"):
+        calc_cape(p[..., :5], t, td, ps, ts, tds, method="dummy")
+
+
+def test_calc_srh_argument_errors(p_t_td_3d, p_t_td_surface):
+    p, t, td = p_t_td_3d
+    ps, ts, tds = p_t_td_surface
+    with pytest.raises(ValueError, match="output_var"):
+        calc_srh(p, t, td, t, td, ps, ts, tds, ps, ts, output_var="helicity")
+    with pytest.raises(ValueError, match="P should be 1d"):
+        calc_srh(p, t, td, t, td, ps, ts, tds, ps, ts, vertical_lev="pressure")
+
+
+def test_fortran_method_needs_reference(p_t_td_3d, p_t_td_surface):
+    p, t, td = p_t_td_3d
+    ps, ts, tds = p_t_td_surface
+    try:
+        import xcape  # noqa: F401
+        pytest.skip("reference xcape installed")
+    except ImportError:
+        pass
+    with pytest.raises(ImportError, match="reference xcape"):
+        calc_cape(p, t, td, ps, ts, tds, vertical_lev="sigma", method="fortran")
+
+
+def _declared_entry_points():
+    text = open(os.path.join(ROOT, "include", "xcape_gb300.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(xc_\w+)\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    declared = _declared_entry_points()
+    assert len(declared) >= 18
+    for name in declared:
+        assert hasattr(L, name), f"{name} declared in include/xcape_gb300.h but not exported"
+    assert set(declared) == set(_lib.exported_symbols())
+    assert "sm_103a" in X.version()
+
+
+def test_invalid_arguments_return_status_without_gpu():
+    L = _lib.lib()
+    null = None
+    # unknown source: the reference Fortran would `stop` (CAPE_CODE_model_lev.f90:343-351)
+    rc = L.xc_loopcape_ml(null, null, null, null, null, null, 0, 500.0, 7, 500.0, 1, 10, 4,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_ERR_INVALID
+    assert b"source" in L.xc_last_error()
+    # undefined adiabat (:492-497)
+    rc = L.xc_loopcape_ml(null, null, null, null, null, null, 0, 500.0, 1, 500.0, 9, 10, 4,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_ERR_INVALID and b"adiabat" in L.xc_last_error()
+    # non-positive pressure increment
+    rc = L.xc_loopcape_ml(null, null, null, null, null, null, 0, 0.0, 1, 500.0, 1, 10, 4,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_ERR_INVALID
+    # bad dtype / level count
+    rc = L.xc_loopcape_ml(null, null, null, null, null, null, 5, 500.0, 1, 500.0, 1, 10, 4,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_ERR_INVALID
+    rc = L.xc_loopcape_ml(null, null, null, null, null, null, 0, 500.0, 1, 500.0, 1, 0, 4,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_ERR_INVALID
+    # grid 3 without start
+    rc = L.xc_loopcape_pl(null, null, null, null, null, null, 0, 500.0, 1, 500.0, 1, null, 10, 4,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_ERR_INVALID
+    # zero columns is a no-op
+    rc = L.xc_loopcape_ml(null, null, null, null, null, null, 0, 500.0, 1, 500.0, 1, 10, 0,
+                          null, null, null, null, null, null)
+    assert rc == _lib.XC_OK
+    # rm/lm/mean6 must come together
+    buf = ctypes.c_void_p(16)
+    rc = L.xc_calc_srh(1, *([null] * 10), 0, null, 3000.0, 2.0, 10, 4, null, null, buf, null,
+                       null, null)
+    assert rc == _lib.XC_ERR_INVALID
+
+
+def test_python_raises_library_errors():
+    with pytest.raises(_lib.XcapeError, match="status 1"):
+        _lib.call("xc_loopcape_ml", None, None, None, None, None, None, 0, 500.0, 4, 500.0, 1,
+                  10, 4, None, None, None, None, None, None)

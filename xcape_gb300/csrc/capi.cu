@@ -1,0 +1,444 @@
+// capi.cu -- extern "C" entry points of libxcape_gb300.so (include/xcape_gb300.h).
+//
+// Argument checks stand in for the reference's `stop` statements and the
+// Python-side ValueError/KeyError paths: every bad argument returns
+// XC_ERR_INVALID with a message in xc_last_error(); nothing aborts.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/xcape_gb300.h"
+#include "xc_kernels.h"
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+  return fail(XC_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+int check_common(int dtype, int nk, int n2) {
+  if (dtype != XC_F32 && dtype != XC_F64) return fail(XC_ERR_INVALID, "dtype must be XC_F32 or XC_F64");
+  if (nk < 1 || nk > XC_MAX_LEVELS) return fail(XC_ERR_INVALID, "nk=%d outside 1..%d", nk, XC_MAX_LEVELS);
+  if (n2 < 0) return fail(XC_ERR_INVALID, "n2=%d is negative", n2);
+  return XC_OK;
+}
+
+int check_cape_opts(float pinc, int source, float ml_depth, int adiabat) {
+  if (source < 1 || source > 3)
+    return fail(XC_ERR_INVALID, "Unknown value for source: %d (1 surface, 2 most unstable, 3 mixed layer)", source);
+  if (adiabat < 1 || adiabat > 4) return fail(XC_ERR_INVALID, "Undefined adiabat: %d (1..4)", adiabat);
+  if (!(pinc > 0.0f)) return fail(XC_ERR_INVALID, "pinc must be a positive pressure increment (Pa)");
+  if (source == 3 && !(ml_depth > 0.0f)) return fail(XC_ERR_INVALID, "ml_depth must be positive");
+  return XC_OK;
+}
+
+// Device workspace of the *_host entry points: one grow-only buffer per
+// device, serialised by a mutex (a host call holds it until its outputs are
+// back, so the buffer is never shared between calls in flight).
+struct Workspace {
+  void *ptr = nullptr;
+  size_t cap = 0;
+};
+std::mutex g_ws_mu;
+std::vector<Workspace> g_ws;
+
+int ws_get(size_t bytes, void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if ((int)g_ws.size() <= dev) g_ws.resize(dev + 1);
+  Workspace &w = g_ws[dev];
+  if (w.cap < bytes) {
+    if (w.ptr) {
+      cudaFree(w.ptr);
+      w.ptr = nullptr;
+      w.cap = 0;
+    }
+    e = cudaMalloc(&w.ptr, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(XC_ERR_NOMEM, "cudaMalloc(%zu) for the host-path workspace: %s", bytes,
+                  cudaGetErrorString(e));
+    }
+    w.cap = bytes;
+  }
+  *out = w.ptr;
+  return XC_OK;
+}
+
+// Carves 256-byte aligned slices out of one workspace allocation.
+struct Carver {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char *xc_last_error(void) { return g_err; }
+
+const char *xc_version(void) { return "xcape_gb300 0.1.0 (sm_103a)"; }
+
+int xc_release_workspace(void) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  int prev = 0;
+  cudaGetDevice(&prev);
+  for (size_t d = 0; d < g_ws.size(); ++d) {
+    if (g_ws[d].ptr) {
+      cudaSetDevice((int)d);
+      cudaFree(g_ws[d].ptr);
+      g_ws[d] = Workspace();
+    }
+  }
+  cudaSetDevice(prev);
+  return XC_OK;
+}
+
+int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                   const void *ts, const void *tds, int dtype, float pinc, int source,
+                   float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
+                   float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                   long long *counters, void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  rc = check_cape_opts(pinc, source, ml_depth, adiabat);
+  if (rc) return rc;
+  if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
+  if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
+  if (guess != XC_GUESS_PLAIN) return fail(XC_ERR_INVALID, "guess %d is not available", guess);
+  if (n2 == 0) return XC_OK;
+  if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  xc::CapeArgs a;
+  a.grid = grid;
+  a.dtype = dtype;
+  a.p = p;
+  a.t = t3d;
+  a.td = td3d;
+  a.ps = ps;
+  a.ts = ts;
+  a.tds = tds;
+  a.start = grid == 1 ? nullptr : start_3d;
+  a.pinc = pinc;
+  a.source = source;
+  a.ml_depth = ml_depth;
+  a.adiabat = adiabat;
+  a.nk = nk;
+  a.n2 = n2;
+  a.guess = guess;
+  a.cape = cape;
+  a.cin = cin;
+  a.mulvl = mulvl;
+  a.z_out = z_out;
+  a.status = status;
+  a.counters = counters;
+  cudaError_t e = xc::launch_cape(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+  return XC_OK;
+}
+
+int xc_loopcape_ml(const void *p3d, const void *t3d, const void *td3d, const void *ps,
+                   const void *ts, const void *tds, int dtype, float pinc, int source,
+                   float ml_depth, int adiabat, int nk, int n2, float *cape, float *cin,
+                   int *mulvl, float *z_out, int *status, void *stream) {
+  return xc_loopcape_ex(1, p3d, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
+                        nullptr, nk, n2, XC_GUESS_PLAIN, cape, cin, mulvl, z_out, status, nullptr,
+                        stream);
+}
+
+int xc_loopcape_pl1d(const void *t3d, const void *td3d, const void *p1d, const void *ps,
+                     const void *ts, const void *tds, int dtype, float pinc, int source,
+                     float ml_depth, int adiabat, const int *start_3d, int nk, int n2,
+                     float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                     void *stream) {
+  return xc_loopcape_ex(2, p1d, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
+                        start_3d, nk, n2, XC_GUESS_PLAIN, cape, cin, mulvl, z_out, status,
+                        nullptr, stream);
+}
+
+int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const void *ps,
+                   const void *ts, const void *tds, int dtype, float pinc, int source,
+                   float ml_depth, int adiabat, const int *start_3d, int nk, int n2,
+                   float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                   void *stream) {
+  return xc_loopcape_ex(3, p3d, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
+                        start_3d, nk, n2, XC_GUESS_PLAIN, cape, cin, mulvl, z_out, status,
+                        nullptr, stream);
+}
+
+int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
+                        const void *ps, const void *ts, const void *tds, int dtype, float pinc,
+                        int source, float ml_depth, int adiabat, const int *start_3d, int nk,
+                        int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
+                        int *status, void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  rc = check_cape_opts(pinc, source, ml_depth, adiabat);
+  if (rc) return rc;
+  if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1, 2 or 3");
+  if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
+  if (n2 == 0) return XC_OK;
+  const size_t es = dtype == XC_F32 ? 4 : 8;
+  const size_t n3 = (size_t)n2 * nk;
+  const size_t p_bytes = (grid == 2 ? (size_t)nk : n3) * es;
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  Carver cv;
+  const size_t o_p = cv.take(p_bytes), o_t = cv.take(n3 * es), o_td = cv.take(n3 * es);
+  const size_t o_ps = cv.take(n2 * es), o_ts = cv.take(n2 * es), o_tds = cv.take(n2 * es);
+  const size_t o_st = (grid != 1 && start_3d) ? cv.take(n2 * 4) : 0;
+  const size_t o_cape = cv.take(n2 * 4), o_cin = cv.take(n2 * 4), o_mu = cv.take(n2 * 4),
+               o_z = cv.take(n2 * 4);
+  const size_t o_stat = status ? cv.take(n2 * 4) : 0;
+  void *base = nullptr;
+  rc = ws_get(cv.off, &base);
+  if (rc) return rc;
+  char *b = (char *)base;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaSuccess;
+#define H2D(off, src, bytes)                                                         \
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, s)
+  H2D(o_p, p, p_bytes);
+  H2D(o_t, t3d, n3 * es);
+  H2D(o_td, td3d, n3 * es);
+  H2D(o_ps, ps, n2 * es);
+  H2D(o_ts, ts, n2 * es);
+  H2D(o_tds, tds, n2 * es);
+  if (grid != 1 && start_3d) H2D(o_st, start_3d, n2 * 4);
+#undef H2D
+  if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
+  rc = xc_loopcape_ex(grid, b + o_p, b + o_t, b + o_td, b + o_ps, b + o_ts, b + o_tds, dtype, pinc,
+                      source, ml_depth, adiabat,
+                      (grid != 1 && start_3d) ? (const int *)(b + o_st) : nullptr, nk, n2, guess,
+                      (float *)(b + o_cape), (float *)(b + o_cin), (int *)(b + o_mu),
+                      (float *)(b + o_z), status ? (int *)(b + o_stat) : nullptr, nullptr, s);
+  if (rc) return rc;
+#define D2H(dst, off, bytes)                                                         \
+  if (e == cudaSuccess) e = cudaMemcpyAsync((dst), b + (off), (bytes), cudaMemcpyDeviceToHost, s)
+  D2H(cape, o_cape, n2 * 4);
+  D2H(cin, o_cin, n2 * 4);
+  D2H(mulvl, o_mu, n2 * 4);
+  D2H(z_out, o_z, n2 * 4);
+  if (status) D2H(status, o_stat, n2 * 4);
+#undef D2H
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "device-to-host copy");
+  return XC_OK;
+}
+
+int xc_calc_srh(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
+                const void *v3d, const void *ps, const void *ts, const void *tds,
+                const void *us, const void *vs, int dtype, const int *start_3d, double depth,
+                double aglh0, int nk, int n2, double *srh_rm, double *srh_lm, float *rm,
+                float *lm, float *mean6, void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  if (grid != 1 && grid != 2) return fail(XC_ERR_INVALID, "grid must be 1 (sigma) or 2 (pressure, 1-D p)");
+  if ((rm == nullptr) != (lm == nullptr) || (rm == nullptr) != (mean6 == nullptr))
+    return fail(XC_ERR_INVALID, "rm, lm and mean6 must be all NULL or all set");
+  if (n2 == 0) return XC_OK;
+  if (!p || !t3d || !td3d || !u3d || !v3d || !ps || !ts || !tds || !us || !vs || !srh_rm || !srh_lm)
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  xc::SrhArgs a;
+  a.grid = grid;
+  a.dtype = dtype;
+  a.p = p;
+  a.t = t3d;
+  a.td = td3d;
+  a.u = u3d;
+  a.v = v3d;
+  a.ps = ps;
+  a.ts = ts;
+  a.tds = tds;
+  a.us = us;
+  a.vs = vs;
+  a.start = grid == 2 ? start_3d : nullptr;
+  a.depth = depth;
+  a.aglh0 = aglh0;
+  a.nk = nk;
+  a.n2 = n2;
+  a.srh_rm = srh_rm;
+  a.srh_lm = srh_lm;
+  a.rm = rm;
+  a.lm = lm;
+  a.mean6 = mean6;
+  cudaError_t e = xc::launch_srh(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "srh kernel launch");
+  return XC_OK;
+}
+
+int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
+                     const void *u3d, const void *v3d, const void *ps, const void *ts,
+                     const void *tds, const void *us, const void *vs, int dtype,
+                     const int *start_3d, double depth, double aglh0, int nk, int n2,
+                     double *srh_rm, double *srh_lm, float *rm, float *lm, float *mean6,
+                     void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  if (grid != 1 && grid != 2) return fail(XC_ERR_INVALID, "grid must be 1 or 2");
+  if ((rm == nullptr) != (lm == nullptr) || (rm == nullptr) != (mean6 == nullptr))
+    return fail(XC_ERR_INVALID, "rm, lm and mean6 must be all NULL or all set");
+  if (n2 == 0) return XC_OK;
+  const size_t es = dtype == XC_F32 ? 4 : 8;
+  const size_t n3 = (size_t)n2 * nk;
+  const size_t p_bytes = (grid == 2 ? (size_t)nk : n3) * es;
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  Carver cv;
+  const size_t o_p = cv.take(p_bytes), o_t = cv.take(n3 * es), o_td = cv.take(n3 * es),
+               o_u = cv.take(n3 * es), o_v = cv.take(n3 * es);
+  const size_t o_ps = cv.take(n2 * es), o_ts = cv.take(n2 * es), o_tds = cv.take(n2 * es),
+               o_us = cv.take(n2 * es), o_vs = cv.take(n2 * es);
+  const size_t o_st = (grid == 2 && start_3d) ? cv.take(n2 * 4) : 0;
+  const size_t o_srm = cv.take(n2 * 8), o_slm = cv.take(n2 * 8);
+  const size_t o_rm = rm ? cv.take(n2 * 8) : 0, o_lm = rm ? cv.take(n2 * 8) : 0,
+               o_mean = rm ? cv.take(n2 * 8) : 0;
+  void *base = nullptr;
+  rc = ws_get(cv.off, &base);
+  if (rc) return rc;
+  char *b = (char *)base;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaSuccess;
+#define H2D(off, src, bytes)                                                         \
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, s)
+  H2D(o_p, p, p_bytes);
+  H2D(o_t, t3d, n3 * es);
+  H2D(o_td, td3d, n3 * es);
+  H2D(o_u, u3d, n3 * es);
+  H2D(o_v, v3d, n3 * es);
+  H2D(o_ps, ps, n2 * es);
+  H2D(o_ts, ts, n2 * es);
+  H2D(o_tds, tds, n2 * es);
+  H2D(o_us, us, n2 * es);
+  H2D(o_vs, vs, n2 * es);
+  if (grid == 2 && start_3d) H2D(o_st, start_3d, n2 * 4);
+#undef H2D
+  if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
+  rc = xc_calc_srh(grid, b + o_p, b + o_t, b + o_td, b + o_u, b + o_v, b + o_ps, b + o_ts,
+                   b + o_tds, b + o_us, b + o_vs, dtype,
+                   (grid == 2 && start_3d) ? (const int *)(b + o_st) : nullptr, depth, aglh0, nk,
+                   n2, (double *)(b + o_srm), (double *)(b + o_slm),
+                   rm ? (float *)(b + o_rm) : nullptr, rm ? (float *)(b + o_lm) : nullptr,
+                   rm ? (float *)(b + o_mean) : nullptr, s);
+  if (rc) return rc;
+#define D2H(dst, off, bytes)                                                         \
+  if (e == cudaSuccess) e = cudaMemcpyAsync((dst), b + (off), (bytes), cudaMemcpyDeviceToHost, s)
+  D2H(srh_rm, o_srm, n2 * 8);
+  D2H(srh_lm, o_slm, n2 * 8);
+  if (rm) {
+    D2H(rm, o_rm, n2 * 8);
+    D2H(lm, o_lm, n2 * 8);
+    D2H(mean6, o_mean, n2 * 8);
+  }
+#undef D2H
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "device-to-host copy");
+  return XC_OK;
+}
+
+int xc_loop_stdheight_ml(const double *P, const double *T, const double *Td, const double *Ps,
+                         const double *Ts, const double *Tds, const double *Hin, int NK, int NX,
+                         double *H, double *Hs, void *stream) {
+  int rc = check_common(XC_F64, NK, NX);
+  if (rc) return rc;
+  cudaError_t e = xc::launch_stdheight(P, NK, T, Td, Ps, Ts, Tds, Hin, nullptr, NK, NX, H, Hs,
+                                       (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "stdheight kernel launch");
+}
+
+int xc_loop_stdheight_pl1d(const double *T, const double *Td, const double *P, const double *Ps,
+                           const double *Ts, const double *Tds, const double *Hin,
+                           const int *start_3d, int NK, int NX, double *H, double *Hs,
+                           void *stream) {
+  int rc = check_common(XC_F64, NK, NX);
+  if (rc) return rc;
+  if (!start_3d) return fail(XC_ERR_INVALID, "start_3d is required");
+  cudaError_t e = xc::launch_stdheight(P, 0, T, Td, Ps, Ts, Tds, Hin, start_3d, NK, NX, H, Hs,
+                                       (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "stdheight kernel launch");
+}
+
+int xc_loop_stdheight_pl(const double *P, const double *T, const double *Td, const double *Ps,
+                         const double *Ts, const double *Tds, const double *Hin,
+                         const int *start_3d, int NK, int NX, double *H, double *Hs,
+                         void *stream) {
+  int rc = check_common(XC_F64, NK, NX);
+  if (rc) return rc;
+  if (!start_3d) return fail(XC_ERR_INVALID, "start_3d is required");
+  cudaError_t e = xc::launch_stdheight(P, NK, T, Td, Ps, Ts, Tds, Hin, start_3d, NK, NX, H, Hs,
+                                       (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "stdheight kernel launch");
+}
+
+int xc_bunkers_loop_ml(const float *U3d, const float *V3d, const float *AGLH3d, const float *Us,
+                       const float *Vs, const float *AGLHs, int nk, int n2, float *RM, float *LM,
+                       float *Mean6kmwind, void *stream) {
+  int rc = check_common(XC_F32, nk, n2);
+  if (rc) return rc;
+  cudaError_t e = xc::launch_bunkers(U3d, V3d, AGLH3d, Us, Vs, AGLHs, nullptr, nk, n2, RM, LM,
+                                     Mean6kmwind, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "bunkers kernel launch");
+}
+
+int xc_bunkers_loop_pl(const float *U3d, const float *V3d, const float *AGLH3d, const float *Us,
+                       const float *Vs, const float *AGLHs, const int *start_3d, int nk, int n2,
+                       float *RM, float *LM, float *Mean6kmwind, void *stream) {
+  int rc = check_common(XC_F32, nk, n2);
+  if (rc) return rc;
+  if (!start_3d) return fail(XC_ERR_INVALID, "start_3d is required");
+  cudaError_t e = xc::launch_bunkers(U3d, V3d, AGLH3d, Us, Vs, AGLHs, start_3d, nk, n2, RM, LM,
+                                     Mean6kmwind, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "bunkers kernel launch");
+}
+
+int xc_loop_sreh_ml(const double *u, const double *v, const double *aglh, const double *us,
+                    const double *vs, const double *aglhs, const double *cu_rm,
+                    const double *cv_rm, const double *cu_lm, const double *cv_lm, double top,
+                    int nk, int n2, double *sreh_rm, double *sreh_lm, void *stream) {
+  int rc = check_common(XC_F64, nk, n2);
+  if (rc) return rc;
+  cudaError_t e = xc::launch_sreh(u, v, aglh, us, vs, aglhs, cu_rm, cv_rm, cu_lm, cv_lm, top,
+                                  nullptr, nk, n2, sreh_rm, sreh_lm, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "sreh kernel launch");
+}
+
+int xc_loop_sreh_pl(const double *u, const double *v, const double *aglh, const double *us,
+                    const double *vs, const double *aglhs, const double *cu_rm,
+                    const double *cv_rm, const double *cu_lm, const double *cv_lm, double top,
+                    const int *start_3d, int nk, int n2, double *sreh_rm, double *sreh_lm,
+                    void *stream) {
+  int rc = check_common(XC_F64, nk, n2);
+  if (rc) return rc;
+  if (!start_3d) return fail(XC_ERR_INVALID, "start_3d is required");
+  cudaError_t e = xc::launch_sreh(u, v, aglh, us, vs, aglhs, cu_rm, cv_rm, cu_lm, cv_lm, top,
+                                  start_3d, nk, n2, sreh_rm, sreh_lm, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "sreh kernel launch");
+}
+
+int xc_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, int n2, int *start_3d,
+                    void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  if (n2 == 0) return XC_OK;
+  cudaError_t e = xc::launch_pres_lev_pos(p1d, ps, dtype, nk, n2, start_3d, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "pres_lev_pos kernel launch");
+}
+
+}  // extern "C"

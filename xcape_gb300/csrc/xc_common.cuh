@@ -1,0 +1,111 @@
+// xc_common.cuh -- shared device helpers for the xcape GB300 column kernels.
+//
+// Thermodynamic constants and helper functions follow the reference Fortran
+// (src/xcape/fortran/CAPE_CODE_model_lev.f90:188-211 for the constants,
+// :570-620 for getqvs/getqvi/getthe).  Single-precision constants are
+// evaluated in float at compile time exactly as gfortran folds `real,
+// parameter` expressions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xc {
+
+// ---- CAPE constants (CAPE_CODE_model_lev.f90:188-211) ---------------------
+constexpr float G = 9.81f;
+constexpr float P00 = 100000.0f;
+constexpr float CP = 1005.7f;
+constexpr float RD = 287.04f;
+constexpr float RV = 461.5f;
+constexpr float XLV = 2501000.0f;
+constexpr float XLS = 2836017.0f;
+constexpr float T0 = 273.15f;
+constexpr float CPV = 1875.0f;
+constexpr float CPL = 4190.0f;
+constexpr float CPI = 2118.636f;
+constexpr float LV1 = XLV + (CPL - CPV) * T0;
+constexpr float LV2 = CPL - CPV;
+constexpr float LS1 = XLS + (CPI - CPV) * T0;
+constexpr float LS2 = CPI - CPV;
+constexpr float RP00 = 1.0f / P00;
+constexpr float REPS = RV / RD;
+constexpr float RDDCP = RD / CP;
+constexpr float CPDG = CP / G;
+constexpr float CONVERGE = 0.0002f;
+constexpr float QEPS = 287.04f / 461.5f;  // eps inside getqvs/getqvi
+
+// Column status bits (mirrors include/xcape_gb300.h).
+constexpr int COL_NOCONV = 1;
+constexpr int COL_BADSTART = 2;
+constexpr int COL_TOOMANYSTEPS = 4;
+
+// Sub-step budget of one column: bounds the work of any input (a column
+// that would need more is flagged and zeroed instead of running on).
+constexpr long long MAX_SUBSTEPS = 1LL << 22;
+
+// ---- getqvs / getqvi / getthe ----------------------------------------------
+// CAPE_CODE_model_lev.f90:570-581
+__device__ __forceinline__ float getqvs(float p, float t) {
+  float es = 611.2f * expf(17.67f * (t - 273.15f) / (t - 29.65f));
+  return QEPS * es / (p - es);
+}
+// CAPE_CODE_model_lev.f90:587-598
+__device__ __forceinline__ float getqvi(float p, float t) {
+  float es = 611.2f * expf(21.8745584f * (t - 273.15f) / (t - 7.66f));
+  return QEPS * es / (p - es);
+}
+// CAPE_CODE_model_lev.f90:604-620 (x**(-1) is 1/x)
+__device__ __forceinline__ float getthe(float p, float t, float td, float q) {
+  float tlcl;
+  if ((td - t) >= -0.1f) {
+    tlcl = t;
+  } else {
+    tlcl = 56.0f + 1.0f / (1.0f / (td - 56.0f) + 0.00125f * logf(t / td));
+  }
+  return t * powf(100000.0f / p, 0.2854f * (1.0f - 0.28f * q)) *
+         expf(((3376.0f / tlcl) - 2.54f) * q * (1.0f + 0.81f * q));
+}
+
+// Fortran MIN/MAX as gfortran lowers them for the reference build: the
+// second operand is returned when the comparison fails (NaN included).
+__device__ __forceinline__ float fmin_f(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float fmax_f(float a, float b) { return a > b ? a : b; }
+
+// ---- input loads ------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ float ldf(const T *ptr) {
+  return (float)__ldg(ptr);
+}
+template <typename T>
+__device__ __forceinline__ double ldd(const T *ptr) {
+  return (double)__ldg(ptr);
+}
+
+// Masked argmin of ps - p over the levels, 1-based (src/xcape/core.py:286-289):
+// entries with ps - p < 0 are masked (filled with +inf), np.argmin then
+// returns the first NaN if there is one, else the first minimum; a column
+// with every entry masked gives index 0.  The difference is taken in the
+// input precision T, as numpy does for same-dtype operands.
+template <typename T>
+__device__ __forceinline__ int pres_lev_pos_col(const T *p1d, T ps, int nk) {
+  T best = ps - __ldg(p1d);
+  int bi = 0;
+  if (!(best < (T)0)) {
+    if (best != best) return 1;
+  } else {
+    best = (T)INFINITY;
+  }
+  for (int k = 1; k < nk; ++k) {
+    T d = ps - __ldg(p1d + k);
+    if (d != d) return k + 1;
+    if (d < (T)0) d = (T)INFINITY;
+    if (d < best) {
+      best = d;
+      bi = k;
+    }
+  }
+  return bi + 1;
+}
+
+}  // namespace xc

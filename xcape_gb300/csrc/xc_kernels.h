@@ -1,0 +1,58 @@
+// xc_kernels.h -- launch interface between the C ABI (capi.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace xc {
+
+struct CapeArgs {
+  int grid;   // 1 sigma/model (p per column), 2 pressure with shared p1d, 3 pressure per column
+  int dtype;  // 0 f32 inputs, 1 f64 inputs
+  const void *p, *t, *td, *ps, *ts, *tds;
+  const int *start;  // nullable for grid 2 (derived in the kernel)
+  float pinc;
+  int source;
+  float ml_depth;
+  int adiabat;
+  int nk;
+  long long n2;
+  int guess;
+  float *cape, *cin;
+  int *mulvl;
+  float *z_out;
+  int *status;             // nullable
+  long long *counters;     // nullable: [0] += sub-steps, [1] += iterations
+};
+
+cudaError_t launch_cape(const CapeArgs &a, cudaStream_t s);
+cudaError_t launch_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, long long n2,
+                                int *start, cudaStream_t s);
+
+struct SrhArgs {
+  int grid;   // 1 sigma/model, 2 pressure with shared p1d
+  int dtype;
+  const void *p, *t, *td, *u, *v, *ps, *ts, *tds, *us, *vs;
+  const int *start;  // nullable for grid 2
+  double depth, aglh0;
+  int nk;
+  long long n2;
+  double *srh_rm, *srh_lm;
+  float *rm, *lm, *mean6;  // nullable, [n2][2]
+};
+
+cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
+
+// Stage kernels mirroring the reference's individual Fortran loops.
+cudaError_t launch_stdheight(const double *P, long long p_stride, const double *T,
+                             const double *Td, const double *Ps, const double *Ts,
+                             const double *Tds, const double *Hin, const int *start, int NK,
+                             long long NX, double *H, double *Hs, cudaStream_t s);
+cudaError_t launch_bunkers(const float *U, const float *V, const float *Z, const float *Us,
+                           const float *Vs, const float *Zs, const int *start, int nk,
+                           long long n2, float *RM, float *LM, float *Mean, cudaStream_t s);
+cudaError_t launch_sreh(const double *u, const double *v, const double *aglh, const double *us,
+                        const double *vs, const double *aglhs, const double *cu_rm,
+                        const double *cv_rm, const double *cu_lm, const double *cv_lm,
+                        double top, const int *start, int nk, long long n2, double *sreh_rm,
+                        double *sreh_lm, cudaStream_t s);
+
+}  // namespace xc
