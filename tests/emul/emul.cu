@@ -1,0 +1,81 @@
+// emul.cu -- host build of the kernels' column routines (test harness).
+//
+// Compiles cape_column.cuh / srh_column.cuh as ordinary host code (glibc
+// expf/logf/powf, -ffp-contract=off) and loops over the columns on the CPU,
+// so that the exact code the CUDA kernels run can be compared with the
+// oracle without a GPU: the only differences allowed are the ones the column
+// routines document (none changes a result for finite inputs).
+#include "../../xcape_gb300/csrc/cape_column.cuh"
+#include "../../xcape_gb300/csrc/srh_column.cuh"
+
+using namespace xc;
+
+template <typename T, int GRID>
+static void cape_loop(const CapeArgs &a, long long *counters) {
+  const bool ice = a.adiabat >= 3, pseudo = (a.adiabat == 1 || a.adiabat == 3);
+  long long s = 0, it = 0;
+  for (long long i = 0; i < a.n2; ++i) {
+    int nsub = 0, niter = 0;
+    if (ice && pseudo) cape_column_run<T, GRID, true, true>(a, i, nsub, niter);
+    else if (ice) cape_column_run<T, GRID, true, false>(a, i, nsub, niter);
+    else if (pseudo) cape_column_run<T, GRID, false, true>(a, i, nsub, niter);
+    else cape_column_run<T, GRID, false, false>(a, i, nsub, niter);
+    s += nsub;
+    it += niter;
+  }
+  if (counters) {
+    counters[0] += s;
+    counters[1] += it;
+  }
+}
+
+extern "C" int emu_cape(int grid, const void *p, const void *t, const void *td, const void *ps,
+                        const void *ts, const void *tds, int dtype, float pinc, int source,
+                        float ml_depth, int adiabat, const int *start, int nk, long long n2,
+                        float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                        long long *counters) {
+  CapeArgs a;
+  a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.ps = ps; a.ts = ts; a.tds = tds;
+  a.start = grid == 1 ? nullptr : start; a.pinc = pinc; a.source = source; a.ml_depth = ml_depth;
+  a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = 0; a.cape = cape; a.cin = cin;
+  a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr;
+  if (dtype == 0) {
+    if (grid == 1) cape_loop<float, 1>(a, counters);
+    else if (grid == 2) cape_loop<float, 2>(a, counters);
+    else cape_loop<float, 3>(a, counters);
+  } else {
+    if (grid == 1) cape_loop<double, 1>(a, counters);
+    else if (grid == 2) cape_loop<double, 2>(a, counters);
+    else cape_loop<double, 3>(a, counters);
+  }
+  return 0;
+}
+
+extern "C" int emu_srh(int grid, const void *p, const void *t, const void *td, const void *u,
+                       const void *v, const void *ps, const void *ts, const void *tds,
+                       const void *us, const void *vs, int dtype, const int *start, double depth,
+                       double aglh0, int nk, long long n2, double *srh_rm, double *srh_lm,
+                       float *rm, float *lm, float *mean6) {
+  SrhArgs a;
+  a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.u = u; a.v = v; a.ps = ps;
+  a.ts = ts; a.tds = tds; a.us = us; a.vs = vs; a.start = grid == 2 ? start : nullptr;
+  a.depth = depth; a.aglh0 = aglh0; a.nk = nk; a.n2 = n2; a.srh_rm = srh_rm; a.srh_lm = srh_lm;
+  a.rm = rm; a.lm = lm; a.mean6 = mean6;
+  for (long long i = 0; i < n2; ++i) {
+    if (dtype == 0) {
+      if (grid == 1) srh_column_run<float, 1>(a, i);
+      else srh_column_run<float, 2>(a, i);
+    } else {
+      if (grid == 1) srh_column_run<double, 1>(a, i);
+      else srh_column_run<double, 2>(a, i);
+    }
+  }
+  return 0;
+}
+
+extern "C" void emu_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, long long n2,
+                                 int *start) {
+  for (long long i = 0; i < n2; ++i)
+    start[i] = dtype == 0 ? pres_lev_pos_col<float>((const float *)p1d, ((const float *)ps)[i], nk)
+                          : pres_lev_pos_col<double>((const double *)p1d, ((const double *)ps)[i], nk);
+}

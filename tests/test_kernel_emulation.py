@@ -1,0 +1,179 @@
+"""CPU checks of the CUDA kernels' column routines.
+
+tests/emul builds cape_column.cuh and srh_column.cuh -- the code every CUDA
+thread runs -- as host code with glibc math and no FMA contraction.  Run that
+way it must reproduce the oracle bit for bit: same operations, same order,
+same rounding.  This pins the kernels' logic (level offsets, the one-pass
+mixed layer, the upward Bunkers sweep, ragged start levels, edge cases) on
+the CPU; the GPU tests then only have to account for CUDA's own expf/logf/
+powf rounding and FMA contraction.
+"""
+import shutil
+
+import numpy as np
+import pytest
+
+import oracle as O
+from xcape_gb300 import synthetic as S
+
+emul = pytest.importorskip("emul")
+if emul.nvcc() is None:
+    pytest.skip("nvcc not available", allow_module_level=True)
+
+SOURCES = (1, 2, 3)
+ADIABATS = (1, 2, 3, 4)
+
+
+def _emu_cape(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0,
+              start=None):
+    L = emul.lib()
+    f64 = any(np.asarray(a).dtype == np.float64 for a in (p, t, td, ps, ts, tds))
+    dt = np.float64 if f64 else np.float32
+    t = np.ascontiguousarray(t, dt)
+    nk = t.shape[-1]
+    n2 = t.size // nk
+    arrs = [np.ascontiguousarray(a, dt) for a in (p, t, td, ps, ts, tds)]
+    st = None if start is None else np.ascontiguousarray(start, np.int32)
+    out = dict(cape=np.empty(n2, np.float32), cin=np.empty(n2, np.float32),
+               mulvl=np.empty(n2, np.int32), z_out=np.empty(n2, np.float32),
+               status=np.empty(n2, np.int32))
+    cnt = np.zeros(2, np.int64)
+    L.emu_cape(grid, *[a.ctypes.data for a in arrs], int(f64), pinc, source, ml_depth, adiabat,
+               None if st is None else st.ctypes.data, nk, n2, out["cape"].ctypes.data,
+               out["cin"].ctypes.data, out["mulvl"].ctypes.data, out["z_out"].ctypes.data,
+               out["status"].ctypes.data, cnt.ctypes.data)
+    out["counters"] = cnt
+    return out
+
+
+def _oracle(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0, start=None):
+    nk = np.shape(t)[-1]
+    t2, td2 = np.reshape(t, (-1, nk)), np.reshape(td, (-1, nk))
+    sf = [np.ravel(a) for a in (ps, ts, tds)]
+    if grid == 1:
+        return O.loopcape(np.reshape(p, (-1, nk)), t2, td2, *sf, pinc, source, ml_depth, adiabat,
+                          stats=True)
+    if grid == 2:
+        st = O.pres_lev_pos(p, sf[0]) if start is None else start
+        return O.loopcape(np.ravel(p), t2, td2, *sf, pinc, source, ml_depth, adiabat, start=st,
+                          p_is_1d=True, stats=True)
+    return O.loopcape(np.reshape(p, (-1, nk)), t2, td2, *sf, pinc, source, ml_depth, adiabat,
+                      start=start, stats=True)
+
+
+def _same(a, b):
+    for k in ("cape", "cin", "mulvl", "z_out", "status"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    assert a["counters"][0] == b["nsub"].sum()
+    assert a["counters"][1] == b["niter"].sum()
+
+
+@pytest.mark.parametrize("adiabat", ADIABATS)
+@pytest.mark.parametrize("source", SOURCES)
+def test_emulated_cape_sigma_bit_exact(source, adiabat):
+    p, t, td, ps, ts, tds = S.sigma_c0(shape=(16, 24))
+    _same(_emu_cape(1, p, t, td, ps, ts, tds, source, adiabat),
+          _oracle(1, p, t, td, ps, ts, tds, source, adiabat))
+
+
+@pytest.mark.parametrize("adiabat", (1, 4))
+@pytest.mark.parametrize("source", SOURCES)
+def test_emulated_cape_pressure_bit_exact(source, adiabat):
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(24, 24))
+    _same(_emu_cape(2, plev, t, td, ps, ts, tds, source, adiabat),
+          _oracle(2, plev, t, td, ps, ts, tds, source, adiabat))
+
+
+def test_emulated_cape_goldens_bit_exact(soundings, era5):
+    s = soundings
+    P, T, TD = s["pressure"], s["temperature"], s["dewpoint"]
+    for source, pinc in ((1, 100.0), (2, 100.0), (3, 1000.0)):
+        args = (P[:, 1:], T[:, 1:], TD[:, 1:], P[:, 0], T[:, 0], TD[:, 0])
+        _same(_emu_cape(1, *args, source, 1, pinc=pinc),
+              _oracle(1, *args, source, 1, pinc=pinc))
+    e = era5
+    for source in SOURCES:
+        args = (e["lev_level"], e["lev_t"], e["lev_td"], e["sfc_p"], e["sfc_t"], e["sfc_td"])
+        _same(_emu_cape(2, *args, source, 1, ml_depth=300.0),
+              _oracle(2, *args, source, 1, ml_depth=300.0))
+
+
+def test_emulated_cape_3d_pressure_and_edges():
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(8, 16))
+    n2 = 128
+    p3 = np.broadcast_to(plev, (n2, plev.size)) + np.random.default_rng(3).normal(
+        0, 0.5, (n2, plev.size)).astype(np.float32)
+    st = O.pres_lev_pos(plev, ps.ravel())
+    st[:3] = [1, 37, 5]
+    for source in SOURCES:
+        _same(_emu_cape(3, p3, t, td, ps, ts, tds, source, 1, start=st),
+              _oracle(3, p3, t, td, ps, ts, tds, source, 1, start=st))
+    # short columns, deep mixed layer, cold surface, MU above 500 hPa
+    p, t, td, ps, ts, tds = (np.array(a) for a in S.sigma_c0(shape=(1, 12), nlev=40, seed=4))
+    ts[0, 0] = -1.0
+    p[0, 2] *= 0.45
+    ps[0, 2] *= 0.45
+    for nlev, mld in ((40, 500.0), (2, 5000.0), (1, 500.0)):
+        for source in SOURCES:
+            args = (p[..., :nlev], t[..., :nlev], td[..., :nlev], ps, ts, tds)
+            _same(_emu_cape(1, *args, source, 1, ml_depth=mld),
+                  _oracle(1, *args, source, 1, ml_depth=mld))
+
+
+@pytest.mark.parametrize("dtype", (np.float32, np.float64))
+def test_emulated_pres_lev_pos(dtype):
+    L = emul.lib()
+    plev = np.array([1000, 975, 950, 950, 900, 850, 700, 500, 300, 100], dtype)
+    ps = np.random.default_rng(11).uniform(800, 1050, 512).astype(dtype)
+    ps[:5] = [1000, 950, 899.99, 80, np.nan]
+    st = np.empty(ps.size, np.int32)
+    L.emu_pres_lev_pos(plev.ctypes.data, ps.ctypes.data, int(dtype == np.float64), plev.size,
+                       ps.size, st.ctypes.data)
+    np.testing.assert_array_equal(st, O.pres_lev_pos(plev, ps))
+
+
+def _emu_srh(grid, p, t, td, u, v, ps, ts, tds, us, vs, depth):
+    L = emul.lib()
+    f64 = any(np.asarray(a).dtype == np.float64 for a in (p, t, td, u, v, ps, ts, tds, us, vs))
+    dt = np.float64 if f64 else np.float32
+    nk = np.shape(t)[-1]
+    n2 = np.size(t) // nk
+    arrs = [np.ascontiguousarray(a, dt) for a in (p, t, td, u, v, ps, ts, tds, us, vs)]
+    srm, slm = np.empty(n2), np.empty(n2)
+    rm, lm, mean = (np.empty((n2, 2), np.float32) for _ in range(3))
+    L.emu_srh(grid, *[a.ctypes.data for a in arrs], int(f64), None, float(depth), 2.0, nk, n2,
+              srm.ctypes.data, slm.ctypes.data, rm.ctypes.data, lm.ctypes.data, mean.ctypes.data)
+    return (srm, slm, rm[:, 0], rm[:, 1], lm[:, 0], lm[:, 1], mean[:, 0], mean[:, 1])
+
+
+def _srh_same(got, args, grid, depth):
+    want = O.calc_srh(*args, depth=depth, vertical_lev="sigma" if grid == 1 else "pressure",
+                      output_var="all")
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g, np.ravel(w))
+
+
+@pytest.mark.parametrize("depth", (1000, 3000))
+def test_emulated_srh_bit_exact(soundings, era5, depth):
+    s = soundings
+    P, T, TD, U, V = s["pressure"], s["temperature"], s["dewpoint"], s["u_wind_ms"], s["v_wind_ms"]
+    args = (P[:, 1:], T[:, 1:], TD[:, 1:], U[:, 1:], V[:, 1:], P[:, 0], T[:, 0], TD[:, 0],
+            U[:, 0], V[:, 0])
+    _srh_same(_emu_srh(1, *args, depth), args, 1, depth)
+    e = era5
+    args = (e["lev_level"], e["lev_t"], e["lev_td"], e["lev_u"], e["lev_v"], e["sfc_p"],
+            e["sfc_t"], e["sfc_td"], e["sfc_u"], e["sfc_v"])
+    _srh_same(_emu_srh(2, *args, depth), args, 2, depth)
+    args = S.srh_c2(shape=(16, 16), nlev=50)
+    _srh_same(_emu_srh(1, *args, depth), args, 1, depth)
+    args = S.pressure_srh(shape=(16, 16))
+    _srh_same(_emu_srh(2, *args, depth), args, 2, depth)
+
+
+def test_emulated_srh_decreasing_heights():
+    p, t, td, u, v, ps, ts, tds, us, vs = (np.array(a, np.float64) for a in
+                                           S.srh_c2(shape=(4, 8), nlev=50, seed=9))
+    p, t, td = (a[..., ::-1].copy() for a in (p, t, td))
+    ps = p[..., 0] * 1.2
+    args = (p, t, td, u, v, ps, ts, tds, us, vs)
+    _srh_same(_emu_srh(1, *args, 3000), args, 1, 3000)

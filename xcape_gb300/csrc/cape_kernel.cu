@@ -1,379 +1,15 @@
-// cape_kernel.cu -- getcape parcel lift (CAPE/CIN) for sm_103a.
-//
-// One thread owns one column.  The column is never materialised: every pass
-// walks the levels upward and recomputes the environment (p, T, Td -> pi, q,
-// theta, theta_v, z) from the input arrays, so the per-thread state is a
-// handful of registers and the inputs are read straight from HBM/L2.
-//
-// The arithmetic follows getcape_ml (src/xcape/fortran/CAPE_CODE_model_lev.f90
-// :97-564; getcape_pl in CAPE_CODE_pressure_lev.f90:174-642 is the same
-// routine) operation for operation, in FP32 with the ML accumulators in FP64
-// (:183).  Two loop-invariant hoists keep the results unchanged:
-//   * log(p2/p1) is evaluated once per sub-step instead of once per
-//     iteration (p1, p2 do not change inside the iteration, :460-462);
-//   * in the liquid-only adiabats the ice term lhs*(qi2-qi1)/(cpm*tbar) is
-//     identically zero (qi1 = qi2 = 0) and is not evaluated, nor is getqvi
-//     whose product with fice = 0 it would be.
-#include "xc_common.cuh"
+// cape_kernel.cu -- CAPE/CIN kernels for sm_103a: one thread per column,
+// running getcape_col (cape_column.cuh).
+#include "cape_column.cuh"
 #include "xc_kernels.h"
 
 namespace xc {
-
-// Environment of one level (:232-240).
-struct Env {
-  float p, t, td, pi, q, th, thv;
-};
-
-__device__ __forceinline__ Env make_env(float pin, float tin, float tdin) {
-  Env e;
-  e.p = 100.0f * pin;
-  e.t = 273.15f + tin;
-  e.td = 273.15f + tdin;
-  e.pi = powf(e.p * RP00, RDDCP);
-  e.q = getqvs(e.p, e.td);
-  e.th = e.t / e.pi;
-  e.thv = e.th * (1.0f + REPS * e.q) / (1.0f + e.q);
-  return e;
-}
-
-// Reader of one assembled column: level 1 is the surface, level j >= 2 is
-// input level (start - 2 + j) (0-based) of the column.
-template <typename T, int GRID>
-struct ColumnReader {
-  const T *p;   // GRID 1/3: this column's p; GRID 2: shared p1d
-  const T *t;   // this column's t
-  const T *td;  // this column's td
-  float ps, ts, tds;
-  int base;     // start - 2 (so that input index = base + j)
-
-  __device__ __forceinline__ void level(int j, float &pin, float &tin, float &tdin) const {
-    if (j == 1) {
-      pin = ps;
-      tin = ts;
-      tdin = tds;
-    } else {
-      int m = base + j;
-      pin = ldf(p + m);
-      tin = ldf(t + m);
-      tdin = ldf(td + m);
-    }
-  }
-  __device__ __forceinline__ float level_p(int j) const { return j == 1 ? ps : ldf(p + base + j); }
-  __device__ __forceinline__ Env env(int j) const {
-    float a, b, c;
-    level(j, a, b, c);
-    return make_env(a, b, c);
-  }
-};
-
-struct CapeResult {
-  float cape, cin, z_out;
-  int mulvl, status;
-  int nsub, niter;
-};
-
-// One sub-step of the moist adiabat (:417-498).  Returns false when the
-// iteration did not converge within 100 steps (:465-474).
-template <bool ICE, bool PSEUDO>
-__device__ __forceinline__ bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
-                                        float &ql2, float &qi2, float &qt, int &niter) {
-  const float p1 = p2, t1 = t2, th1 = th2, qv1 = qv2, ql1 = ql2, qi1 = qi2;
-  p2 = p2 - dp;
-  const float pi2 = powf(p2 * RP00, RDDCP);
-  const float lp = logf(p2 / p1);
-  float thlast = th1;
-  int i = 0;
-  while (true) {
-    i = i + 1;
-    t2 = thlast * pi2;
-    float fliq, fice, qsat;
-    if (ICE) {
-      fliq = fmax_f(fmin_f((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
-      fice = 1.0f - fliq;
-      qsat = fliq * getqvs(p2, t2) + fice * getqvi(p2, t2);
-    } else {
-      fliq = 1.0f;
-      fice = 0.0f;
-      qsat = getqvs(p2, t2);
-    }
-    qv2 = fmin_f(qt, qsat);
-    if (ICE) {
-      qi2 = fmax_f(fice * (qt - qv2), 0.0f);
-    } else {
-      qi2 = 0.0f;
-    }
-    ql2 = fmax_f(qt - qv2 - qi2, 0.0f);
-
-    const float tbar = 0.5f * (t1 + t2);
-    const float qvbar = 0.5f * (qv1 + qv2);
-    const float qlbar = 0.5f * (ql1 + ql2);
-    const float lhv = LV1 - LV2 * tbar;
-    const float rm = RD + RV * qvbar;
-    float expo;
-    if (ICE) {
-      const float qibar = 0.5f * (qi1 + qi2);
-      const float lhs = LS1 - LS2 * tbar;
-      const float cpm = CP + CPV * qvbar + CPL * qlbar + CPI * qibar;
-      expo = lhv * (ql2 - ql1) / (cpm * tbar) + lhs * (qi2 - qi1) / (cpm * tbar) +
-             (rm / cpm - RDDCP) * lp;
-    } else {
-      const float cpm = CP + CPV * qvbar + CPL * qlbar;
-      expo = lhv * (ql2 - ql1) / (cpm * tbar) + (rm / cpm - RDDCP) * lp;
-    }
-    th2 = th1 * expf(expo);
-    ++niter;
-    if (i > 100) return false;
-    if (fabsf(th2 - thlast) > CONVERGE) {
-      thlast = thlast + 0.3f * (th2 - thlast);
-    } else {
-      break;
-    }
-  }
-  if (PSEUDO) {  // :487-491
-    qt = qv2;
-    ql2 = 0.0f;
-    qi2 = 0.0f;
-  }
-  return true;
-}
-
-// getcape on one assembled column of ncl levels (surface included).
-template <bool ICE, bool PSEUDO, typename T, int GRID>
-__device__ CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
-                                  int source, float ml_depth) {
-  CapeResult r;
-  r.mulvl = -999999;  // :252-253
-  r.z_out = -999999.f;
-  r.cape = 0.0f;
-  r.cin = 0.0f;
-  r.status = 0;
-  r.nsub = 0;
-  r.niter = 0;
-
-  int kmax = 1;
-  double avgth = 0.0, avgqv = 0.0;
-
-  if (source == 2) {
-    // :261-281 -- argmax of theta-e over levels with p >= 500 hPa, strict >.
-    const float p1 = 100.0f * col.ps;
-    if (!(p1 < 50000.0f)) {
-      float maxthe = 0.0f;
-      for (int j = 1; j <= ncl; ++j) {
-        float pin, tin, tdin;
-        col.level(j, pin, tin, tdin);
-        const float p = 100.0f * pin;
-        if (p >= 50000.0f) {
-          const float t = 273.15f + tin;
-          const float td = 273.15f + tdin;
-          const float q = getqvs(p, td);
-          const float the = getthe(p, t, td, q);
-          if (the > maxthe) {
-            r.mulvl = j;
-            maxthe = the;
-            kmax = j;
-          }
-        }
-      }
-    }
-  } else if (source == 3) {
-    // :284-339 -- mixed layer.  One upward pass evaluates the do-while
-    // accumulation (:313-322) and the two guards (:287, :295), which need
-    // z(2) and z(nk).
-    Env prev = col.env(1);
-    const Env e1 = prev;
-    float zprev = 0.0f, z2 = 0.0f;
-    bool active = true;
-    double acc_th = 0.0, acc_qv = 0.0;
-    Env last = prev;
-    for (int j = 2; j <= ncl; ++j) {
-      const Env e = col.env(j);
-      const float dz = -CPDG * 0.5f * (e.thv + prev.thv) * (e.pi - prev.pi);
-      const float z = zprev + dz;
-      if (j == 2) z2 = z;
-      if (active) {
-        if (z <= ml_depth) {
-          acc_th = acc_th + (double)(0.5f * (z - zprev) * (e.th + prev.th));
-          acc_qv = acc_qv + (double)(0.5f * (z - zprev) * (e.q + prev.q));
-        } else {
-          const float th2 = prev.th + (e.th - prev.th) * (ml_depth - zprev) / (z - zprev);
-          const float qv2 = prev.q + (e.q - prev.q) * (ml_depth - zprev) / (z - zprev);
-          acc_th = acc_th + (double)(0.5f * (ml_depth - zprev) * (th2 + prev.th));
-          acc_qv = acc_qv + (double)(0.5f * (ml_depth - zprev) * (qv2 + prev.q));
-          active = false;
-        }
-      }
-      prev = e;
-      zprev = z;
-      last = e;
-    }
-    if (active) {
-      // The loop ran past the top (z(nk) == ml_depth): the interpolation
-      // term is multiplied by ml_depth - z(nk) == 0, th2 = th(nk).
-      acc_th = acc_th + (double)(0.5f * (ml_depth - zprev) * (last.th + last.th));
-      acc_qv = acc_qv + (double)(0.5f * (ml_depth - zprev) * (last.q + last.q));
-    }
-    if ((z2 - 0.0f) > ml_depth) {
-      avgth = e1.th;
-      avgqv = e1.q;
-      kmax = 1;
-    } else if (zprev < ml_depth) {
-      // Top-most level inside the mixed layer: the ascent starts at the top
-      // and never runs (k < nk fails), so cape = cin = 0 and the sentinels
-      // stay.
-      return r;
-    } else {
-      avgth = acc_th / (double)ml_depth;
-      avgqv = acc_qv / (double)ml_depth;
-      kmax = 1;
-    }
-  }
-
-  // Ascent (:355-559).  Levels below kmax only integrate z.
-  Env prev = col.env(1);
-  float z = 0.0f;
-  float th2 = 0.f, p2 = 0.f, t2 = 0.f, qv2 = 0.f, b2 = 0.f, ql2 = 0.f, qi2 = 0.f, qt = 0.f;
-  float narea = 0.0f;
-  long long nsub_total = 0;
-  auto init_parcel = [&](const Env &e) {
-    if (source == 3) {
-      th2 = (float)avgth;
-      qv2 = (float)avgqv;
-      const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2);
-      p2 = e.p;
-      t2 = th2 * e.pi;
-      b2 = G * (thv2 - e.thv) / e.thv;
-    } else {
-      th2 = e.th;
-      p2 = e.p;
-      t2 = e.t;
-      qv2 = e.q;
-      b2 = 0.0f;
-    }
-    ql2 = 0.0f;
-    qi2 = 0.0f;
-    qt = qv2;
-  };
-  if (kmax == 1) init_parcel(prev);
-
-  for (int k = 2; k <= ncl; ++k) {
-    const Env cur = col.env(k);
-    const float dz = -CPDG * 0.5f * (cur.thv + prev.thv) * (cur.pi - prev.pi);
-    z = z + dz;
-    if (k == kmax) {
-      init_parcel(cur);
-    } else if (k > kmax) {
-      const float b1 = b2;
-      float dp = prev.p - cur.p;
-      int nloop;
-      if (dp < pinc) {
-        nloop = 1;
-      } else {
-        const float f = dp / pinc;
-        if (!(f < (float)MAX_SUBSTEPS)) {
-          r.cape = 0.0f;
-          r.cin = 0.0f;
-          r.status |= COL_TOOMANYSTEPS;
-          return r;
-        }
-        nloop = 1 + (int)f;
-        dp = dp / (float)nloop;
-      }
-      nsub_total += nloop;
-      if (nsub_total > MAX_SUBSTEPS) {
-        r.cape = 0.0f;
-        r.cin = 0.0f;
-        r.status |= COL_TOOMANYSTEPS;
-        return r;
-      }
-      for (int n = 1; n <= nloop; ++n) {
-        ++r.nsub;
-        if (!substep<ICE, PSEUDO>(dp, p2, t2, th2, qv2, ql2, qi2, qt, r.niter)) {
-          r.cape = 0.0f;  // :471-473
-          r.cin = 0.0f;
-          r.status |= COL_NOCONV;
-          return r;
-        }
-      }
-      // :501-503
-      const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2 + ql2 + qi2);
-      b2 = G * (thv2 - cur.thv) / cur.thv;
-      // :509-547
-      float parea;
-      if ((b2 >= 0.0f) && (b1 < 0.0f)) {
-        const float frac = b2 / (b2 - b1);
-        parea = 0.5f * b2 * dz * frac;
-        narea = narea - 0.5f * b1 * dz * (1.0f - frac);
-        r.cin = r.cin + narea;
-        narea = 0.0f;
-      } else if ((b2 < 0.0f) && (b1 > 0.0f)) {
-        const float frac = b1 / (b1 - b2);
-        parea = 0.5f * b1 * dz * frac;
-        narea = -0.5f * b2 * dz * (1.0f - frac);
-      } else if (b2 < 0.0f) {
-        parea = 0.0f;
-        narea = narea - 0.5f * dz * (b1 + b2);
-      } else {
-        parea = 0.5f * dz * (b1 + b2);
-        narea = 0.0f;
-      }
-      r.cape = r.cape + fmax_f(0.0f, parea);
-      r.z_out = z;
-      // :554-557
-      if ((cur.p <= 10000.0f) && (b2 < 0.0f)) break;
-    }
-    prev = cur;
-  }
-  return r;
-}
 
 template <typename T, int GRID, bool ICE, bool PSEUDO>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nsub = 0, niter = 0;
-  if (i < a.n2) {
-    const T *tin = (const T *)a.t + i * a.nk;
-    const T *tdin = (const T *)a.td + i * a.nk;
-    const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
-    const float ts = ldf((const T *)a.ts + i);
-    float cape = 0.0f, cin = 0.0f, zo = 0.0f;
-    int mulvl = 0, status = 0;
-    int start = 1;
-    if (GRID != 1) {
-      if (a.start) {
-        start = __ldg(a.start + i);
-      } else {
-        start = pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
-      }
-    }
-    if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
-      if (start < 1 || start > a.nk) {
-        status = COL_BADSTART;
-      } else {
-        ColumnReader<T, GRID> col;
-        col.p = pin;
-        col.t = tin;
-        col.td = tdin;
-        col.ps = ldf((const T *)a.ps + i);
-        col.ts = ts;
-        col.tds = ldf((const T *)a.tds + i);
-        col.base = start - 2;
-        const int ncl = a.nk - start + 2;
-        CapeResult r = getcape_col<ICE, PSEUDO>(col, ncl, a.pinc, a.source, a.ml_depth);
-        cape = r.cape;
-        cin = r.cin;
-        zo = r.z_out;
-        mulvl = r.mulvl;
-        status = r.status;
-        nsub = r.nsub;
-        niter = r.niter;
-      }
-    }
-    a.cape[i] = cape;
-    a.cin[i] = cin;
-    a.mulvl[i] = mulvl;
-    a.z_out[i] = zo;
-    if (a.status) a.status[i] = status;
-  }
+  if (i < a.n2) cape_column_run<T, GRID, ICE, PSEUDO>(a, i, nsub, niter);
   if (a.counters) {
     // Work accounting: warp-reduce, one atomic per warp.
     long long s = nsub, it = niter;

@@ -10,6 +10,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#if defined(__CUDACC__)
+#define XC_HD __host__ __device__ __forceinline__
+#else
+#define XC_HD inline
+#endif
+
 namespace xc {
 
 // ---- CAPE constants (CAPE_CODE_model_lev.f90:188-211) ---------------------
@@ -46,17 +52,17 @@ constexpr long long MAX_SUBSTEPS = 1LL << 22;
 
 // ---- getqvs / getqvi / getthe ----------------------------------------------
 // CAPE_CODE_model_lev.f90:570-581
-__device__ __forceinline__ float getqvs(float p, float t) {
+XC_HD float getqvs(float p, float t) {
   float es = 611.2f * expf(17.67f * (t - 273.15f) / (t - 29.65f));
   return QEPS * es / (p - es);
 }
 // CAPE_CODE_model_lev.f90:587-598
-__device__ __forceinline__ float getqvi(float p, float t) {
+XC_HD float getqvi(float p, float t) {
   float es = 611.2f * expf(21.8745584f * (t - 273.15f) / (t - 7.66f));
   return QEPS * es / (p - es);
 }
 // CAPE_CODE_model_lev.f90:604-620 (x**(-1) is 1/x)
-__device__ __forceinline__ float getthe(float p, float t, float td, float q) {
+XC_HD float getthe(float p, float t, float td, float q) {
   float tlcl;
   if ((td - t) >= -0.1f) {
     tlcl = t;
@@ -69,17 +75,25 @@ __device__ __forceinline__ float getthe(float p, float t, float td, float q) {
 
 // Fortran MIN/MAX as gfortran lowers them for the reference build: the
 // second operand is returned when the comparison fails (NaN included).
-__device__ __forceinline__ float fmin_f(float a, float b) { return a < b ? a : b; }
-__device__ __forceinline__ float fmax_f(float a, float b) { return a > b ? a : b; }
+XC_HD float fmin_f(float a, float b) { return a < b ? a : b; }
+XC_HD float fmax_f(float a, float b) { return a > b ? a : b; }
 
 // ---- input loads ------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ float ldf(const T *ptr) {
-  return (float)__ldg(ptr);
+XC_HD T ld(const T *ptr) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(ptr);
+#else
+  return *ptr;
+#endif
 }
 template <typename T>
-__device__ __forceinline__ double ldd(const T *ptr) {
-  return (double)__ldg(ptr);
+XC_HD float ldf(const T *ptr) {
+  return (float)ld(ptr);
+}
+template <typename T>
+XC_HD double ldd(const T *ptr) {
+  return (double)ld(ptr);
 }
 
 // Masked argmin of ps - p over the levels, 1-based (src/xcape/core.py:286-289):
@@ -88,8 +102,8 @@ __device__ __forceinline__ double ldd(const T *ptr) {
 // with every entry masked gives index 0.  The difference is taken in the
 // input precision T, as numpy does for same-dtype operands.
 template <typename T>
-__device__ __forceinline__ int pres_lev_pos_col(const T *p1d, T ps, int nk) {
-  T best = ps - __ldg(p1d);
+XC_HD int pres_lev_pos_col(const T *p1d, T ps, int nk) {
+  T best = ps - ld(p1d);
   int bi = 0;
   if (!(best < (T)0)) {
     if (best != best) return 1;
@@ -97,7 +111,7 @@ __device__ __forceinline__ int pres_lev_pos_col(const T *p1d, T ps, int nk) {
     best = (T)INFINITY;
   }
   for (int k = 1; k < nk; ++k) {
-    T d = ps - __ldg(p1d + k);
+    T d = ps - ld(p1d + k);
     if (d != d) return k + 1;
     if (d < (T)0) d = (T)INFINITY;
     if (d < best) {
