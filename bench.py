@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--guess", default="plain", choices=["plain", "learned"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one launch per source and exit (for ncu captures)")
     return ap.parse_args()
 
 
@@ -253,6 +255,11 @@ def run_ours(args):
     def step():
         for src, code in SOURCES:
             launch(code, outs[src])
+
+    if args.profile:
+        step()
+        torch.cuda.synchronize()
+        return 0
 
     # work accounting (untimed): sub-steps and iterations per source
     cnt = torch.zeros(2, dtype=torch.int64, device=dev)

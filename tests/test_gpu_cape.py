@@ -208,11 +208,12 @@ def test_cape_edge_cases():
     want = _oracle_cols(1, p[:, :1], t[:, :1], td[:, :1], ps, ts, tds, "surface",
                         "pseudo-liquid", 500.0, 500.0)
     np.testing.assert_allclose(got["cape"][ok], want["cape"][ok], atol=1.0)
-    # start outside 1..nk on the 3-D pressure grid: flagged, zeros
-    st = np.array([0, 41] + [1] * 10, np.int32)
+    # start outside 1..nk on the 3-D pressure grid: flagged, zeros (the
+    # ts > 0 gate comes first, so a cold column stays unflagged)
+    st = np.array([0, 1, 1, 1, 0, 41] + [1] * 6, np.int32)
     got = cape_device(3, p, t, td, ps, ts, tds, "surface", "pseudo-liquid", start=st)
-    assert got["status"][0] & _lib.COL_BADSTART and got["status"][1] & _lib.COL_BADSTART
-    assert got["cape"][0] == 0 and got["cape"][1] == 0
+    assert got["status"][4] & _lib.COL_BADSTART and got["status"][5] & _lib.COL_BADSTART
+    assert got["cape"][4] == 0 and got["cape"][5] == 0 and got["status"][0] == 0
 
 
 def test_host_and_device_paths_agree():
