@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--guess", default="plain", choices=["plain", "learned"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-order", action="store_true",
+                    help="launch the lift in natural column order (no ordering workspace)")
     ap.add_argument("--profile", action="store_true",
                     help="one launch per source and exit (for ncu captures)")
     return ap.parse_args()
@@ -243,6 +245,11 @@ def run_ours(args):
             [torch.empty(n2, dtype=torch.int32, device=dev)] for src, _ in SOURCES}
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
+    ws_bytes = _lib.workspace_bytes(n2)
+    wsbuf = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
+    ws = wsbuf.data_ptr() + (-wsbuf.data_ptr()) % 256
+    order = not args.no_order
+    launches_per_call = 4 if order else 1  # 3 ordering kernels + the lift
 
     def launch(src_code, o, counters=None):
         cape, cin, zout, mulvl = o
@@ -250,7 +257,8 @@ def run_ours(args):
                                     TS.data_ptr(), TDS.data_ptr(), _lib.XC_F32, PINC, src_code,
                                     ML_DEPTH, ADIABAT, None, NLEV, n2, guess, cape.data_ptr(),
                                     cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), None,
-                                    counters, sptr))
+                                    counters, ws if order else None, ws_bytes if order else 0,
+                                    sptr))
 
     def step():
         for src, code in SOURCES:
@@ -353,6 +361,7 @@ def run_ours(args):
                                "ps~U(700,1030) ragged, sources most-unstable + mixed-layer(500 m), "
                                "pseudo-liquid, pinc 500 Pa",
                    "columns": cols_all, "levels": NLEV, "guess": args.guess,
+                   "column_order": "start level x surface dewpoint" if order else "natural",
                    "l2": "inputs (307 MB) larger than L2 (129 MB), no flush"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None,
@@ -364,7 +373,7 @@ def run_ours(args):
         "work": {k: {"substeps": v[0], "iterations": v[1]} for k, v in work.items()},
         "e2e": {"value": cols_all / e2e_dt, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "xcape_gb300.calc_cape(numpy, pinned)"},
-        "gpu_launches": args.steps * len(SOURCES),
+        "gpu_launches": args.steps * len(SOURCES) * launches_per_call,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline and world == 1:

@@ -28,6 +28,8 @@
 #ifndef XCAPE_GB300_H
 #define XCAPE_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -103,12 +105,21 @@ int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const voi
  * three grid kinds.  grid: 1 = sigma/model (p3d per column), 2 = pressure
  * with shared p1d (start_3d optional), 3 = pressure with per-column p3d
  * (start_3d required).  guess: XC_GUESS_*.  counters (nullable, 2 x int64 on
- * the device) receives the total sub-steps and iterations, atomically added. */
+ * the device) receives the total sub-steps and iterations, atomically added.
+ * workspace (nullable, device memory of at least
+ * xc_loopcape_workspace_bytes(n2) bytes, 256-byte aligned) lets the call
+ * reorder the columns by level count and surface dewpoint before the lift,
+ * so that each warp's columns need similar work; the results do not depend
+ * on it.  The call keeps using the workspace until the stream reaches the
+ * end of the launch. */
 int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
                    const void *ts, const void *tds, int dtype, float pinc, int source,
                    float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
                    float *cape, float *cin, int *mulvl, float *z_out, int *status,
-                   long long *counters, void *stream);
+                   long long *counters, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Device workspace that lets xc_loopcape_ex order n2 columns. */
+size_t xc_loopcape_workspace_bytes(int n2);
 
 /* Host-pointer form of xc_loopcape_ex (see the family note above). */
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,

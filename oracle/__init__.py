@@ -56,12 +56,12 @@ def lib():
         for prec, rp, rt in (("f32", _f32p, ctypes.c_float), ("f64", _f64p, ctypes.c_double)):
             f = getattr(L, f"oc_loopcape_ml_{prec}")
             f.argtypes = [rp, rp, rp, rp, rp, rp, rt, _int, rt, _int, _int, _int,
-                          rp, rp, _i32p, rp, _vp, _vp, _vp, _int]
+                          rp, rp, _i32p, rp, _vp, _vp, _vp, _vp, _int]
             f.restype = None
             for name in (f"oc_loopcape_pl1d_{prec}", f"oc_loopcape_pl_{prec}"):
                 f = getattr(L, name)
                 f.argtypes = [rp, rp, rp, rp, rp, rp, rt, _int, rt, _int, _i32p, _int, _int,
-                              rp, rp, _i32p, rp, _vp, _vp, _vp, _int]
+                              rp, rp, _i32p, rp, _vp, _vp, _vp, _vp, _int]
                 f.restype = None
             f = getattr(L, f"oc_bunkers_loop_ml_{prec}")
             f.argtypes = [rp, rp, rp, rp, rp, rp, _int, _int, rp, rp, rp, _int]
@@ -114,12 +114,13 @@ def loopcape(p, t, td, ps, ts, tds, pinc, source, ml_depth, adiabat, start=None,
     nsub = np.zeros(n2, np.int32) if stats else None
     niter = np.zeros(n2, np.int32) if stats else None
     status = np.zeros(n2, np.int32) if stats else None
+    bmin = np.zeros(n2, np.float32) if stats else None
     ptr = lambda a: a.ctypes.data if a is not None else None
     L = lib()
     if start is None:
         getattr(L, f"oc_loopcape_ml_{precision}")(
             p, t, td, ps, ts, tds, pinc, source, ml_depth, adiabat, nk, n2,
-            cape, cin, mulvl, zout, ptr(nsub), ptr(niter), ptr(status), nthreads)
+            cape, cin, mulvl, zout, ptr(nsub), ptr(niter), ptr(status), ptr(bmin), nthreads)
     else:
         start = _c(np.ravel(start), np.int32)
         name = f"oc_loopcape_pl1d_{precision}" if p_is_1d else f"oc_loopcape_pl_{precision}"
@@ -128,10 +129,10 @@ def loopcape(p, t, td, ps, ts, tds, pinc, source, ml_depth, adiabat, start=None,
         else:
             args = (p, t, td)
         getattr(L, name)(*args, ps, ts, tds, pinc, source, ml_depth, adiabat, start, nk, n2,
-                         cape, cin, mulvl, zout, ptr(nsub), ptr(niter), ptr(status), nthreads)
+                         cape, cin, mulvl, zout, ptr(nsub), ptr(niter), ptr(status), ptr(bmin), nthreads)
     out = dict(cape=cape, cin=cin, mulvl=mulvl, z_out=zout)
     if stats:
-        out.update(nsub=nsub, niter=niter, status=status)
+        out.update(nsub=nsub, niter=niter, status=status, bmin=bmin)
     return out
 
 

@@ -116,7 +116,7 @@ static real getthe(real p, real t, real td, real q) {
 static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_B, real ts_B,
                     real tds_B, real pinc, int source, real ml_depth, int adiabat, int nk_in,
                     real *cape_out, real *cin_out, int *mulvl_out, real *z_out_out,
-                    int *nsub_out, int *niter_out, int *status_out) {
+                    int *nsub_out, int *niter_out, int *status_out, float *bmin_out) {
   /* CAPE_CODE_model_lev.f90:188-211 */
   const real g = LIT(9.81);
   const real p00 = LIT(100000.0);
@@ -154,6 +154,7 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
   double avgth = 0.0, avgqv = 0.0; /* real*8, :183 */
   int doit, ice, not_converged;
   int nsub = 0, niter = 0, status = 0;
+  double bmin = INFINITY; /* smallest |buoyancy| met by the ascent (test statistic) */
 
   /* :220-225 -- surface first, then the 3-D levels; then :232-240 */
   for (k = 1; k <= nk; ++k) {
@@ -259,6 +260,7 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
     p2 = p[kmax];
     t2 = th2 * pi2;
     b2 = g * (thv2 - thv[kmax]) / thv[kmax];
+    bmin = fabs((double)b2);
   }
   (void)thv2;
   ql2 = LIT(0.0);
@@ -349,6 +351,7 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
     /* :501-503 */
     thv2 = th2 * (LIT(1.0) + reps * qv2) / (LIT(1.0) + qv2 + ql2 + qi2);
     b2 = g * (thv2 - thv[k]) / thv[k];
+    if (fabs((double)b2) < bmin) bmin = fabs((double)b2);
     dz = -cpdg * LIT(0.5) * (thv[k] + thv[k - 1]) * (pi[k] - pi[k - 1]);
 
     /* :509-547 */
@@ -384,6 +387,7 @@ done:
   if (nsub_out) *nsub_out = nsub;
   if (niter_out) *niter_out = niter;
   if (status_out) *status_out = status;
+  if (bmin_out) *bmin_out = (float)bmin;
   free(buf);
 }
 
@@ -392,15 +396,17 @@ OC_EXPORT void SFX(oc_loopcape_ml)(const real *p3d, const real *t3d, const real 
                                    const real *ps, const real *ts, const real *tds, real pinc,
                                    int source, real ml_depth, int adiabat, int nk, int n2,
                                    real *cape, real *cin, int *mulvl, real *z_out, int *nsub,
-                                   int *niter, int *status, int nthreads) {
+                                   int *niter, int *status, float *bmin, int nthreads) {
   set_threads(nthreads);
   long i;
 #pragma omp parallel for schedule(dynamic, 64)
   for (i = 0; i < n2; ++i) {
+    if (bmin) bmin[i] = INFINITY;
     if (ts[i] > LIT(0.0)) {
       getcape(p3d + (size_t)i * nk, t3d + (size_t)i * nk, td3d + (size_t)i * nk, ps[i], ts[i],
               tds[i], pinc, source, ml_depth, adiabat, nk, &cape[i], &cin[i], &mulvl[i],
-              &z_out[i], nsub ? &nsub[i] : 0, niter ? &niter[i] : 0, status ? &status[i] : 0);
+              &z_out[i], nsub ? &nsub[i] : 0, niter ? &niter[i] : 0, status ? &status[i] : 0,
+              bmin ? &bmin[i] : 0);
     } else {
       cape[i] = LIT(0.0);
       cin[i] = LIT(0.0);
@@ -420,18 +426,19 @@ static void loopcape_pl_common(const real *p3d, long p_stride, const real *t3d, 
                                const real *ps, const real *ts, const real *tds, real pinc,
                                int source, real ml_depth, int adiabat, const int *start, int nk,
                                int n2, real *cape, real *cin, int *mulvl, real *z_out, int *nsub,
-                               int *niter, int *status, int nthreads) {
+                               int *niter, int *status, float *bmin, int nthreads) {
   set_threads(nthreads);
   long i;
 #pragma omp parallel for schedule(dynamic, 64)
   for (i = 0; i < n2; ++i) {
     int st = start[i];
+    if (bmin) bmin[i] = INFINITY;
     if (ts[i] > LIT(0.0) && st >= 1 && st <= nk) {
       int nk_pl_in = nk - st + 1;
       getcape(p3d + (size_t)i * p_stride + (st - 1), t3d + (size_t)i * nk + (st - 1),
               td3d + (size_t)i * nk + (st - 1), ps[i], ts[i], tds[i], pinc, source, ml_depth,
               adiabat, nk_pl_in, &cape[i], &cin[i], &mulvl[i], &z_out[i], nsub ? &nsub[i] : 0,
-              niter ? &niter[i] : 0, status ? &status[i] : 0);
+              niter ? &niter[i] : 0, status ? &status[i] : 0, bmin ? &bmin[i] : 0);
     } else {
       cape[i] = LIT(0.0);
       cin[i] = LIT(0.0);
@@ -449,18 +456,19 @@ OC_EXPORT void SFX(oc_loopcape_pl1d)(const real *t3d, const real *td3d, const re
                                      int source, real ml_depth, int adiabat, const int *start,
                                      int nk, int n2, real *cape, real *cin, int *mulvl,
                                      real *z_out, int *nsub, int *niter, int *status,
-                                     int nthreads) {
+                                     float *bmin, int nthreads) {
   loopcape_pl_common(p1d, 0, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, start, nk,
-                     n2, cape, cin, mulvl, z_out, nsub, niter, status, nthreads);
+                     n2, cape, cin, mulvl, z_out, nsub, niter, status, bmin, nthreads);
 }
 
 OC_EXPORT void SFX(oc_loopcape_pl)(const real *p3d, const real *t3d, const real *td3d,
                                    const real *ps, const real *ts, const real *tds, real pinc,
                                    int source, real ml_depth, int adiabat, const int *start,
                                    int nk, int n2, real *cape, real *cin, int *mulvl, real *z_out,
-                                   int *nsub, int *niter, int *status, int nthreads) {
+                                   int *nsub, int *niter, int *status, float *bmin,
+                                   int nthreads) {
   loopcape_pl_common(p3d, nk, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, start, nk,
-                     n2, cape, cin, mulvl, z_out, nsub, niter, status, nthreads);
+                     n2, cape, cin, mulvl, z_out, nsub, niter, status, bmin, nthreads);
 }
 
 /* ---------------------------------------------------------------------- */

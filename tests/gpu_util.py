@@ -11,7 +11,14 @@ reference's own ``decimal=0`` on CAPE/CIN):
     test: FP32 rounding can leave the damped iteration in a two-value limit
     cycle whose step is just above the 2e-4 K threshold, and a one-ulp
     difference in expf decides whether that cycle is entered.  Such columns
-    are counted, bounded, and excluded from the value comparison.
+    are counted and bounded (2 %); where only the GPU converged, its result
+    must agree with the FP64 oracle;
+  * CIN banks the accumulated negative area only at a negative-to-positive
+    buoyancy crossing (CAPE_CODE_model_lev.f90:509-523), so where the
+    parcel's buoyancy comes within 1e-3 m/s^2 of zero at some level, a
+    rounding-level difference decides whether a whole layer is banked.  CIN
+    may differ only in such columns (the oracle reports the smallest |b|),
+    at most 0.5 % of them; CAPE is continuous there and is always compared.
 """
 import numpy as np
 
@@ -37,8 +44,9 @@ def to_dev(*arrays, dtype=None):
 
 
 def cape_device(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0,
-                start=None, guess=0, counters=False):
-    """Runs xc_loopcape_ex on device copies; returns numpy outputs + status."""
+                start=None, guess=0, counters=False, order=True):
+    """Runs xc_loopcape_ex on device copies; returns numpy outputs + status.
+    order: pass a workspace so that the columns are ordered before the lift."""
     torch = torch_cuda()
     t = np.asarray(t)
     nk = t.shape[-1]
@@ -54,12 +62,17 @@ def cape_device(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_dep
     status = torch.empty(n2, dtype=torch.int32, device="cuda")
     cnt = torch.zeros(2, dtype=torch.int64, device="cuda") if counters else None
     stream = torch.cuda.current_stream().cuda_stream
+    ws, ws_bytes = None, 0
+    if order:
+        ws_bytes = _lib.workspace_bytes(n2)
+        wsbuf = torch.empty(ws_bytes + 256, dtype=torch.uint8, device="cuda")
+        ws = wsbuf.data_ptr() + (-wsbuf.data_ptr()) % 256
     _lib.call("xc_loopcape_ex", grid, P.data_ptr(), T.data_ptr(), TD.data_ptr(), PS.data_ptr(),
               TS.data_ptr(), TDS.data_ptr(), _lib.XC_F64 if f64 else _lib.XC_F32, float(pinc),
               SOURCES.get(source, source), float(ml_depth), ADIABATS.get(adiabat, adiabat),
               ST.data_ptr() if ST is not None else None, nk, n2, guess, cape.data_ptr(),
               cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), status.data_ptr(),
-              cnt.data_ptr() if cnt is not None else None, stream)
+              cnt.data_ptr() if cnt is not None else None, ws, ws_bytes, stream)
     torch.cuda.synchronize()
     out = dict(cape=cape.cpu().numpy(), cin=cin.cpu().numpy(), mulvl=mulvl.cpu().numpy(),
                z_out=zout.cpu().numpy(), status=status.cpu().numpy())
@@ -82,20 +95,45 @@ def thetae_f64(p_hpa, t_c, td_c):
         ((3376.0 / tlcl) - 2.54) * q * (1.0 + 0.81 * q))
 
 
-def compare_cape(got, want, max_status_flip=0.01, what=""):
-    """Asserts the parity criteria above; returns a summary dict."""
+BUOYANCY_TIE = 1e-3  # m/s^2: |b| below this at some level makes CIN's banking a near-tie
+
+
+def _tol(w):
+    return np.maximum(1.0, 1e-3 * np.abs(w))
+
+
+def compare_cape(got, want, want64=None, max_status_flip=0.02, max_cin_ties=0.005, what=""):
+    """Asserts the parity criteria above; returns a summary dict.
+
+    got: GPU outputs with status; want: FP32 oracle with stats (status,
+    bmin); want64: optional FP64 oracle, against which a column that only
+    the GPU brought to convergence is checked.
+    """
     n = got["cape"].size
     noconv_g = (got["status"] & _lib.COL_NOCONV) != 0
     noconv_w = (want["status"] & _lib.COL_NOCONV) != 0
     flip = noconv_g != noconv_w
     assert flip.mean() <= max_status_flip, f"{what}: {flip.sum()} of {n} convergence flips"
-    keep = ~flip
     summary = {"n": n, "flips": int(flip.sum())}
-    for key in ("cape", "cin"):
-        g, w = got[key][keep].astype(np.float64), want[key][keep].astype(np.float64)
-        tol = np.maximum(1.0, 1e-3 * np.abs(w))
-        bad = np.abs(g - w) > tol
-        summary["max_abs_" + key] = float(np.max(np.abs(g - w))) if g.size else 0.0
-        assert not bad.any(), (f"{what}: {key} differs in {bad.sum()} columns, worst "
-                               f"{np.max(np.abs(g - w)):.4f} (got {g[bad][:5]} want {w[bad][:5]})")
+    if want64 is not None:
+        # the GPU converged where FP32 Fortran arithmetic cycled: FP64 agrees
+        only_gpu = flip & ~noconv_g & ((want64["status"] & _lib.COL_NOCONV) == 0)
+        d = np.abs(got["cape"][only_gpu] - want64["cape"][only_gpu])
+        assert np.all(d <= _tol(want64["cape"][only_gpu])), f"{what}: converged flips vs FP64"
+        summary["flips_checked_vs_f64"] = int(only_gpu.sum())
+    keep = ~flip
+    g, w = got["cape"][keep].astype(np.float64), want["cape"][keep].astype(np.float64)
+    bad = np.abs(g - w) > _tol(w)
+    summary["max_abs_cape"] = float(np.max(np.abs(g - w))) if g.size else 0.0
+    assert not bad.any(), (f"{what}: cape differs in {bad.sum()} columns, worst "
+                           f"{np.max(np.abs(g - w)):.4f} (got {g[bad][:5]} want {w[bad][:5]})")
+    g, w = got["cin"][keep].astype(np.float64), want["cin"][keep].astype(np.float64)
+    bad = np.abs(g - w) > _tol(w)
+    tie = want["bmin"][keep] < BUOYANCY_TIE
+    assert not (bad & ~tie).any(), (
+        f"{what}: cin differs in {(bad & ~tie).sum()} columns without a buoyancy near-tie "
+        f"(got {g[bad & ~tie][:5]} want {w[bad & ~tie][:5]})")
+    assert bad.sum() <= max(2, max_cin_ties * n), f"{what}: {bad.sum()} CIN near-ties"
+    summary["cin_ties"] = int(bad.sum())
+    summary["max_abs_cin_nontie"] = float(np.max(np.abs(g - w)[~tie])) if (~tie).any() else 0.0
     return summary

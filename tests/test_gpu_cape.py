@@ -75,21 +75,22 @@ def test_cape_pressure_golden(era5, source, keys, use_torch):
         _close(got, e[key])
 
 
-def _oracle_cols(grid, p, t, td, ps, ts, tds, source, adiabat, pinc, ml_depth, start=None):
+def _oracle_cols(grid, p, t, td, ps, ts, tds, source, adiabat, pinc, ml_depth, start=None,
+                 precision="f32"):
     n2 = int(np.prod(np.shape(t)[:-1]))
     nk = np.shape(t)[-1]
     t2, td2 = np.reshape(t, (n2, nk)), np.reshape(td, (n2, nk))
     sf = [np.ravel(a) for a in (ps, ts, tds)]
     src, adi = SOURCES[source], ADIABATS[adiabat]
+    kw = dict(stats=True, precision=precision)
     if grid == 1:
-        return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi,
-                          stats=True)
+        return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, **kw)
     if grid == 2:
         st = O.pres_lev_pos(p, sf[0]) if start is None else start
         return O.loopcape(np.ravel(p), t2, td2, *sf, pinc, src, ml_depth, adi, start=st,
-                          p_is_1d=True, stats=True)
+                          p_is_1d=True, **kw)
     return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, start=start,
-                      stats=True)
+                      **kw)
 
 
 def _check_mulvl(got, want, p, t, td, ps, ts, tds, grid, start=None):
@@ -105,7 +106,7 @@ def _check_mulvl(got, want, p, t, td, ps, ts, tds, grid, start=None):
         def level(j):
             if j == 1:
                 return np.ravel(ps)[c], np.ravel(ts)[c], np.ravel(tds)[c]
-            m = (start[c] if start is not None else 1) - 2 + j
+            m = (start[c] if start is not None else 1) - 3 + j
             pj = p[m] if grid == 2 else np.reshape(p, (-1, nk))[c, m]
             return pj, t2[c, m], td2[c, m]
         a = thetae_f64(*level(got["mulvl"][c]))
@@ -121,7 +122,9 @@ def test_cape_sigma_synthetic_vs_oracle(source, adiabat):
     p, t, td, ps, ts, tds = S.sigma_c0()
     got = cape_device(1, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0)
     want = _oracle_cols(1, p, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0)
-    compare_cape(got, want, what=f"sigma {source} {adiabat}")
+    want64 = _oracle_cols(1, p, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0,
+                          precision="f64")
+    compare_cape(got, want, want64, what=f"sigma {source} {adiabat}")
     if source == "most-unstable":
         _check_mulvl(got, want, p, t, td, ps, ts, tds, 1)
     else:
@@ -136,7 +139,9 @@ def test_cape_pressure_synthetic_vs_oracle(source, adiabat):
     plev, t, td, ps, ts, tds = S.pressure_c1(shape=(128, 128))
     got = cape_device(2, plev, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0)
     want = _oracle_cols(2, plev, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0)
-    compare_cape(got, want, what=f"pressure {source} {adiabat}")
+    want64 = _oracle_cols(2, plev, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0,
+                          precision="f64")
+    compare_cape(got, want, want64, what=f"pressure {source} {adiabat}")
     if source == "most-unstable":
         st = O.pres_lev_pos(plev, ps.ravel())
         _check_mulvl(got, want, plev, t, td, ps, ts, tds, 2, start=st)
@@ -246,6 +251,10 @@ def test_cape_full_size_pressure_workload():
     b = cape_device(2, plev, t, td, ps, ts, tds, "most-unstable", "pseudo-liquid")
     for k in a:
         np.testing.assert_array_equal(a[k], b[k])
+    # the column ordering changes which warp computes a column, never its result
+    u = cape_device(2, plev, t, td, ps, ts, tds, "most-unstable", "pseudo-liquid", order=False)
+    for k in a:
+        np.testing.assert_array_equal(a[k], u[k])
     perm = np.random.default_rng(5).permutation(n2)
     t2, td2 = t.reshape(n2, -1)[perm], td.reshape(n2, -1)[perm]
     c = cape_device(2, plev, t2, td2, ps.ravel()[perm], ts.ravel()[perm], tds.ravel()[perm],

@@ -91,7 +91,7 @@ def test_fortran_method_needs_reference(p_t_td_3d, p_t_td_surface):
 
 def _declared_entry_points():
     text = open(os.path.join(ROOT, "include", "xcape_gb300.h")).read()
-    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(xc_\w+)\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|size_t|const char \*)\s*(xc_\w+)\(", text, re.M)))
 
 
 def test_library_exports_every_declared_symbol():

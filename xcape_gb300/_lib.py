@@ -42,7 +42,8 @@ SIGNATURES = {
     "xc_loopcape_ml": [_vp] * 6 + [_i, _f, _i, _f, _i, _i, _i] + [_vp] * 5 + [_vp],
     "xc_loopcape_pl1d": [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i] + [_vp] * 5 + [_vp],
     "xc_loopcape_pl": [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i] + [_vp] * 5 + [_vp],
-    "xc_loopcape_ex": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 6 + [_vp],
+    "xc_loopcape_ex": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 6
+    + [_vp, ctypes.c_size_t, _vp],
     "xc_loopcape_ex_host": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 5
     + [_vp],
     "xc_calc_srh": [_i] + [_vp] * 10 + [_i, _vp, _d, _d, _i, _i] + [_vp] * 5 + [_vp],
@@ -87,6 +88,8 @@ def lib():
                 fn = getattr(L, name)
                 fn.argtypes = argtypes
                 fn.restype = ctypes.c_int
+            L.xc_loopcape_workspace_bytes.restype = ctypes.c_size_t
+            L.xc_loopcape_workspace_bytes.argtypes = [_i]
             L.xc_last_error.restype = ctypes.c_char_p
             L.xc_last_error.argtypes = []
             L.xc_version.restype = ctypes.c_char_p
@@ -110,4 +113,10 @@ def version():
 
 def exported_symbols():
     """Names of the entry points declared in include/xcape_gb300.h."""
-    return sorted(list(SIGNATURES) + ["xc_last_error", "xc_version"])
+    return sorted(list(SIGNATURES) + ["xc_last_error", "xc_version",
+                                      "xc_loopcape_workspace_bytes"])
+
+
+def workspace_bytes(n2):
+    """Device scratch that lets xc_loopcape_ex order n2 columns."""
+    return int(lib().xc_loopcape_workspace_bytes(int(n2)))

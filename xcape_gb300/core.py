@@ -128,6 +128,15 @@ class _Batch:
             return None
         return a.data_ptr() if self.torch else a.ctypes.data
 
+    def workspace(self, nbytes):
+        """A 256-byte aligned device scratch buffer (torch's caching
+        allocator), kept alive on the batch until the call returns."""
+        import torch
+        buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
+        self._ws = buf
+        ptr = buf.data_ptr()
+        return ptr + (-ptr) % 256, nbytes
+
     def empty(self, n, kind):
         if self.torch:
             import torch
@@ -243,7 +252,8 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
              float(ml_depth), adi, None, b.nk, b.n2, gs, b.ptr(cape), b.ptr(cin), b.ptr(mulvl),
              b.ptr(zout), None)
     if b.torch:
-        _lib.call("xc_loopcape_ex", *args_, None, b.stream)
+        ws, ws_bytes = b.workspace(_lib.workspace_bytes(b.n2))
+        _lib.call("xc_loopcape_ex", *args_, None, ws, ws_bytes, b.stream)
     else:
         _lib.call("xc_loopcape_ex_host", *args_, None)
     shp = _out_shape(original_shape)

@@ -7,9 +7,12 @@ namespace xc {
 
 template <typename T, int GRID, bool ICE, bool PSEUDO>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nsub = 0, niter = 0;
-  if (i < a.n2) cape_column_run<T, GRID, ICE, PSEUDO>(a, i, nsub, niter);
+  if (t < a.n2) {
+    const long long i = a.perm ? (long long)__ldg(a.perm + t) : t;
+    cape_column_run<T, GRID, ICE, PSEUDO>(a, i, nsub, niter);
+  }
   if (a.counters) {
     // Work accounting: warp-reduce, one atomic per warp.
     long long s = nsub, it = niter;
@@ -28,6 +31,126 @@ template <typename T>
 __global__ void pres_lev_pos_kernel(const T *p1d, const T *ps, int nk, long long n2, int *start) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n2) start[i] = pres_lev_pos_col<T>(p1d, __ldg(ps + i), nk);
+}
+
+// ---- column ordering ---------------------------------------------------------
+// Warps run in lockstep, so a warp pays for its slowest column at every
+// sub-step and for its tallest column at the end.  Sorting the columns by
+// (start level, surface dewpoint) groups columns with equal level counts and
+// similar moisture -- hence similar iteration counts -- into the same warp.
+// The sort is a counting sort over ORDER_BUCKETS buckets; order inside a
+// bucket is whatever the atomics give, which changes no result (each column
+// is still computed by one thread and written to its own index).
+
+template <typename T, int GRID>
+__device__ __forceinline__ int order_bucket(const CapeArgs &a, long long i) {
+  int start = 1;
+  if (GRID != 1)
+    start = a.start ? __ldg(a.start + i)
+                    : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
+  start = start < 0 ? 0 : (start > ORDER_START_CAP ? ORDER_START_CAP : start);
+  const float tds = ldf((const T *)a.tds + i);
+  int bin = ORDER_TD_BINS - 1;  // NaN dewpoints share the last bin
+  if (tds == tds) {
+    const float x = (tds + 40.0f) * (ORDER_TD_BINS / 80.0f);
+    bin = x <= 0.0f ? 0 : (x >= (float)(ORDER_TD_BINS - 1) ? ORDER_TD_BINS - 1 : (int)x);
+  }
+  return start * ORDER_TD_BINS + bin;
+}
+
+template <typename T, int GRID>
+__global__ void order_bucket_kernel(CapeArgs a, unsigned short *bucket, unsigned *hist) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n2) return;
+  const int b = order_bucket<T, GRID>(a, i);
+  bucket[i] = (unsigned short)b;
+  atomicAdd(hist + b, 1u);
+}
+
+// Exclusive scan of the ORDER_BUCKETS counters in place: one block of 1024
+// threads, 16 consecutive counters per thread.
+__global__ void __launch_bounds__(1024) order_scan_kernel(unsigned *hist) {
+  constexpr int PER = ORDER_BUCKETS / 1024;
+  __shared__ unsigned warp_tot[32];
+  const int tid = threadIdx.x;
+  unsigned v[PER], sum = 0;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    v[j] = hist[tid * PER + j];
+    sum += v[j];
+  }
+  // inclusive scan of `sum` across the block
+  unsigned x = sum;
+  const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    unsigned z = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
+    }
+    warp_tot[lane] = z;
+  }
+  __syncthreads();
+  unsigned run = x - sum + (w > 0 ? warp_tot[w - 1] : 0u);
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    hist[tid * PER + j] = run;
+    run += v[j];
+  }
+}
+
+__global__ void order_scatter_kernel(const unsigned short *bucket, unsigned *offs, int *perm,
+                                     long long n2) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const unsigned pos = atomicAdd(offs + bucket[i], 1u);
+  perm[pos] = (int)i;
+}
+
+static size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t order_workspace_bytes(long long n2) {
+  return round256(sizeof(unsigned) * ORDER_BUCKETS) + round256(sizeof(unsigned short) * n2) +
+         round256(sizeof(int) * n2);
+}
+
+template <typename T, int GRID>
+static void launch_bucket(const CapeArgs &a, unsigned short *bucket, unsigned *hist,
+                          unsigned blocks, cudaStream_t s) {
+  order_bucket_kernel<T, GRID><<<blocks, 256, 0, s>>>(a, bucket, hist);
+}
+
+cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStream_t s) {
+  char *b = (char *)ws;
+  unsigned *hist = (unsigned *)b;
+  unsigned short *bucket = (unsigned short *)(b + round256(sizeof(unsigned) * ORDER_BUCKETS));
+  int *pm = (int *)(b + round256(sizeof(unsigned) * ORDER_BUCKETS) +
+                    round256(sizeof(unsigned short) * a.n2));
+  *perm = pm;
+  if (a.n2 <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * ORDER_BUCKETS, s);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((a.n2 + 255) / 256);
+  if (a.dtype == 0) {
+    if (a.grid == 1) launch_bucket<float, 1>(a, bucket, hist, blocks, s);
+    else if (a.grid == 2) launch_bucket<float, 2>(a, bucket, hist, blocks, s);
+    else launch_bucket<float, 3>(a, bucket, hist, blocks, s);
+  } else {
+    if (a.grid == 1) launch_bucket<double, 1>(a, bucket, hist, blocks, s);
+    else if (a.grid == 2) launch_bucket<double, 2>(a, bucket, hist, blocks, s);
+    else launch_bucket<double, 3>(a, bucket, hist, blocks, s);
+  }
+  order_scan_kernel<<<1, 1024, 0, s>>>(hist);
+  order_scatter_kernel<<<blocks, 256, 0, s>>>(bucket, hist, pm, a.n2);
+  return cudaGetLastError();
 }
 
 // ---- launchers ---------------------------------------------------------------

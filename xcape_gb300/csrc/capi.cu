@@ -113,11 +113,15 @@ int xc_release_workspace(void) {
   return XC_OK;
 }
 
+size_t xc_loopcape_workspace_bytes(int n2) {
+  return n2 > 0 ? xc::order_workspace_bytes(n2) : 0;
+}
+
 int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
                    const void *ts, const void *tds, int dtype, float pinc, int source,
                    float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
                    float *cape, float *cin, int *mulvl, float *z_out, int *status,
-                   long long *counters, void *stream) {
+                   long long *counters, void *workspace, size_t workspace_bytes, void *stream) {
   int rc = check_common(dtype, nk, n2);
   if (rc) return rc;
   rc = check_cape_opts(pinc, source, ml_depth, adiabat);
@@ -151,7 +155,17 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   a.z_out = z_out;
   a.status = status;
   a.counters = counters;
-  cudaError_t e = xc::launch_cape(a, (cudaStream_t)stream);
+  a.perm = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (workspace) {
+    if (workspace_bytes < xc::order_workspace_bytes(n2))
+      return fail(XC_ERR_INVALID, "workspace of %zu bytes is smaller than the %zu needed",
+                  workspace_bytes, xc::order_workspace_bytes(n2));
+    if (((size_t)workspace & 255) != 0) return fail(XC_ERR_INVALID, "workspace must be 256-byte aligned");
+    e = xc::launch_order(a, workspace, &a.perm, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
+  }
+  e = xc::launch_cape(a, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
   return XC_OK;
 }
@@ -162,7 +176,7 @@ int xc_loopcape_ml(const void *p3d, const void *t3d, const void *td3d, const voi
                    int *mulvl, float *z_out, int *status, void *stream) {
   return xc_loopcape_ex(1, p3d, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
                         nullptr, nk, n2, XC_GUESS_PLAIN, cape, cin, mulvl, z_out, status, nullptr,
-                        stream);
+                        nullptr, 0, stream);
 }
 
 int xc_loopcape_pl1d(const void *t3d, const void *td3d, const void *p1d, const void *ps,
@@ -172,7 +186,7 @@ int xc_loopcape_pl1d(const void *t3d, const void *td3d, const void *p1d, const v
                      void *stream) {
   return xc_loopcape_ex(2, p1d, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
                         start_3d, nk, n2, XC_GUESS_PLAIN, cape, cin, mulvl, z_out, status,
-                        nullptr, stream);
+                        nullptr, nullptr, 0, stream);
 }
 
 int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const void *ps,
@@ -182,7 +196,7 @@ int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const voi
                    void *stream) {
   return xc_loopcape_ex(3, p3d, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
                         start_3d, nk, n2, XC_GUESS_PLAIN, cape, cin, mulvl, z_out, status,
-                        nullptr, stream);
+                        nullptr, nullptr, 0, stream);
 }
 
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
@@ -208,6 +222,8 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   const size_t o_cape = cv.take(n2 * 4), o_cin = cv.take(n2 * 4), o_mu = cv.take(n2 * 4),
                o_z = cv.take(n2 * 4);
   const size_t o_stat = status ? cv.take(n2 * 4) : 0;
+  const size_t ord_bytes = xc::order_workspace_bytes(n2);
+  const size_t o_ord = cv.take(ord_bytes);
   void *base = nullptr;
   rc = ws_get(cv.off, &base);
   if (rc) return rc;
@@ -229,7 +245,8 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
                       source, ml_depth, adiabat,
                       (grid != 1 && start_3d) ? (const int *)(b + o_st) : nullptr, nk, n2, guess,
                       (float *)(b + o_cape), (float *)(b + o_cin), (int *)(b + o_mu),
-                      (float *)(b + o_z), status ? (int *)(b + o_stat) : nullptr, nullptr, s);
+                      (float *)(b + o_z), status ? (int *)(b + o_stat) : nullptr, nullptr,
+                      b + o_ord, ord_bytes, s);
   if (rc) return rc;
 #define D2H(dst, off, bytes)                                                         \
   if (e == cudaSuccess) e = cudaMemcpyAsync((dst), b + (off), (bytes), cudaMemcpyDeviceToHost, s)

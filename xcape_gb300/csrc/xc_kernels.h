@@ -21,9 +21,22 @@ struct CapeArgs {
   float *z_out;
   int *status;             // nullable
   long long *counters;     // nullable: [0] += sub-steps, [1] += iterations
+  const int *perm;         // nullable: thread t computes column perm[t]
 };
 
 cudaError_t launch_cape(const CapeArgs &a, cudaStream_t s);
+
+// Column ordering (cape_kernel.cu): a counting sort of the columns by
+// (start level, surface dewpoint) so that the 32 columns of a warp need
+// similar numbers of levels and iterations.  Scratch: ORDER_BUCKETS counters
+// plus a 16-bit bucket and a 32-bit permutation entry per column.
+constexpr int ORDER_START_CAP = 63;
+constexpr int ORDER_TD_BINS = 256;
+constexpr int ORDER_BUCKETS = (ORDER_START_CAP + 1) * ORDER_TD_BINS;
+size_t order_workspace_bytes(long long n2);
+// Carves `ws` (order_workspace_bytes(n2) bytes, 256-byte aligned) and
+// launches the three ordering kernels; on return *perm points into ws.
+cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStream_t s);
 cudaError_t launch_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, long long n2,
                                 int *start, cudaStream_t s);
 
