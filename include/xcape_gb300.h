@@ -59,9 +59,15 @@ extern "C" {
 #define XC_COL_NOCONV 1   /* moist-adiabat iteration passed 100 steps: cape=cin=0 */
 #define XC_COL_BADSTART 2 /* start_3d outside 1..nk: outputs zero              */
 
-/* First guess of the moist-adiabat iteration (xc_loopcape_*_ex). */
-#define XC_GUESS_PLAIN 0   /* thlast = th1, exactly as the reference            */
-#define XC_GUESS_LEARNED 1 /* the loaded guess network (xc_guess_load)          */
+/* Moist-adiabat solver of xc_loopcape_ex (`guess` argument).
+ * XC_GUESS_PLAIN is the reference's iteration: first guess thlast = th1,
+ * damped step 0.3 * (F(x) - x), stop when |F(x) - x| <= 2e-4 K, give up after
+ * 100 steps (CAPE_CODE_model_lev.f90:431-480).  The other modes keep the map
+ * F, the stopping test and the result th2 = F(x), and change how x moves:
+ * a better first guess, then secant steps on F(x) - x. */
+#define XC_GUESS_PLAIN 0
+#define XC_GUESS_LEARNED 1      /* first guess from the trained guess network  */
+#define XC_GUESS_EXTRAPOLATED 2 /* first guess extrapolates the previous step  */
 
 /* Largest supported level count of one column (without the surface). */
 #define XC_MAX_LEVELS 4096

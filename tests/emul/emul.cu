@@ -10,16 +10,16 @@
 
 using namespace xc;
 
-template <typename T, int GRID>
-static void cape_loop(const CapeArgs &a, long long *counters) {
+template <typename T, int GRID, int SOLVER>
+static void cape_loop_s(const CapeArgs &a, long long *counters) {
   const bool ice = a.adiabat >= 3, pseudo = (a.adiabat == 1 || a.adiabat == 3);
   long long s = 0, it = 0;
   for (long long i = 0; i < a.n2; ++i) {
     int nsub = 0, niter = 0;
-    if (ice && pseudo) cape_column_run<T, GRID, true, true>(a, i, nsub, niter);
-    else if (ice) cape_column_run<T, GRID, true, false>(a, i, nsub, niter);
-    else if (pseudo) cape_column_run<T, GRID, false, true>(a, i, nsub, niter);
-    else cape_column_run<T, GRID, false, false>(a, i, nsub, niter);
+    if (ice && pseudo) cape_column_run<T, GRID, true, true, SOLVER>(a, i, nsub, niter);
+    else if (ice) cape_column_run<T, GRID, true, false, SOLVER>(a, i, nsub, niter);
+    else if (pseudo) cape_column_run<T, GRID, false, true, SOLVER>(a, i, nsub, niter);
+    else cape_column_run<T, GRID, false, false, SOLVER>(a, i, nsub, niter);
     s += nsub;
     it += niter;
   }
@@ -29,15 +29,21 @@ static void cape_loop(const CapeArgs &a, long long *counters) {
   }
 }
 
+template <typename T, int GRID>
+static void cape_loop(const CapeArgs &a, long long *counters) {
+  if (a.guess == 0) cape_loop_s<T, GRID, SOLVE_PLAIN>(a, counters);
+  else cape_loop_s<T, GRID, SOLVE_ACCEL>(a, counters);
+}
+
 extern "C" int emu_cape(int grid, const void *p, const void *t, const void *td, const void *ps,
                         const void *ts, const void *tds, int dtype, float pinc, int source,
                         float ml_depth, int adiabat, const int *start, int nk, long long n2,
                         float *cape, float *cin, int *mulvl, float *z_out, int *status,
-                        long long *counters) {
+                        long long *counters, int guess) {
   CapeArgs a;
   a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.ps = ps; a.ts = ts; a.tds = tds;
   a.start = grid == 1 ? nullptr : start; a.pinc = pinc; a.source = source; a.ml_depth = ml_depth;
-  a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = 0; a.cape = cape; a.cin = cin;
+  a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = guess; a.perm = nullptr; a.cape = cape; a.cin = cin;
   a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr;
   if (dtype == 0) {
     if (grid == 1) cape_loop<float, 1>(a, counters);

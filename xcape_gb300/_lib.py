@@ -20,6 +20,7 @@ XC_F64 = 1
 
 XC_GUESS_PLAIN = 0
 XC_GUESS_LEARNED = 1
+XC_GUESS_EXTRAPOLATED = 2
 
 COL_NOCONV = 1
 COL_BADSTART = 2

@@ -43,7 +43,8 @@ _SOURCE = {"surface": 1, "most-unstable": 2, "mixed-layer": 3}
 _ADIABAT = {"pseudo-liquid": 1, "reversible-liquid": 2, "pseudo-ice": 3, "reversible-ice": 4}
 _VERTICAL = {"sigma": 1, "model": 1, "pressure": 2}
 _OUTPUT = {"srh": 1, "all": 2}
-_GUESS = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED}
+_GUESS = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
+          "extrapolated": _lib.XC_GUESS_EXTRAPOLATED}
 
 
 def _is_torch(a):

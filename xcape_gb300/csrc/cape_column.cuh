@@ -72,16 +72,41 @@ struct CapeResult {
   int nsub, niter;
 };
 
+// Moist-adiabat solvers of a sub-step.
+//   SOLVE_PLAIN: the reference's damped fixed point, thlast = th1, step
+//                0.3 * (th2 - thlast) (:431-480).
+//   SOLVE_ACCEL: same map F, same stopping test |F(x) - x| <= 2e-4 and the
+//                same result th2 = F(x), but the first guess extrapolates
+//                the previous sub-step's increment (scaled by the ratio of
+//                the pressure steps) and, from the second evaluation on,
+//                x moves by a secant step on g(x) = F(x) - x.  The fixed
+//                0.3 damping contracts by |1 - 0.3 (1 - F')|, about 0.8 for
+//                the F' ~ -5 of warm saturated sub-steps, and in FP32 it can
+//                lock into a two-value cycle one ulp wide whose step stays
+//                above 2e-4 (the reference then gives up after 100
+//                iterations); the secant step lands on the fixed point.
+constexpr int SOLVE_PLAIN = 0;
+constexpr int SOLVE_ACCEL = 1;
+
+struct SolverState {
+  float dth_prev = 0.0f;  // th2 - th1 of the previous sub-step
+  float dp_prev = 1.0f;   // its pressure step
+  bool have_prev = false;
+};
+
 // One sub-step of the moist adiabat (:417-498).  Returns false when the
 // iteration did not converge within 100 steps (:465-474).
-template <bool ICE, bool PSEUDO>
+template <bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
 XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
-                                        float &ql2, float &qi2, float &qt, int &niter) {
+                                        float &ql2, float &qi2, float &qt, int &niter,
+                                        SolverState &ss) {
   const float p1 = p2, t1 = t2, th1 = th2, qv1 = qv2, ql1 = ql2, qi1 = qi2;
   p2 = p2 - dp;
   const float pi2 = powf(p2 * RP00, RDDCP);
   const float lp = logf(p2 / p1);
   float thlast = th1;
+  float x_prev = 0.0f, f_prev = 0.0f;
+  if (SOLVER == SOLVE_ACCEL && ss.have_prev) thlast = th1 + ss.dth_prev * (dp / ss.dp_prev);
   int i = 0;
   while (true) {
     i = i + 1;
@@ -124,10 +149,27 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     ++niter;
     if (i > 100) return false;
     if (fabsf(th2 - thlast) > CONVERGE) {
-      thlast = thlast + 0.3f * (th2 - thlast);
+      if (SOLVER == SOLVE_ACCEL && i >= 2 && thlast != x_prev) {
+        // secant step on g(x) = F(x) - x; the slope of F is kept in
+        // [-50, 0.5] so that a noisy difference quotient cannot throw x far
+        float s = (th2 - f_prev) / (thlast - x_prev);
+        s = fmin_f(fmax_f(s, -50.0f), 0.5f);
+        x_prev = thlast;
+        f_prev = th2;
+        thlast = thlast + (th2 - thlast) / (1.0f - s);
+      } else {
+        x_prev = thlast;
+        f_prev = th2;
+        thlast = thlast + 0.3f * (th2 - thlast);
+      }
     } else {
       break;
     }
+  }
+  if (SOLVER == SOLVE_ACCEL) {
+    ss.dth_prev = th2 - th1;
+    ss.dp_prev = dp;
+    ss.have_prev = true;
   }
   if (PSEUDO) {  // :487-491
     qt = qv2;
@@ -137,8 +179,25 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   return true;
 }
 
+// Running sum with Kahan compensation (SOLVE_ACCEL) or plain FP32 addition in
+// the reference's order (SOLVE_PLAIN).
+template <bool COMPENSATED>
+struct Acc {
+  float s = 0.0f, c = 0.0f;
+  XC_HD void add(float x) {
+    if (COMPENSATED) {
+      const float y = x - c;
+      const float t = s + y;
+      c = (t - s) - y;
+      s = t;
+    } else {
+      s = s + x;
+    }
+  }
+};
+
 // getcape on one assembled column of ncl levels (surface included).
-template <bool ICE, bool PSEUDO, typename T, int GRID>
+template <bool ICE, bool PSEUDO, int SOLVER, typename T, int GRID>
 XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
                                   int source, float ml_depth) {
   CapeResult r;
@@ -234,6 +293,8 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
   float th2 = 0.f, p2 = 0.f, t2 = 0.f, qv2 = 0.f, b2 = 0.f, ql2 = 0.f, qi2 = 0.f, qt = 0.f;
   float narea = 0.0f;
   long long nsub_total = 0;
+  SolverState ss;
+  Acc<SOLVER == SOLVE_ACCEL> cape_acc, cin_acc;
   auto init_parcel = [&](const Env &e) {
     if (source == 3) {
       th2 = (float)avgth;
@@ -287,7 +348,7 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
       }
       for (int n = 1; n <= nloop; ++n) {
         ++r.nsub;
-        if (!substep<ICE, PSEUDO>(dp, p2, t2, th2, qv2, ql2, qi2, qt, r.niter)) {
+        if (!substep<ICE, PSEUDO, SOLVER>(dp, p2, t2, th2, qv2, ql2, qi2, qt, r.niter, ss)) {
           r.cape = 0.0f;  // :471-473
           r.cin = 0.0f;
           r.status |= COL_NOCONV;
@@ -303,7 +364,7 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
         const float frac = b2 / (b2 - b1);
         parea = 0.5f * b2 * dz * frac;
         narea = narea - 0.5f * b1 * dz * (1.0f - frac);
-        r.cin = r.cin + narea;
+        cin_acc.add(narea);
         narea = 0.0f;
       } else if ((b2 < 0.0f) && (b1 > 0.0f)) {
         const float frac = b1 / (b1 - b2);
@@ -316,13 +377,15 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
         parea = 0.5f * dz * (b1 + b2);
         narea = 0.0f;
       }
-      r.cape = r.cape + fmax_f(0.0f, parea);
+      cape_acc.add(fmax_f(0.0f, parea));
       r.z_out = z;
       // :554-557
       if ((cur.p <= 10000.0f) && (b2 < 0.0f)) break;
     }
     prev = cur;
   }
+  r.cape = cape_acc.s;
+  r.cin = cin_acc.s;
   return r;
 }
 
@@ -330,7 +393,7 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
 // One column of loopcape_ml / loopcape_pl1d / loopcape_pl
 // (CAPE_CODE_model_lev.f90:76-89, CAPE_CODE_pressure_lev.f90:66-82, 151-167):
 // the ts > 0 gate, the start level, getcape, and the outputs of column i.
-template <typename T, int GRID, bool ICE, bool PSEUDO>
+template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
 XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter) {
     const T *tin = (const T *)a.t + i * a.nk;
     const T *tdin = (const T *)a.td + i * a.nk;
@@ -359,7 +422,8 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
         col.tds = ldf((const T *)a.tds + i);
         col.base = start - 3;
         const int ncl = a.nk - start + 2;
-        CapeResult r = getcape_col<ICE, PSEUDO>(col, ncl, a.pinc, a.source, a.ml_depth);
+        CapeResult r =
+            getcape_col<ICE, PSEUDO, SOLVER>(col, ncl, a.pinc, a.source, a.ml_depth);
         cape = r.cape;
         cin = r.cin;
         zo = r.z_out;

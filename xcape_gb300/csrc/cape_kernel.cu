@@ -5,13 +5,13 @@
 
 namespace xc {
 
-template <typename T, int GRID, bool ICE, bool PSEUDO>
+template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nsub = 0, niter = 0;
   if (t < a.n2) {
     const long long i = a.perm ? (long long)__ldg(a.perm + t) : t;
-    cape_column_run<T, GRID, ICE, PSEUDO>(a, i, nsub, niter);
+    cape_column_run<T, GRID, ICE, PSEUDO, SOLVER>(a, i, nsub, niter);
   }
   if (a.counters) {
     // Work accounting: warp-reduce, one atomic per warp.
@@ -154,21 +154,29 @@ cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStre
 }
 
 // ---- launchers ---------------------------------------------------------------
+template <typename T, int GRID, int SOLVER>
+static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaStream_t s) {
+  const bool ice = a.adiabat >= 3;
+  const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
+  if (ice && pseudo)
+    cape_kernel<T, GRID, true, true, SOLVER><<<blocks, threads, 0, s>>>(a);
+  else if (ice)
+    cape_kernel<T, GRID, true, false, SOLVER><<<blocks, threads, 0, s>>>(a);
+  else if (pseudo)
+    cape_kernel<T, GRID, false, true, SOLVER><<<blocks, threads, 0, s>>>(a);
+  else
+    cape_kernel<T, GRID, false, false, SOLVER><<<blocks, threads, 0, s>>>(a);
+}
+
 template <typename T, int GRID>
 static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
   const int threads = 128;
   const unsigned blocks = (unsigned)((a.n2 + threads - 1) / threads);
   if (blocks == 0) return cudaSuccess;
-  const bool ice = a.adiabat >= 3;
-  const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
-  if (ice && pseudo)
-    cape_kernel<T, GRID, true, true><<<blocks, threads, 0, s>>>(a);
-  else if (ice)
-    cape_kernel<T, GRID, true, false><<<blocks, threads, 0, s>>>(a);
-  else if (pseudo)
-    cape_kernel<T, GRID, false, true><<<blocks, threads, 0, s>>>(a);
+  if (a.guess == 0)
+    launch_cape_s<T, GRID, SOLVE_PLAIN>(a, blocks, threads, s);
   else
-    cape_kernel<T, GRID, false, false><<<blocks, threads, 0, s>>>(a);
+    launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s);
   return cudaGetLastError();
 }
 

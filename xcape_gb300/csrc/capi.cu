@@ -128,7 +128,8 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   if (rc) return rc;
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
-  if (guess != XC_GUESS_PLAIN) return fail(XC_ERR_INVALID, "guess %d is not available", guess);
+  if (guess != XC_GUESS_PLAIN && guess != XC_GUESS_EXTRAPOLATED)
+    return fail(XC_ERR_INVALID, "guess %d is not available", guess);
   if (n2 == 0) return XC_OK;
   if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
     return fail(XC_ERR_INVALID, "NULL array argument");
