@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--guess", default="plain", choices=["plain", "learned"])
+    ap.add_argument("--guess", default="plain", choices=["plain", "extrapolated", "learned"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-order", action="store_true",
@@ -233,7 +233,8 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     from xcape_gb300 import _lib
     L = _lib.lib()
-    guess = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED}[args.guess]
+    guess = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
+             "extrapolated": _lib.XC_GUESS_EXTRAPOLATED}[args.guess]
 
     n_total = GRID_SHAPE[0] * GRID_SHAPE[1]
     lo, hi = shard(n_total, world, rank)
