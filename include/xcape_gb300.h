@@ -127,6 +127,28 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
 /* Device workspace that lets xc_loopcape_ex order n2 columns. */
 size_t xc_loopcape_workspace_bytes(int n2);
 
+/* Largest n2 that xc_loopcape_ex_noalloc accepts. */
+#define XC_NOALLOC_MAX_COLUMNS 1048576
+
+/* xc_loopcape_ex for callers that cannot allocate device memory -- a host
+ * framework that owns every byte of the device's memory, a serving process
+ * under a fixed memory budget, a real-time loop that forbids allocation after
+ * start-up.  No counterpart in the reference (its Fortran runs on the host).
+ * Same arguments and results as xc_loopcape_ex (device pointers, columns
+ * ordered before the lift), but the ordering scratch lives in a static
+ * device array inside the library (about 6.1 MiB, held on every GPU that
+ * loads the library until the process exits), so the call allocates nothing.
+ * n2 above XC_NOALLOC_MAX_COLUMNS is rejected with XC_ERR_INVALID.  The first
+ * call on each device looks up the array's device address and should come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be issued one after the other. */
+int xc_loopcape_ex_noalloc(int grid, const void *p, const void *t3d, const void *td3d,
+                           const void *ps, const void *ts, const void *tds, int dtype,
+                           float pinc, int source, float ml_depth, int adiabat,
+                           const int *start_3d, int nk, int n2, int guess, float *cape,
+                           float *cin, int *mulvl, float *z_out, int *status,
+                           long long *counters, void *stream);
+
 /* Host-pointer form of xc_loopcape_ex (see the family note above). */
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
                         const void *ps, const void *ts, const void *tds, int dtype, float pinc,

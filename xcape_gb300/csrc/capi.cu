@@ -460,3 +460,11 @@ int xc_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, int n2, 
 }
 
 }  // extern "C"
+
+namespace xc {
+// Records `msg` as the calling thread's xc_last_error() text; returns code.
+int set_error(int code, const char *msg) {
+  snprintf(g_err, sizeof(g_err), "%s", msg);
+  return code;
+}
+}  // namespace xc

@@ -37,6 +37,9 @@ size_t order_workspace_bytes(long long n2);
 // Carves `ws` (order_workspace_bytes(n2) bytes, 256-byte aligned) and
 // launches the three ordering kernels; on return *perm points into ws.
 cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStream_t s);
+
+// Records msg as the calling thread's xc_last_error() text (capi.cu).
+int set_error(int code, const char *msg);
 cudaError_t launch_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, long long n2,
                                 int *start, cudaStream_t s);
 
