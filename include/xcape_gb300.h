@@ -173,13 +173,28 @@ int xc_calc_srh(int grid, const void *p, const void *t3d, const void *td3d, cons
                 double aglh0, int nk, int n2, double *srh_rm, double *srh_lm, float *rm,
                 float *lm, float *mean6, void *stream);
 
-/* Host-pointer form of xc_calc_srh. */
+/* Precision of the stdheight and SREH stages (xc_calc_srh_ex). */
+#define XC_SRH_REFERENCE 0 /* as the reference: FP64 stdheight and SREH, FP32 Bunkers */
+#define XC_SRH_FP32 1      /* FP32 throughout, Kahan-compensated height and helicity sums */
+
+/* xc_calc_srh with a choice of precision for the height and helicity stages
+ * (xc_calc_srh uses XC_SRH_REFERENCE).  XC_SRH_FP32 trades the FP64 stages
+ * for FP32 ones with compensated sums; its difference from the reference is
+ * stated in the test suite (tests/test_gpu_srh.py) and is far inside
+ * 0.5 m^2/s^2. */
+int xc_calc_srh_ex(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
+                   const void *v3d, const void *ps, const void *ts, const void *tds,
+                   const void *us, const void *vs, int dtype, const int *start_3d, double depth,
+                   double aglh0, int nk, int n2, int precision, double *srh_rm, double *srh_lm,
+                   float *rm, float *lm, float *mean6, void *stream);
+
+/* Host-pointer form of xc_calc_srh_ex. */
 int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
                      const void *u3d, const void *v3d, const void *ps, const void *ts,
                      const void *tds, const void *us, const void *vs, int dtype,
                      const int *start_3d, double depth, double aglh0, int nk, int n2,
-                     double *srh_rm, double *srh_lm, float *rm, float *lm, float *mean6,
-                     void *stream);
+                     int precision, double *srh_rm, double *srh_lm, float *rm, float *lm,
+                     float *mean6, void *stream);
 
 /* Replaces loop_stdheight_ml: stdheight_2D_model_lev.pyf:6-19,
  * stdheight_2D_model_lev.f90:4-34 (+ stdheight_ml :74-160).  All f64. */

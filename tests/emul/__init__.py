@@ -41,7 +41,7 @@ def lib():
         vp, i, f, d, ll = (ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double,
                            ctypes.c_longlong)
         L.emu_cape.argtypes = [i] + [vp] * 6 + [i, f, i, f, i, vp, i, ll] + [vp] * 6 + [i]
-        L.emu_srh.argtypes = [i] + [vp] * 10 + [i, vp, d, d, i, ll] + [vp] * 5
+        L.emu_srh.argtypes = [i] + [vp] * 10 + [i, vp, d, d, i, ll] + [vp] * 5 + [i]
         L.emu_pres_lev_pos.argtypes = [vp, vp, i, i, ll, vp]
         _lib = L
     return _lib

@@ -61,14 +61,22 @@ extern "C" int emu_srh(int grid, const void *p, const void *t, const void *td, c
                        const void *v, const void *ps, const void *ts, const void *tds,
                        const void *us, const void *vs, int dtype, const int *start, double depth,
                        double aglh0, int nk, long long n2, double *srh_rm, double *srh_lm,
-                       float *rm, float *lm, float *mean6) {
+                       float *rm, float *lm, float *mean6, int precision) {
   SrhArgs a;
   a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.u = u; a.v = v; a.ps = ps;
   a.ts = ts; a.tds = tds; a.us = us; a.vs = vs; a.start = grid == 2 ? start : nullptr;
   a.depth = depth; a.aglh0 = aglh0; a.nk = nk; a.n2 = n2; a.srh_rm = srh_rm; a.srh_lm = srh_lm;
-  a.rm = rm; a.lm = lm; a.mean6 = mean6;
+  a.rm = rm; a.lm = lm; a.mean6 = mean6; a.precision = precision;
   for (long long i = 0; i < n2; ++i) {
-    if (dtype == 0) {
+    if (precision == 1) {
+      if (dtype == 0) {
+        if (grid == 1) srh_column_run<float, 1, true>(a, i);
+        else srh_column_run<float, 2, true>(a, i);
+      } else {
+        if (grid == 1) srh_column_run<double, 1, true>(a, i);
+        else srh_column_run<double, 2, true>(a, i);
+      }
+    } else if (dtype == 0) {
       if (grid == 1) srh_column_run<float, 1>(a, i);
       else srh_column_run<float, 2>(a, i);
     } else {

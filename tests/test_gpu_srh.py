@@ -199,3 +199,18 @@ def test_srh_full_size_workload():
     want = O.calc_srh(*sub, depth=3000, vertical_lev="model", output_var="all")
     got = [x.reshape(-1).cpu().numpy()[idx] for x in a]
     _check_all(got, want, 1e-6)
+
+
+@pytest.mark.parametrize("depth", [1000, 3000])
+def test_srh_fp32_precision_vs_fp64(depth):
+    """precision='fp32' (FP32 height and helicity stages, compensated sums)
+    against the oracle run in FP64 throughout: SRH within 0.05 m^2/s^2 --
+    the stated tolerance is 0.5 -- and storm motion within 1e-3 m/s."""
+    for args, vl in ((S.srh_c2(shape=(128, 128)), "model"),
+                     (S.pressure_srh(shape=(96, 96)), "pressure")):
+        got = X.calc_srh(*args, depth=depth, vertical_lev=vl, output_var="all", precision="fp32")
+        want = O.calc_srh(*args, depth=depth, vertical_lev=vl, output_var="all", precision="f64")
+        for g, w in zip(got[:2], want[:2]):
+            np.testing.assert_allclose(g, w, rtol=0, atol=0.05)
+        for g, w in zip(got[2:], want[2:]):
+            np.testing.assert_allclose(g, w, rtol=0, atol=1e-3)

@@ -158,7 +158,7 @@ def test_emulated_pres_lev_pos(dtype):
     np.testing.assert_array_equal(st, O.pres_lev_pos(plev, ps))
 
 
-def _emu_srh(grid, p, t, td, u, v, ps, ts, tds, us, vs, depth):
+def _emu_srh(grid, p, t, td, u, v, ps, ts, tds, us, vs, depth, precision=0):
     L = emul.lib()
     f64 = any(np.asarray(a).dtype == np.float64 for a in (p, t, td, u, v, ps, ts, tds, us, vs))
     dt = np.float64 if f64 else np.float32
@@ -168,7 +168,8 @@ def _emu_srh(grid, p, t, td, u, v, ps, ts, tds, us, vs, depth):
     srm, slm = np.empty(n2), np.empty(n2)
     rm, lm, mean = (np.empty((n2, 2), np.float32) for _ in range(3))
     L.emu_srh(grid, *[a.ctypes.data for a in arrs], int(f64), None, float(depth), 2.0, nk, n2,
-              srm.ctypes.data, slm.ctypes.data, rm.ctypes.data, lm.ctypes.data, mean.ctypes.data)
+              srm.ctypes.data, slm.ctypes.data, rm.ctypes.data, lm.ctypes.data, mean.ctypes.data,
+              precision)
     return (srm, slm, rm[:, 0], rm[:, 1], lm[:, 0], lm[:, 1], mean[:, 0], mean[:, 1])
 
 
@@ -203,3 +204,19 @@ def test_emulated_srh_decreasing_heights():
     ps = p[..., 0] * 1.2
     args = (p, t, td, u, v, ps, ts, tds, us, vs)
     _srh_same(_emu_srh(1, *args, 3000), args, 1, 3000)
+
+
+@pytest.mark.parametrize("depth", (1000, 3000))
+def test_emulated_fp32_srh_vs_fp64_oracle(soundings, depth):
+    """precision=XC_SRH_FP32 (FP32 height and helicity with compensated
+    sums) against the oracle run in FP64 throughout: SRH within 0.05
+    m^2/s^2 (the stated tolerance is 0.5), storm motion within 1e-3 m/s."""
+    for args, grid in ((S.srh_c2(shape=(64, 64), nlev=50), 1),
+                       (S.pressure_srh(shape=(48, 48)), 2)):
+        got = _emu_srh(grid, *args, depth, precision=1)
+        vl = "sigma" if grid == 1 else "pressure"
+        want = O.calc_srh(*args, depth=depth, vertical_lev=vl, output_var="all", precision="f64")
+        for g, w in zip(got[:2], want[:2]):
+            np.testing.assert_allclose(g, np.ravel(w), rtol=0, atol=0.05)
+        for g, w in zip(got[2:], want[2:]):
+            np.testing.assert_allclose(g, np.ravel(w), rtol=0, atol=1e-3)

@@ -267,9 +267,20 @@ int xc_calc_srh(int grid, const void *p, const void *t3d, const void *td3d, cons
                 const void *us, const void *vs, int dtype, const int *start_3d, double depth,
                 double aglh0, int nk, int n2, double *srh_rm, double *srh_lm, float *rm,
                 float *lm, float *mean6, void *stream) {
+  return xc_calc_srh_ex(grid, p, t3d, td3d, u3d, v3d, ps, ts, tds, us, vs, dtype, start_3d, depth,
+                        aglh0, nk, n2, XC_SRH_REFERENCE, srh_rm, srh_lm, rm, lm, mean6, stream);
+}
+
+int xc_calc_srh_ex(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
+                   const void *v3d, const void *ps, const void *ts, const void *tds,
+                   const void *us, const void *vs, int dtype, const int *start_3d, double depth,
+                   double aglh0, int nk, int n2, int precision, double *srh_rm, double *srh_lm,
+                   float *rm, float *lm, float *mean6, void *stream) {
   int rc = check_common(dtype, nk, n2);
   if (rc) return rc;
   if (grid != 1 && grid != 2) return fail(XC_ERR_INVALID, "grid must be 1 (sigma) or 2 (pressure, 1-D p)");
+  if (precision != XC_SRH_REFERENCE && precision != XC_SRH_FP32)
+    return fail(XC_ERR_INVALID, "precision must be XC_SRH_REFERENCE or XC_SRH_FP32");
   if ((rm == nullptr) != (lm == nullptr) || (rm == nullptr) != (mean6 == nullptr))
     return fail(XC_ERR_INVALID, "rm, lm and mean6 must be all NULL or all set");
   if (n2 == 0) return XC_OK;
@@ -298,6 +309,7 @@ int xc_calc_srh(int grid, const void *p, const void *t3d, const void *td3d, cons
   a.rm = rm;
   a.lm = lm;
   a.mean6 = mean6;
+  a.precision = precision;
   cudaError_t e = xc::launch_srh(a, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "srh kernel launch");
   return XC_OK;
@@ -307,8 +319,8 @@ int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
                      const void *u3d, const void *v3d, const void *ps, const void *ts,
                      const void *tds, const void *us, const void *vs, int dtype,
                      const int *start_3d, double depth, double aglh0, int nk, int n2,
-                     double *srh_rm, double *srh_lm, float *rm, float *lm, float *mean6,
-                     void *stream) {
+                     int precision, double *srh_rm, double *srh_lm, float *rm, float *lm,
+                     float *mean6, void *stream) {
   int rc = check_common(dtype, nk, n2);
   if (rc) return rc;
   if (grid != 1 && grid != 2) return fail(XC_ERR_INVALID, "grid must be 1 or 2");
@@ -349,12 +361,12 @@ int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
   if (grid == 2 && start_3d) H2D(o_st, start_3d, n2 * 4);
 #undef H2D
   if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
-  rc = xc_calc_srh(grid, b + o_p, b + o_t, b + o_td, b + o_u, b + o_v, b + o_ps, b + o_ts,
-                   b + o_tds, b + o_us, b + o_vs, dtype,
-                   (grid == 2 && start_3d) ? (const int *)(b + o_st) : nullptr, depth, aglh0, nk,
-                   n2, (double *)(b + o_srm), (double *)(b + o_slm),
-                   rm ? (float *)(b + o_rm) : nullptr, rm ? (float *)(b + o_lm) : nullptr,
-                   rm ? (float *)(b + o_mean) : nullptr, s);
+  rc = xc_calc_srh_ex(grid, b + o_p, b + o_t, b + o_td, b + o_u, b + o_v, b + o_ps, b + o_ts,
+                      b + o_tds, b + o_us, b + o_vs, dtype,
+                      (grid == 2 && start_3d) ? (const int *)(b + o_st) : nullptr, depth, aglh0,
+                      nk, n2, precision, (double *)(b + o_srm), (double *)(b + o_slm),
+                      rm ? (float *)(b + o_rm) : nullptr, rm ? (float *)(b + o_lm) : nullptr,
+                      rm ? (float *)(b + o_mean) : nullptr, s);
   if (rc) return rc;
 #define D2H(dst, off, bytes)                                                         \
   if (e == cudaSuccess) e = cudaMemcpyAsync((dst), b + (off), (bytes), cudaMemcpyDeviceToHost, s)

@@ -53,6 +53,43 @@ XC_HD double stdh_step(double Hprev, double Tv, double Tvprev, double P, double 
   return Hprev + ((SH_R * ((Tv + Tvprev) / 2.0) / SH_G)) * (log(P / Pprev));
 }
 
+// FP32 forms of the two stdheight formulas, for the FP32 SRH path (the
+// height is then accumulated with Kahan compensation, see srh_pass1).
+XC_HD float stdh_tv_f(float P, float T, float Td) {
+  const float eps = 0.6219800858985514f;
+  const float Tin = T + 273.15f;
+  const float Tdin = Td + 273.15f;
+  const float E = 6.112f * expf((53.49f - (6808.0f / Tdin) - 5.09f * logf(Tdin)));
+  const float w = eps * (E / (P - E));
+  return Tin * ((w + eps) / (eps * (1.0f + w)));
+}
+XC_HD float stdh_dh_f(float Tv, float Tvprev, float P, float Pprev) {
+  return ((287.04f * ((Tv + Tvprev) / 2.0f) / -9.80665f)) * logf(P / Pprev);
+}
+
+// Real type of the stdheight / SREH stages: double as in the reference, or
+// float for the FP32 path.
+template <bool F32> struct SrhReal { typedef double type; };
+template <> struct SrhReal<true> { typedef float type; };
+
+// Kahan-compensated running sum in R (plain addition for double, where the
+// reference's own order is kept).
+template <typename R>
+struct KSum {
+  R s, c;
+  XC_HD explicit KSum(R init) : s(init), c(0) {}
+  XC_HD void add(R x) {
+    if (sizeof(R) == 4) {
+      const R y = x - c;
+      const R t = s + y;
+      c = (t - s) - y;
+      s = t;
+    } else {
+      s = s + x;
+    }
+  }
+};
+
 // DINTERP2DZ (Bunkers_model_lev.f90:188-236) folded into an upward sweep:
 // the level pair (KP-1, KP) = (lo, hi) matches target h when
 // Z(KP-IM) <= h < Z(KP-IP).  Every match overwrites (highest KP wins).
@@ -123,37 +160,51 @@ struct SrhPass1 {
   float ztop_f;       // f2py-rounded height of the top level (Z(NZ))
 };
 
-// Pass 1 over levels 2..ncl (see the file comment).
-template <bool DEC, typename T>
+// Pass 1 over levels 2..ncl (see the file comment).  F32 selects the FP32
+// height integration (Kahan-compensated) and FP32 helicity inputs.
+template <bool DEC, bool F32, typename T>
 XC_HD SrhPass1 srh_pass1(const SrhColumn<T> &c, int ncl, double depth, double aglh0, float *u6,
                          float *v6) {
+  typedef typename SrhReal<F32>::type R;
   SrhPass1 r;
   r.ktop = 0;
   r.utop = 0.0;
   r.vtop = 0.0;
-  double Pprev = c.ps;
-  double Hprev = aglh0;
-  double Tvprev = stdh_tv(c.ps, c.ts, c.tds);
+  R Pprev = (R)c.ps;
+  KSum<R> Hsum((R)aglh0);
+  R Hprev = (R)aglh0;
+  R Tvprev = F32 ? (R)stdh_tv_f((float)c.ps, (float)c.ts, (float)c.tds)
+                 : (R)stdh_tv(c.ps, c.ts, c.tds);
+  const R rdepth = (R)depth;
   float zprev = (float)aglh0, uprev = (float)c.us, vprev = (float)c.vs;
-  double udprev = c.us, vdprev = c.vs;
+  R udprev = (R)c.us, vdprev = (R)c.vs;
   for (int j = 2; j <= ncl; ++j) {
     const int m = c.base + j;
-    const double P = ldd(c.p + m);
-    const double Tv = stdh_tv(P, ldd(c.t + m), ldd(c.td + m));
-    const double H = stdh_step(Hprev, Tv, Tvprev, P, Pprev);
-    const double ud = ldd(c.u + m), vd = ldd(c.v + m);
+    R P, Tv, H;
+    if (F32) {
+      P = (R)ldf(c.p + m);
+      Tv = (R)stdh_tv_f((float)P, ldf(c.t + m), ldf(c.td + m));
+      Hsum.add((R)stdh_dh_f((float)Tv, (float)Tvprev, (float)P, (float)Pprev));
+      H = Hsum.s;
+    } else {
+      P = (R)ldd(c.p + m);
+      Tv = (R)stdh_tv((double)P, ldd(c.t + m), ldd(c.td + m));
+      H = (R)stdh_step((double)Hprev, (double)Tv, (double)Tvprev, (double)P, (double)Pprev);
+    }
+    const R ud = F32 ? (R)ldf(c.u + m) : (R)ldd(c.u + m);
+    const R vd = F32 ? (R)ldf(c.v + m) : (R)ldd(c.v + m);
     const float zf = (float)H, uf = (float)ud, vf = (float)vd;
     bunkers_bracket<DEC>(zprev, zf, uprev, uf, vprev, vf, u6, v6);
-    if (r.ktop == 0 && H > depth) {
+    if (r.ktop == 0 && H > rdepth) {
       // DCALRELHL :85-95 with INTERP1 (SREH_model_lev.f90:123-129), whose
       // X1 argument is aglh(ktop) passed by reference.
       r.ktop = j;
-      double x1 = H;
-      const double x3 = Hprev;
-      if (x3 == x1) x1 = x1 - (double)0.01f;
-      r.utop = ud + ((udprev - ud) * ((depth - x1) / (x3 - x1)));
-      if (x3 == x1) x1 = x1 - (double)0.01f;
-      r.vtop = vd + ((vdprev - vd) * ((depth - x1) / (x3 - x1)));
+      R x1 = H;
+      const R x3 = Hprev;
+      if (x3 == x1) x1 = x1 - (R)0.01f;
+      r.utop = (double)(ud + ((udprev - ud) * ((rdepth - x1) / (x3 - x1))));
+      if (x3 == x1) x1 = x1 - (R)0.01f;
+      r.vtop = (double)(vd + ((vdprev - vd) * ((rdepth - x1) / (x3 - x1))));
     }
     Pprev = P;
     Hprev = H;
@@ -169,8 +220,12 @@ XC_HD SrhPass1 srh_pass1(const SrhColumn<T> &c, int ncl, double depth, double ag
 }
 
 // Column i of the fused SRH path (core.py:_calc_srh_numpy :473-542).
-template <typename T, int GRID>
+// F32 = false follows the reference's precisions (FP64 stdheight and SREH,
+// FP32 Bunkers); F32 = true runs the stdheight and SREH stages in FP32 with
+// compensated sums.
+template <typename T, int GRID, bool F32 = false>
 XC_HD void srh_column_run(const SrhArgs &a, long long i) {
+  typedef typename SrhReal<F32>::type R;
   SrhColumn<T> c;
   c.p = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
   c.t = (const T *)a.t + i * a.nk;
@@ -195,14 +250,14 @@ XC_HD void srh_column_run(const SrhArgs &a, long long i) {
     u6[k] = VMSG;
     v6[k] = VMSG;
   }
-  SrhPass1 r = srh_pass1<false>(c, ncl, a.depth, a.aglh0, u6, v6);
+  SrhPass1 r = srh_pass1<false, F32>(c, ncl, a.depth, a.aglh0, u6, v6);
   if ((float)a.aglh0 > r.ztop_f) {
     // Z(1) > Z(NZ): DINTERP2DZ switches to the decreasing-height rule.
     for (int k = 0; k < 12; ++k) {
       u6[k] = VMSG;
       v6[k] = VMSG;
     }
-    r = srh_pass1<true>(c, ncl, a.depth, a.aglh0, u6, v6);
+    r = srh_pass1<true, F32>(c, ncl, a.depth, a.aglh0, u6, v6);
   }
   float rm[2], lm[2], mean[2];
   bunkers_finish((float)c.us, (float)c.vs, u6, v6, rm, lm, mean);
@@ -215,25 +270,25 @@ XC_HD void srh_column_run(const SrhArgs &a, long long i) {
     a.mean6[2 * i + 1] = mean[1];
   }
   // Pass 2: DCALRELHL :100-114.
-  const double cu_rm = rm[0], cv_rm = rm[1], cu_lm = lm[0], cv_lm = lm[1];
-  double s_rm = 0.0, s_lm = 0.0;
-  double uprev = c.us, vprev = c.vs;
+  const R cu_rm = rm[0], cv_rm = rm[1], cu_lm = lm[0], cv_lm = lm[1];
+  KSum<R> s_rm((R)0), s_lm((R)0);
+  R uprev = (R)c.us, vprev = (R)c.vs;
   for (int k = 2; k <= r.ktop; ++k) {
-    double uk, vk;
+    R uk, vk;
     if (k == r.ktop) {
-      uk = r.utop;
-      vk = r.vtop;
+      uk = (R)r.utop;
+      vk = (R)r.vtop;
     } else {
-      uk = ldd(c.u + c.base + k);
-      vk = ldd(c.v + c.base + k);
+      uk = F32 ? (R)ldf(c.u + c.base + k) : (R)ldd(c.u + c.base + k);
+      vk = F32 ? (R)ldf(c.v + c.base + k) : (R)ldd(c.v + c.base + k);
     }
-    s_rm = s_rm + (((uk - cu_rm) * (vk - vprev)) - ((vk - cv_rm) * (uk - uprev)));
-    s_lm = s_lm + (((uk - cu_lm) * (vk - vprev)) - ((vk - cv_lm) * (uk - uprev)));
+    s_rm.add(((uk - cu_rm) * (vk - vprev)) - ((vk - cv_rm) * (uk - uprev)));
+    s_lm.add(((uk - cu_lm) * (vk - vprev)) - ((vk - cv_lm) * (uk - uprev)));
     uprev = uk;
     vprev = vk;
   }
-  a.srh_rm[i] = -s_rm;
-  a.srh_lm[i] = -s_lm;
+  a.srh_rm[i] = -(double)s_rm.s;
+  a.srh_lm[i] = -(double)s_lm.s;
 }
 
 // ---- stage columns -----------------------------------------------------------

@@ -5,10 +5,10 @@
 
 namespace xc {
 
-template <typename T, int GRID>
+template <typename T, int GRID, bool F32>
 __global__ void __launch_bounds__(128) srh_fused_kernel(SrhArgs a) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.n2) srh_column_run<T, GRID>(a, i);
+  if (i < a.n2) srh_column_run<T, GRID, F32>(a, i);
 }
 
 __global__ void stdheight_kernel(const double *P, long long p_stride, const double *T,
@@ -41,20 +41,28 @@ static unsigned blocks_for(long long n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
+template <bool F32>
+static void launch_srh_p(const SrhArgs &a, unsigned blocks, cudaStream_t s) {
+  if (a.dtype == 0) {
+    if (a.grid == 1)
+      srh_fused_kernel<float, 1, F32><<<blocks, 128, 0, s>>>(a);
+    else
+      srh_fused_kernel<float, 2, F32><<<blocks, 128, 0, s>>>(a);
+  } else {
+    if (a.grid == 1)
+      srh_fused_kernel<double, 1, F32><<<blocks, 128, 0, s>>>(a);
+    else
+      srh_fused_kernel<double, 2, F32><<<blocks, 128, 0, s>>>(a);
+  }
+}
+
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s) {
   const unsigned blocks = blocks_for(a.n2, 128);
   if (blocks == 0) return cudaSuccess;
-  if (a.dtype == 0) {
-    if (a.grid == 1)
-      srh_fused_kernel<float, 1><<<blocks, 128, 0, s>>>(a);
-    else
-      srh_fused_kernel<float, 2><<<blocks, 128, 0, s>>>(a);
-  } else {
-    if (a.grid == 1)
-      srh_fused_kernel<double, 1><<<blocks, 128, 0, s>>>(a);
-    else
-      srh_fused_kernel<double, 2><<<blocks, 128, 0, s>>>(a);
-  }
+  if (a.precision == 1)
+    launch_srh_p<true>(a, blocks, s);
+  else
+    launch_srh_p<false>(a, blocks, s);
   return cudaGetLastError();
 }
 

@@ -53,6 +53,7 @@ struct SrhArgs {
   long long n2;
   double *srh_rm, *srh_lm;
   float *rm, *lm, *mean6;  // nullable, [n2][2]
+  int precision;           // 0: reference precisions (FP64 stdheight/SREH), 1: FP32
 };
 
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
