@@ -68,6 +68,11 @@ extern "C" {
 #define XC_GUESS_PLAIN 0
 #define XC_GUESS_LEARNED 1      /* first guess from the trained guess network  */
 #define XC_GUESS_EXTRAPOLATED 2 /* first guess extrapolates the previous step  */
+#define XC_GUESS_SECANT 3       /* first guess th1 (the reference's), secant steps */
+
+/* Parameters of the guess network (3 -> 64 -> 64 -> 1, ReLU), flat:
+ * W1[64][3] b1[64] W2[64][64] b2[64] w3[64] b3. */
+#define XC_GUESS_NPARAM 4481
 
 /* Largest supported level count of one column (without the surface). */
 #define XC_MAX_LEVELS 4096
@@ -248,6 +253,38 @@ int xc_loop_sreh_pl(const double *u, const double *v, const double *aglh, const 
  * it is host numpy code. */
 int xc_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, int n2, int *start_3d,
                     void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Learned first guess (no counterpart in the reference)                  */
+/* ---------------------------------------------------------------------- */
+/* The network maps a saturated parcel's (target pressure, theta-e, total
+ * water) to its temperature at the end of a sub-step.  All pointers below are
+ * device memory except where stated; calls are asynchronous on `stream`. */
+
+/* Loads the network that XC_GUESS_LEARNED uses on the current device
+ * (weights: XC_GUESS_NPARAM floats, host memory if on_device == 0).
+ * Synchronises `stream`. */
+int xc_guess_set_weights(const float *weights, int on_device, void *stream);
+
+/* n training pairs drawn with `seed`: saturated parcels, p 100..1050 hPa,
+ * T -80..40 degC, pressure steps 1..25 hPa, each solved with the plain
+ * (reference) iteration.  feats [n][3], targets [n] (normalised end
+ * temperature), iters [n] (iterations used, negative if it gave up). */
+int xc_guess_pairs(long long n, unsigned long long seed, float *feats, float *targets, int *iters,
+                   void *stream);
+
+/* Adds the gradient of the mean squared error over the n pairs to grad
+ * [XC_GUESS_NPARAM] and the loss to *loss (both must be zeroed first). */
+int xc_guess_grad(const float *weights, const float *feats, const float *targets, long long n,
+                  float *grad, float *loss, void *stream);
+
+/* One Adam step (step >= 1) on the FP32 weights; zeroes grad. */
+int xc_guess_adam(float *weights, float *grad, float *m, float *v, float lr, int step,
+                  void *stream);
+
+/* Batched inference: out [n] = network(feats [n][3]). */
+int xc_guess_eval(const float *weights, const float *feats, long long n, float *out,
+                  void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* Library services                                                       */

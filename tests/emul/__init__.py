@@ -40,7 +40,9 @@ def lib():
         L = ctypes.CDLL(OUT)
         vp, i, f, d, ll = (ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double,
                            ctypes.c_longlong)
-        L.emu_cape.argtypes = [i] + [vp] * 6 + [i, f, i, f, i, vp, i, ll] + [vp] * 6 + [i]
+        L.emu_cape.argtypes = [i] + [vp] * 6 + [i, f, i, f, i, vp, i, ll] + [vp] * 6 + [i, vp]
+        L.emu_guess_eval.argtypes = [vp, f, f, f]
+        L.emu_guess_eval.restype = f
         L.emu_srh.argtypes = [i] + [vp] * 10 + [i, vp, d, d, i, ll] + [vp] * 5 + [i]
         L.emu_pres_lev_pos.argtypes = [vp, vp, i, i, ll, vp]
         _lib = L

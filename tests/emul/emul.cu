@@ -16,10 +16,11 @@ static void cape_loop_s(const CapeArgs &a, long long *counters) {
   long long s = 0, it = 0;
   for (long long i = 0; i < a.n2; ++i) {
     int nsub = 0, niter = 0;
-    if (ice && pseudo) cape_column_run<T, GRID, true, true, SOLVER>(a, i, nsub, niter);
-    else if (ice) cape_column_run<T, GRID, true, false, SOLVER>(a, i, nsub, niter);
-    else if (pseudo) cape_column_run<T, GRID, false, true, SOLVER>(a, i, nsub, niter);
-    else cape_column_run<T, GRID, false, false, SOLVER>(a, i, nsub, niter);
+    const float *w = a.guess_w;
+    if (ice && pseudo) cape_column_run<T, GRID, true, true, SOLVER>(a, i, nsub, niter, w);
+    else if (ice) cape_column_run<T, GRID, true, false, SOLVER>(a, i, nsub, niter, w);
+    else if (pseudo) cape_column_run<T, GRID, false, true, SOLVER>(a, i, nsub, niter, w);
+    else cape_column_run<T, GRID, false, false, SOLVER>(a, i, nsub, niter, w);
     s += nsub;
     it += niter;
   }
@@ -31,20 +32,24 @@ static void cape_loop_s(const CapeArgs &a, long long *counters) {
 
 template <typename T, int GRID>
 static void cape_loop(const CapeArgs &a, long long *counters) {
-  if (a.guess == 0) cape_loop_s<T, GRID, SOLVE_PLAIN>(a, counters);
-  else cape_loop_s<T, GRID, SOLVE_ACCEL>(a, counters);
+  switch (a.guess) {
+    case 0: cape_loop_s<T, GRID, SOLVE_PLAIN>(a, counters); break;
+    case 1: cape_loop_s<T, GRID, SOLVE_LEARNED>(a, counters); break;
+    case 2: cape_loop_s<T, GRID, SOLVE_ACCEL>(a, counters); break;
+    default: cape_loop_s<T, GRID, SOLVE_SECANT>(a, counters); break;
+  }
 }
 
 extern "C" int emu_cape(int grid, const void *p, const void *t, const void *td, const void *ps,
                         const void *ts, const void *tds, int dtype, float pinc, int source,
                         float ml_depth, int adiabat, const int *start, int nk, long long n2,
                         float *cape, float *cin, int *mulvl, float *z_out, int *status,
-                        long long *counters, int guess) {
+                        long long *counters, int guess, const float *guess_w) {
   CapeArgs a;
   a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.ps = ps; a.ts = ts; a.tds = tds;
   a.start = grid == 1 ? nullptr : start; a.pinc = pinc; a.source = source; a.ml_depth = ml_depth;
   a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = guess; a.perm = nullptr; a.cape = cape; a.cin = cin;
-  a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr;
+  a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr; a.guess_w = guess_w;
   if (dtype == 0) {
     if (grid == 1) cape_loop<float, 1>(a, counters);
     else if (grid == 2) cape_loop<float, 2>(a, counters);
@@ -92,4 +97,8 @@ extern "C" void emu_pres_lev_pos(const void *p1d, const void *ps, int dtype, int
   for (long long i = 0; i < n2; ++i)
     start[i] = dtype == 0 ? pres_lev_pos_col<float>((const float *)p1d, ((const float *)ps)[i], nk)
                           : pres_lev_pos_col<double>((const double *)p1d, ((const double *)ps)[i], nk);
+}
+
+extern "C" float emu_guess_eval(const float *w, float f0, float f1, float f2) {
+  return guess_eval(w, f0, f1, f2);
 }

@@ -1,0 +1,49 @@
+"""CPU checks of the learned-guess machinery: BF16 rounding, the network's
+per-thread evaluation (the code the CAPE kernel runs, built for the host),
+and the learned / secant solver modes of the column routine against the FP64
+oracle.  A first guess only changes where the iteration starts: whatever the
+network says, the stopping test is the reference's, so the results must stay
+as close to FP64 as the plain FP32 iteration -- checked here with an
+untrained (random) network, the worst case."""
+import numpy as np
+import pytest
+
+import oracle as O
+from xcape_gb300 import guess as G
+from xcape_gb300 import synthetic as S
+
+from guess_ref import forward
+
+emul = pytest.importorskip("emul")
+if emul.nvcc() is None:
+    pytest.skip("nvcc not available", allow_module_level=True)
+
+
+def test_bf16_round_matches_torch():
+    torch = pytest.importorskip("torch")
+    x = np.random.default_rng(0).normal(0, 3, 10000).astype(np.float32)
+    x[:4] = [0.0, -0.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9]  # exact ties round to even
+    want = torch.from_numpy(x).to(torch.bfloat16).to(torch.float32).numpy()
+    np.testing.assert_array_equal(G.bf16_round(x), want)
+
+
+def test_host_guess_eval_matches_numpy():
+    L = emul.lib()
+    w = G.bf16_round(G.init_weights(3, 0.5))
+    x = np.random.default_rng(1).uniform(-1, 1, (64, 3)).astype(np.float32)
+    want = forward(w, x, bf16_hidden=False)[0]
+    got = np.array([L.emu_guess_eval(w.ctypes.data, *map(float, r)) for r in x])
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("guess", [1, 3])
+def test_emulated_learned_and_secant_modes_vs_fp64(guess):
+    from test_kernel_emulation import _emu_cape, _oracle
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(16, 48))
+    w = G.bf16_round(G.init_weights(5, 1.5))
+    got = _emu_cape(2, plev, t, td, ps, ts, tds, 1, 1, guess=guess, guess_w=w)
+    ref = _oracle(2, plev, t, td, ps, ts, tds, 1, 1, precision="f64")
+    conv = (ref["status"] & 1) == 0
+    assert not np.any((got["status"] & 1) & conv)
+    d = np.abs(got["cape"][conv].astype(np.float64) - ref["cape"][conv])
+    assert np.all(d <= np.maximum(1.0, 1e-3 * ref["cape"][conv])), d.max()

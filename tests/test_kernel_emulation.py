@@ -25,7 +25,7 @@ ADIABATS = (1, 2, 3, 4)
 
 
 def _emu_cape(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0,
-              start=None, guess=0):
+              start=None, guess=0, guess_w=None):
     L = emul.lib()
     f64 = any(np.asarray(a).dtype == np.float64 for a in (p, t, td, ps, ts, tds))
     dt = np.float64 if f64 else np.float32
@@ -38,10 +38,12 @@ def _emu_cape(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth
                mulvl=np.empty(n2, np.int32), z_out=np.empty(n2, np.float32),
                status=np.empty(n2, np.int32))
     cnt = np.zeros(2, np.int64)
+    gw = None if guess_w is None else np.ascontiguousarray(guess_w, np.float32)
     L.emu_cape(grid, *[a.ctypes.data for a in arrs], int(f64), pinc, source, ml_depth, adiabat,
                None if st is None else st.ctypes.data, nk, n2, out["cape"].ctypes.data,
                out["cin"].ctypes.data, out["mulvl"].ctypes.data, out["z_out"].ctypes.data,
-               out["status"].ctypes.data, cnt.ctypes.data, guess)
+               out["status"].ctypes.data, cnt.ctypes.data, guess,
+               None if gw is None else gw.ctypes.data)
     out["counters"] = cnt
     return out
 

@@ -21,6 +21,8 @@ XC_F64 = 1
 XC_GUESS_PLAIN = 0
 XC_GUESS_LEARNED = 1
 XC_GUESS_EXTRAPOLATED = 2
+XC_GUESS_SECANT = 3
+XC_GUESS_NPARAM = 4481
 
 COL_NOCONV = 1
 COL_BADSTART = 2
@@ -60,6 +62,11 @@ SIGNATURES = {
     "xc_loop_sreh_ml": [_vp] * 10 + [_d, _i, _i, _vp, _vp, _vp],
     "xc_loop_sreh_pl": [_vp] * 10 + [_d, _vp, _i, _i, _vp, _vp, _vp],
     "xc_pres_lev_pos": [_vp, _vp, _i, _i, _i, _vp, _vp],
+    "xc_guess_set_weights": [_vp, _i, _vp],
+    "xc_guess_pairs": [ctypes.c_longlong, ctypes.c_ulonglong, _vp, _vp, _vp, _vp],
+    "xc_guess_grad": [_vp, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp],
+    "xc_guess_adam": [_vp, _vp, _vp, _vp, _f, _i, _vp],
+    "xc_guess_eval": [_vp, _vp, ctypes.c_longlong, _vp, _vp],
     "xc_release_workspace": [],
 }
 

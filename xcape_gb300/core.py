@@ -44,7 +44,7 @@ _ADIABAT = {"pseudo-liquid": 1, "reversible-liquid": 2, "pseudo-ice": 3, "revers
 _VERTICAL = {"sigma": 1, "model": 1, "pressure": 2}
 _OUTPUT = {"srh": 1, "all": 2}
 _GUESS = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
-          "extrapolated": _lib.XC_GUESS_EXTRAPOLATED}
+          "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT}
 
 
 def _is_torch(a):
@@ -245,6 +245,9 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
     if method != "cuda":
         raise ValueError("invalid method")
 
+    if gs == _lib.XC_GUESS_LEARNED:
+        from . import guess as _guess
+        _guess.ensure_loaded()
     b = _Batch([t, td], [ps, ts, tds], p, grid)
     cape, cin, zout = (b.empty(b.n2, "f4") for _ in range(3))
     mulvl = b.empty(b.n2, "i4")

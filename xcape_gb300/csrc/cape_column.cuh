@@ -15,6 +15,7 @@
 //     identically zero (qi1 = qi2 = 0) and is not evaluated, nor is getqvi
 //     whose product with fice = 0 it would be.
 #pragma once
+#include "guess_mlp.cuh"
 #include "xc_common.cuh"
 #include "xc_kernels.h"
 
@@ -85,13 +86,22 @@ struct CapeResult {
 //                lock into a two-value cycle one ulp wide whose step stays
 //                above 2e-4 (the reference then gives up after 100
 //                iterations); the secant step lands on the fixed point.
+//   SOLVE_LEARNED: first guess from the guess network (guess_mlp.cuh) when
+//                the parcel was saturated at the end of the previous
+//                sub-step, th1 otherwise; secant steps as SOLVE_ACCEL.
+//   SOLVE_SECANT: first guess th1 (the reference's), secant steps -- the
+//                baseline that shows what the network's guess saves.
 constexpr int SOLVE_PLAIN = 0;
 constexpr int SOLVE_ACCEL = 1;
+constexpr int SOLVE_LEARNED = 2;
+constexpr int SOLVE_SECANT = 3;
 
 struct SolverState {
   float dth_prev = 0.0f;  // th2 - th1 of the previous sub-step
   float dp_prev = 1.0f;   // its pressure step
   bool have_prev = false;
+  bool saturated = false;       // condensate present at the end of the previous sub-step
+  const float *guess_w = nullptr;  // guess network parameters (SOLVE_LEARNED)
 };
 
 // One sub-step of the moist adiabat (:417-498).  Returns false when the
@@ -107,6 +117,12 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   float thlast = th1;
   float x_prev = 0.0f, f_prev = 0.0f;
   if (SOLVER == SOLVE_ACCEL && ss.have_prev) thlast = th1 + ss.dth_prev * (dp / ss.dp_prev);
+  if (SOLVER == SOLVE_LEARNED && ss.saturated) {
+    float f0, f1, f2;
+    guess_features(p2, getthe(p1, t1, t1, qv1), qt, f0, f1, f2);
+    const float t2g = GUESS_T_MID + GUESS_T_SCALE * guess_eval(ss.guess_w, f0, f1, f2);
+    if (t2g > 150.0f && t2g < 350.0f) thlast = t2g / pi2;  // else keep th1
+  }
   int i = 0;
   while (true) {
     i = i + 1;
@@ -149,7 +165,7 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     ++niter;
     if (i > 100) return false;
     if (fabsf(th2 - thlast) > CONVERGE) {
-      if (SOLVER == SOLVE_ACCEL && i >= 2 && thlast != x_prev) {
+      if (SOLVER != SOLVE_PLAIN && i >= 2 && thlast != x_prev) {
         // secant step on g(x) = F(x) - x; the slope of F is kept in
         // [-50, 0.5] so that a noisy difference quotient cannot throw x far
         float s = (th2 - f_prev) / (thlast - x_prev);
@@ -171,6 +187,7 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     ss.dp_prev = dp;
     ss.have_prev = true;
   }
+  if (SOLVER == SOLVE_LEARNED) ss.saturated = ql2 + qi2 > 0.0f;
   if (PSEUDO) {  // :487-491
     qt = qv2;
     ql2 = 0.0f;
@@ -199,7 +216,7 @@ struct Acc {
 // getcape on one assembled column of ncl levels (surface included).
 template <bool ICE, bool PSEUDO, int SOLVER, typename T, int GRID>
 XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
-                                  int source, float ml_depth) {
+                                  int source, float ml_depth, const float *guess_w = nullptr) {
   CapeResult r;
   r.mulvl = -999999;  // :252-253
   r.z_out = -999999.f;
@@ -294,7 +311,8 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
   float narea = 0.0f;
   long long nsub_total = 0;
   SolverState ss;
-  Acc<SOLVER == SOLVE_ACCEL> cape_acc, cin_acc;
+  ss.guess_w = guess_w;
+  Acc<SOLVER != SOLVE_PLAIN> cape_acc, cin_acc;
   auto init_parcel = [&](const Env &e) {
     if (source == 3) {
       th2 = (float)avgth;
@@ -394,7 +412,8 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
 // (CAPE_CODE_model_lev.f90:76-89, CAPE_CODE_pressure_lev.f90:66-82, 151-167):
 // the ts > 0 gate, the start level, getcape, and the outputs of column i.
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
-XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter) {
+XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter,
+                           const float *guess_w = nullptr) {
     const T *tin = (const T *)a.t + i * a.nk;
     const T *tdin = (const T *)a.td + i * a.nk;
     const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
@@ -423,7 +442,7 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
         col.base = start - 3;
         const int ncl = a.nk - start + 2;
         CapeResult r =
-            getcape_col<ICE, PSEUDO, SOLVER>(col, ncl, a.pinc, a.source, a.ml_depth);
+            getcape_col<ICE, PSEUDO, SOLVER>(col, ncl, a.pinc, a.source, a.ml_depth, guess_w);
         cape = r.cape;
         cin = r.cin;
         zo = r.z_out;

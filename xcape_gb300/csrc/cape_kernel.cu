@@ -7,11 +7,18 @@ namespace xc {
 
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
+  extern __shared__ float guess_sm[];  // the guess network, SOLVE_LEARNED only
+  const float *gw = nullptr;
+  if (SOLVER == SOLVE_LEARNED) {
+    for (int k = threadIdx.x; k < GUESS_NPARAM; k += blockDim.x) guess_sm[k] = a.guess_w[k];
+    __syncthreads();
+    gw = guess_sm;
+  }
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nsub = 0, niter = 0;
   if (t < a.n2) {
     const long long i = a.perm ? (long long)__ldg(a.perm + t) : t;
-    cape_column_run<T, GRID, ICE, PSEUDO, SOLVER>(a, i, nsub, niter);
+    cape_column_run<T, GRID, ICE, PSEUDO, SOLVER>(a, i, nsub, niter, gw);
   }
   if (a.counters) {
     // Work accounting: warp-reduce, one atomic per warp.
@@ -158,25 +165,30 @@ template <typename T, int GRID, int SOLVER>
 static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaStream_t s) {
   const bool ice = a.adiabat >= 3;
   const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
+  const size_t sm = SOLVER == SOLVE_LEARNED ? sizeof(float) * GUESS_NPARAM : 0;
   if (ice && pseudo)
-    cape_kernel<T, GRID, true, true, SOLVER><<<blocks, threads, 0, s>>>(a);
+    cape_kernel<T, GRID, true, true, SOLVER><<<blocks, threads, sm, s>>>(a);
   else if (ice)
-    cape_kernel<T, GRID, true, false, SOLVER><<<blocks, threads, 0, s>>>(a);
+    cape_kernel<T, GRID, true, false, SOLVER><<<blocks, threads, sm, s>>>(a);
   else if (pseudo)
-    cape_kernel<T, GRID, false, true, SOLVER><<<blocks, threads, 0, s>>>(a);
+    cape_kernel<T, GRID, false, true, SOLVER><<<blocks, threads, sm, s>>>(a);
   else
-    cape_kernel<T, GRID, false, false, SOLVER><<<blocks, threads, 0, s>>>(a);
+    cape_kernel<T, GRID, false, false, SOLVER><<<blocks, threads, sm, s>>>(a);
 }
 
+// guess codes (include/xcape_gb300.h): 0 plain, 1 learned, 2 extrapolated,
+// 3 plain first guess with secant steps.
 template <typename T, int GRID>
 static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
   const int threads = 128;
   const unsigned blocks = (unsigned)((a.n2 + threads - 1) / threads);
   if (blocks == 0) return cudaSuccess;
-  if (a.guess == 0)
-    launch_cape_s<T, GRID, SOLVE_PLAIN>(a, blocks, threads, s);
-  else
-    launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s);
+  switch (a.guess) {
+    case 0: launch_cape_s<T, GRID, SOLVE_PLAIN>(a, blocks, threads, s); break;
+    case 1: launch_cape_s<T, GRID, SOLVE_LEARNED>(a, blocks, threads, s); break;
+    case 2: launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s); break;
+    default: launch_cape_s<T, GRID, SOLVE_SECANT>(a, blocks, threads, s); break;
+  }
   return cudaGetLastError();
 }
 

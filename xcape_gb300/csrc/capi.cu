@@ -80,6 +80,30 @@ int ws_get(size_t bytes, void **out) {
   return XC_OK;
 }
 
+// The guess network used by XC_GUESS_LEARNED: a static device array per
+// device, filled by xc_guess_set_weights.
+__device__ float g_guess_w[XC_GUESS_NPARAM];
+constexpr int kMaxGuessDevices = 64;
+std::mutex g_guess_mu;
+bool g_guess_loaded[kMaxGuessDevices] = {};
+
+int guess_weights(const float **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxGuessDevices) return fail(XC_ERR_INVALID, "device %d out of range", dev);
+  {
+    std::lock_guard<std::mutex> lk(g_guess_mu);
+    if (!g_guess_loaded[dev])
+      return fail(XC_ERR_INVALID, "no guess network is loaded on device %d (xc_guess_set_weights)", dev);
+  }
+  void *p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_guess_w);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+  *out = (const float *)p;
+  return XC_OK;
+}
+
 // Carves 256-byte aligned slices out of one workspace allocation.
 struct Carver {
   size_t off = 0;
@@ -128,8 +152,13 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   if (rc) return rc;
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
-  if (guess != XC_GUESS_PLAIN && guess != XC_GUESS_EXTRAPOLATED)
-    return fail(XC_ERR_INVALID, "guess %d is not available", guess);
+  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_SECANT)
+    return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
+  const float *guess_w = nullptr;
+  if (guess == XC_GUESS_LEARNED) {
+    rc = guess_weights(&guess_w);
+    if (rc) return rc;
+  }
   if (n2 == 0) return XC_OK;
   if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
     return fail(XC_ERR_INVALID, "NULL array argument");
@@ -157,6 +186,7 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   a.status = status;
   a.counters = counters;
   a.perm = nullptr;
+  a.guess_w = guess_w;
   cudaError_t e = cudaSuccess;
   if (workspace) {
     if (workspace_bytes < xc::order_workspace_bytes(n2))
@@ -469,6 +499,59 @@ int xc_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, int n2, 
   if (n2 == 0) return XC_OK;
   cudaError_t e = xc::launch_pres_lev_pos(p1d, ps, dtype, nk, n2, start_3d, (cudaStream_t)stream);
   return e == cudaSuccess ? XC_OK : cuda_fail(e, "pres_lev_pos kernel launch");
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int xc_guess_set_weights(const float *weights, int on_device, void *stream) {
+  if (!weights) return fail(XC_ERR_INVALID, "NULL weights");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxGuessDevices) return fail(XC_ERR_INVALID, "device %d out of range", dev);
+  e = cudaMemcpyToSymbolAsync(g_guess_w, weights, sizeof(float) * XC_GUESS_NPARAM, 0,
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                              (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "loading the guess network");
+  std::lock_guard<std::mutex> lk(g_guess_mu);
+  g_guess_loaded[dev] = true;
+  return XC_OK;
+}
+
+int xc_guess_pairs(long long n, unsigned long long seed, float *feats, float *targets, int *iters,
+                   void *stream) {
+  if (n < 0) return fail(XC_ERR_INVALID, "n is negative");
+  if (n > 0 && (!feats || !targets || !iters)) return fail(XC_ERR_INVALID, "NULL array argument");
+  cudaError_t e = xc::launch_guess_pairs(n, seed, feats, targets, iters, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "guess pair kernel launch");
+}
+
+int xc_guess_grad(const float *weights, const float *feats, const float *targets, long long n,
+                  float *grad, float *loss, void *stream) {
+  if (n < 0) return fail(XC_ERR_INVALID, "n is negative");
+  if (n > 0 && (!weights || !feats || !targets || !grad || !loss))
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  cudaError_t e = xc::launch_guess_grad(weights, feats, targets, 0, n, grad, loss,
+                                        (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "guess training kernel launch");
+}
+
+int xc_guess_adam(float *weights, float *grad, float *m, float *v, float lr, int step,
+                  void *stream) {
+  if (!weights || !grad || !m || !v || step < 1) return fail(XC_ERR_INVALID, "bad Adam arguments");
+  cudaError_t e = xc::launch_guess_adam(weights, grad, m, v, lr, step, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "Adam kernel launch");
+}
+
+int xc_guess_eval(const float *weights, const float *feats, long long n, float *out,
+                  void *stream) {
+  if (n < 0) return fail(XC_ERR_INVALID, "n is negative");
+  if (n > 0 && (!weights || !feats || !out)) return fail(XC_ERR_INVALID, "NULL array argument");
+  cudaError_t e = xc::launch_guess_eval(weights, feats, n, out, (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "guess inference kernel launch");
 }
 
 }  // extern "C"

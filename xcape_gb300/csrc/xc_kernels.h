@@ -22,7 +22,20 @@ struct CapeArgs {
   int *status;             // nullable
   long long *counters;     // nullable: [0] += sub-steps, [1] += iterations
   const int *perm;         // nullable: thread t computes column perm[t]
+  const float *guess_w;    // guess network parameters (device), guess == XC_GUESS_LEARNED
 };
+
+// Guess network (guess_mlp.cu).
+size_t guess_smem_bytes();
+cudaError_t launch_guess_pairs(long long n, unsigned long long seed, float *feats,
+                               float *targets, int *iters, cudaStream_t s);
+cudaError_t launch_guess_grad(const float *w, const float *feats, const float *targets,
+                              long long batch0, long long nb, float *grad, float *loss,
+                              cudaStream_t s);
+cudaError_t launch_guess_adam(float *w, float *grad, float *m, float *v, float lr, int step,
+                              cudaStream_t s);
+cudaError_t launch_guess_eval(const float *w, const float *feats, long long n, float *out,
+                              cudaStream_t s);
 
 cudaError_t launch_cape(const CapeArgs &a, cudaStream_t s);
 

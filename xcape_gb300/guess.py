@@ -1,0 +1,203 @@
+"""The learned first guess of the moist-adiabat iteration.
+
+A 3 -> 64 -> 64 -> 1 ReLU network (``xcape_gb300/csrc/guess_mlp.cuh``) maps a
+saturated parcel's (target pressure, theta-e, total water) to its
+temperature at the end of a sub-step.  ``calc_cape(..., guess='learned')``
+starts each saturated sub-step's iteration there instead of at the previous
+sub-step's theta, and then takes secant steps; the stopping test and the
+result are the reference's.
+
+Everything runs on the GPU through the library:
+  * ``xc_guess_pairs``  -- training pairs, solved by the plain (reference)
+    iteration;
+  * ``xc_guess_grad``   -- forward (hidden layer on the tensor cores, BF16
+    operands, FP32 accumulation) and backward pass of the squared error;
+  * ``xc_guess_adam``   -- Adam on FP32 master weights;
+  * ``xc_guess_eval``   -- batched inference.
+The trained weights are stored rounded to BF16 in
+``xcape_gb300/data/guess_mlp.npz`` with their training metadata, and
+``load()`` hands them to the library (``xc_guess_set_weights``).
+
+    python -m xcape_gb300.guess train [--pairs N] [--epochs E] [--out PATH]
+"""
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _lib
+
+NPARAM = _lib.XC_GUESS_NPARAM
+H = 64
+OFF_W1, OFF_B1, OFF_W2, OFF_B2, OFF_W3, OFF_B3 = 0, 192, 256, 4352, 4416, 4480
+T_MID, T_SCALE = 233.15, 50.0
+DEFAULT_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_mlp.npz")
+
+_loaded = set()
+
+
+def bf16_round(w):
+    """Round float32 values to the nearest BF16 value (ties to even)."""
+    u = np.ascontiguousarray(w, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def init_weights(seed=0, target_mean=0.0):
+    rng = np.random.default_rng(seed)
+    w = np.zeros(NPARAM, np.float32)
+    w[OFF_W1:OFF_B1] = rng.normal(0, np.sqrt(2.0 / 3), 3 * H)
+    w[OFF_B1:OFF_W2] = 0.1
+    w[OFF_W2:OFF_B2] = rng.normal(0, np.sqrt(2.0 / H), H * H)
+    w[OFF_B2:OFF_W3] = 0.1
+    w[OFF_W3:OFF_B3] = rng.normal(0, np.sqrt(1.0 / H), H)
+    w[OFF_B3] = target_mean
+    return w
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("the guess network is trained and evaluated on the GPU")
+    return torch
+
+
+def make_pairs(n, seed=1):
+    """n training pairs as CUDA tensors (feats [n,3], targets [n], iters [n])."""
+    torch = _torch()
+    f = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    it = torch.empty(n, dtype=torch.int32, device="cuda")
+    _lib.call("xc_guess_pairs", n, seed, f.data_ptr(), t.data_ptr(), it.data_ptr(),
+              torch.cuda.current_stream().cuda_stream)
+    return f, t, it
+
+
+def gradient(weights, feats, targets):
+    """(grad [NPARAM], loss) of the mean squared error, on the GPU."""
+    torch = _torch()
+    w = torch.as_tensor(np.asarray(weights, np.float32)).cuda()
+    f = torch.as_tensor(np.asarray(feats, np.float32)).cuda().contiguous()
+    t = torch.as_tensor(np.asarray(targets, np.float32)).cuda().contiguous()
+    g = torch.zeros(NPARAM, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    _lib.call("xc_guess_grad", w.data_ptr(), f.data_ptr(), t.data_ptr(), t.numel(), g.data_ptr(),
+              loss.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return g.cpu().numpy(), float(loss.item())
+
+
+def evaluate(weights, feats):
+    """Network outputs for feats [n, 3] (normalised temperatures)."""
+    torch = _torch()
+    w = torch.as_tensor(np.asarray(weights, np.float32)).cuda()
+    f = torch.as_tensor(feats).cuda().contiguous() if not hasattr(feats, "data_ptr") else feats
+    out = torch.empty(f.shape[0], dtype=torch.float32, device="cuda")
+    _lib.call("xc_guess_eval", w.data_ptr(), f.data_ptr(), f.shape[0], out.data_ptr(),
+              torch.cuda.current_stream().cuda_stream)
+    return out
+
+
+def train(n_pairs=1 << 21, epochs=12, batch=8192, lr=2e-3, seed=7, log=print):
+    """Trains the network on the GPU; returns (weights rounded to BF16, meta)."""
+    torch = _torch()
+    t0 = time.time()
+    feats, targets, iters = make_pairs(n_pairs, seed)
+    n_val = n_pairs // 32
+    n_tr = n_pairs - n_val
+    fv, tv = feats[n_tr:], targets[n_tr:]
+    w = torch.as_tensor(init_weights(seed, float(targets[:n_tr].mean().item()))).cuda()
+    m = torch.zeros_like(w)
+    v = torch.zeros_like(w)
+    grad = torch.zeros_like(w)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    step = 0
+    curve = []
+    n_batches = n_tr // batch
+    for ep in range(epochs):
+        perm = torch.randperm(n_tr, device="cuda", generator=gen)
+        fe, te = feats[perm].contiguous(), targets[perm].contiguous()
+        lr_ep = lr * (0.5 * (1 + np.cos(np.pi * ep / epochs)))
+        loss.zero_()
+        for b in range(n_batches):
+            step += 1
+            _lib.call("xc_guess_grad", w.data_ptr(), fe[b * batch:].data_ptr(),
+                      te[b * batch:].data_ptr(), batch, grad.data_ptr(), loss.data_ptr(), stream)
+            _lib.call("xc_guess_adam", w.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(),
+                      float(lr_ep), step, stream)
+        rmse_k = float(np.sqrt(loss.item() / n_batches)) * T_SCALE
+        curve.append(rmse_k)
+        if log:
+            log(f"epoch {ep + 1}/{epochs}: train RMS error {rmse_k:.4f} K")
+    w_bf = bf16_round(w.cpu().numpy())
+    pred = evaluate(w_bf, fv)
+    val_rmse = float(torch.sqrt(torch.mean((pred - tv) ** 2)).item()) * T_SCALE
+    it = iters.cpu().numpy()
+    meta = {"version": 1, "pairs": n_pairs, "epochs": epochs, "batch": batch, "lr": lr,
+            "seed": seed, "train_rms_K": curve, "val_rms_K_bf16": val_rmse,
+            "plain_iterations_mean": float(np.abs(it).mean()),
+            "plain_gave_up": int((it < 0).sum()), "seconds": time.time() - t0}
+    if log:
+        log(f"validation RMS error with BF16 weights: {val_rmse:.4f} K")
+    return w_bf, meta
+
+
+def save(path, weights, meta):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    np.savez_compressed(path, weights=np.asarray(weights, np.float32),
+                        meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
+
+
+def read(path=DEFAULT_PATH):
+    with np.load(path) as z:
+        return z["weights"], json.loads(bytes(z["meta"]).decode())
+
+
+def set_weights(weights):
+    """Makes `weights` the network XC_GUESS_LEARNED uses on the current device."""
+    w = np.ascontiguousarray(weights, np.float32)
+    if w.size != NPARAM:
+        raise ValueError(f"expected {NPARAM} parameters, got {w.size}")
+    _lib.call("xc_guess_set_weights", w.ctypes.data, 0, None)
+    try:
+        import torch
+        _loaded.add(torch.cuda.current_device())
+    except Exception:
+        pass
+
+
+def ensure_loaded(path=DEFAULT_PATH):
+    """Loads the stored network on the current device once."""
+    try:
+        import torch
+        dev = torch.cuda.current_device() if torch.cuda.is_available() else None
+    except ImportError:
+        dev = None
+    if dev is not None and dev in _loaded:
+        return
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"guess='learned' needs the trained network ({path}); "
+                                "train it with `python -m xcape_gb300.guess train`")
+    set_weights(read(path)[0])
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m xcape_gb300.guess")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    tr = sub.add_parser("train")
+    tr.add_argument("--pairs", type=int, default=1 << 21)
+    tr.add_argument("--epochs", type=int, default=12)
+    tr.add_argument("--out", default=DEFAULT_PATH)
+    args = ap.parse_args(argv)
+    w, meta = train(n_pairs=args.pairs, epochs=args.epochs)
+    save(args.out, w, meta)
+    print(json.dumps(meta))
+
+
+if __name__ == "__main__":
+    main()
