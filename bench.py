@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--guess", default="plain", choices=["plain", "extrapolated", "learned"])
+    ap.add_argument("--guess", default="plain",
+                    choices=["plain", "extrapolated", "learned", "secant"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-order", action="store_true",
@@ -234,7 +235,10 @@ def run_ours(args):
     from xcape_gb300 import _lib
     L = _lib.lib()
     guess = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
-             "extrapolated": _lib.XC_GUESS_EXTRAPOLATED}[args.guess]
+             "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT}[args.guess]
+    if guess == _lib.XC_GUESS_LEARNED:
+        from xcape_gb300 import guess as guess_net
+        guess_net.ensure_loaded()
 
     n_total = GRID_SHAPE[0] * GRID_SHAPE[1]
     lo, hi = shard(n_total, world, rank)
