@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--guess", default="plain",
-                    choices=["plain", "extrapolated", "learned", "secant"])
+                    choices=["plain", "extrapolated", "learned", "secant", "learned-every"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-order", action="store_true",
@@ -235,8 +235,9 @@ def run_ours(args):
     from xcape_gb300 import _lib
     L = _lib.lib()
     guess = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
-             "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT}[args.guess]
-    if guess == _lib.XC_GUESS_LEARNED:
+             "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT,
+             "learned-every": _lib.XC_GUESS_LEARNED_EVERY}[args.guess]
+    if guess in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY):
         from xcape_gb300 import guess as guess_net
         guess_net.ensure_loaded()
 

@@ -64,11 +64,15 @@ extern "C" {
  * damped step 0.3 * (F(x) - x), stop when |F(x) - x| <= 2e-4 K, give up after
  * 100 steps (CAPE_CODE_model_lev.f90:431-480).  The other modes keep the map
  * F, the stopping test and the result th2 = F(x), and change how x moves:
- * a better first guess, then secant steps on F(x) - x. */
+ * a better first guess, then secant steps on F(x) - x, with approximate
+ * (a few ulp) hardware exp and divides. */
 #define XC_GUESS_PLAIN 0
-#define XC_GUESS_LEARNED 1      /* first guess from the trained guess network  */
+#define XC_GUESS_LEARNED 1      /* extrapolated, with the guess network's guess on the
+                                   first sub-step that starts saturated */
 #define XC_GUESS_EXTRAPOLATED 2 /* first guess extrapolates the previous step  */
 #define XC_GUESS_SECANT 3       /* first guess th1 (the reference's), secant steps */
+#define XC_GUESS_LEARNED_EVERY 4 /* the network's guess on every sub-step that starts
+                                    saturated, th1 on the others; secant steps */
 
 /* Parameters of the guess network (3 -> 64 -> 64 -> 1, ReLU), flat:
  * W1[64][3] b1[64] W2[64][64] b2[64] w3[64] b3. */

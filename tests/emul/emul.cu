@@ -36,7 +36,8 @@ static void cape_loop(const CapeArgs &a, long long *counters) {
     case 0: cape_loop_s<T, GRID, SOLVE_PLAIN>(a, counters); break;
     case 1: cape_loop_s<T, GRID, SOLVE_LEARNED>(a, counters); break;
     case 2: cape_loop_s<T, GRID, SOLVE_ACCEL>(a, counters); break;
-    default: cape_loop_s<T, GRID, SOLVE_SECANT>(a, counters); break;
+    case 3: cape_loop_s<T, GRID, SOLVE_SECANT>(a, counters); break;
+    default: cape_loop_s<T, GRID, SOLVE_LEARNED_ALL>(a, counters); break;
   }
 }
 
@@ -101,4 +102,9 @@ extern "C" void emu_pres_lev_pos(const void *p1d, const void *ps, int dtype, int
 
 extern "C" float emu_guess_eval(const float *w, float f0, float f1, float f2) {
   return guess_eval(w, f0, f1, f2);
+}
+
+extern "C" void emu_guess_pairs(long long n, unsigned long long seed, float *feats,
+                                float *targets, int *iters) {
+  for (long long i = 0; i < n; ++i) iters[i] = guess_pair(seed, i, feats + 3 * i, targets + i);
 }

@@ -3,12 +3,14 @@
 * the training kernel's gradient against a numpy FP64 reference that rounds
   the hidden layer's operands to BF16 as the tensor cores see them;
 * the batched (tensor-core) inference against the same reference;
+* the GPU's training pairs against the host build of the same code;
 * a short training run that cuts the error of the untrained network;
-* what the trained network gains over the method without it: with the same
-  secant solver and the reference's stopping test, the network's first guess
-  against the plain first guess (th1), on the ragged pressure-level workload,
-  counting iterations on the device and checking CAPE against the FP64
-  oracle.
+* what the trained network gains over the method without it, on the ragged
+  pressure-level workload, counting iterations on the device and checking
+  CAPE against the FP64 oracle: with the same secant solver and the
+  reference's stopping test, the network's guess on every saturated
+  sub-step against the plain first guess (th1); and the learned mode
+  against the extrapolated mode it extends.
 """
 import os
 
@@ -34,11 +36,27 @@ def pairs():
 
 
 def test_pairs_are_solved_by_the_plain_iteration(pairs):
-    f, t, it = pairs
-    assert np.all(np.isfinite(f)) and np.all(np.isfinite(t))
-    assert np.mean(np.abs(it)) > 2 and np.all(np.abs(it) >= 1)
-    temps = G.T_MID + G.T_SCALE * t
-    assert temps.min() > 150 and temps.max() < 330
+    f, y, it = pairs
+    assert np.all(np.isfinite(f)) and np.all(np.isfinite(y))
+    assert np.mean(np.abs(it)) > 2 and np.all(it >= 1)
+    assert y.min() > 0 and y.max() < 1.5
+
+
+def test_pairs_match_host_build(pairs):
+    emul = pytest.importorskip("emul")
+    if emul.nvcc() is None:
+        pytest.skip("nvcc not available")
+    f, y, it = pairs
+    n = len(y)
+    fh, yh, ith = (np.zeros((n, 3), np.float32), np.zeros(n, np.float32), np.zeros(n, np.int32))
+    emul.lib().emu_guess_pairs(n, 123, fh.ctypes.data, yh.ctypes.data, ith.ctypes.data)
+    # same draws; CUDA's and glibc's expf/powf/logf differ by an ulp or two,
+    # and the iteration stops anywhere within its 2e-4 K tolerance
+    np.testing.assert_allclose(f, fh, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(y, yh, rtol=0, atol=5e-3)
+    # an ulp can move the stop of the damped iteration by a step either way
+    assert np.mean(it == ith) > 0.8
+    assert np.mean(np.abs(it - ith) <= 1) > 0.98
 
 
 def test_training_gradient_matches_fp64_reference(pairs):
@@ -60,37 +78,60 @@ def test_tensor_core_inference_matches_reference(pairs):
     w = G.bf16_round(G.init_weights(4, 0.3))
     got = G.evaluate(w, f).cpu().numpy()
     want = forward(w, f)[0]
-    np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-4)
+    # FP32 accumulation of the BF16 products can move a pre-activation across
+    # zero where the FP64 sum does not; that bounds the few worst elements
+    np.testing.assert_allclose(got, want, rtol=1e-3, atol=1e-3)
+    assert np.mean(np.abs(got - want) < 1e-4) > 0.99
 
 
 def test_short_training_reduces_error():
-    w, meta = G.train(n_pairs=1 << 16, epochs=3, batch=4096, log=None)
-    assert meta["train_rms_K"][-1] < 0.5 * meta["train_rms_K"][0]
-    assert meta["val_rms_K_bf16"] < 3.0
+    w, meta = G.train(n_pairs=1 << 17, epochs=4, batch=4096, log=None)
+    assert meta["train_rms_y"][-1] < 0.5 * meta["train_rms_y"][0]
+    assert meta["val_rel_rms_bf16"] < 0.3
+
+
+_trained = []
 
 
 def _network():
+    """The stored network, or one trained here when none is stored."""
     if os.path.exists(G.DEFAULT_PATH):
         return G.read()[0]
-    return G.train(n_pairs=1 << 19, epochs=6, log=None)[0]
+    if not _trained:
+        _trained.append(G.train(n_pairs=1 << 20, epochs=8, log=None)[0])
+    return _trained[0]
 
 
-def test_learned_guess_saves_iterations_over_plain_first_guess():
-    w = _network()
-    G.set_weights(w)
-    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(96, 128))
-    base = cape_device(2, plev, t, td, ps, ts, tds, "surface", "pseudo-liquid",
-                       guess=_lib.XC_GUESS_SECANT, counters=True)
-    lrn = cape_device(2, plev, t, td, ps, ts, tds, "surface", "pseudo-liquid",
-                      guess=_lib.XC_GUESS_LEARNED, counters=True)
+def _run(guess, shape=(96, 128)):
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=shape)
+    got = cape_device(2, plev, t, td, ps, ts, tds, "surface", "pseudo-liquid", guess=guess,
+                      counters=True)
     n2 = ps.size
     ref = O.loopcape(plev, t.reshape(n2, -1), td.reshape(n2, -1), ps.ravel(), ts.ravel(),
                      tds.ravel(), 500.0, 1, 500.0, 1, start=O.pres_lev_pos(plev, ps.ravel()),
                      p_is_1d=True, precision="f64", stats=True)
     conv = (ref["status"] & 1) == 0
-    for got in (base, lrn):
-        assert not np.any((got["status"] & 1).astype(bool) & conv)
-        d = np.abs(got["cape"][conv].astype(np.float64) - ref["cape"][conv])
-        assert np.all(d <= np.maximum(1.0, 1e-3 * ref["cape"][conv])), d.max()
+    assert not np.any((got["status"] & 1).astype(bool) & conv)
+    d = np.abs(got["cape"][conv].astype(np.float64) - ref["cape"][conv])
+    assert np.all(d <= np.maximum(1.0, 1e-3 * ref["cape"][conv])), d.max()
+    return got
+
+
+def test_network_guess_saves_iterations_over_plain_first_guess():
+    G.set_weights(_network())
+    base = _run(_lib.XC_GUESS_SECANT)
+    lrn = _run(_lib.XC_GUESS_LEARNED_EVERY)
     assert lrn["nsub_total"] == base["nsub_total"]
-    assert lrn["niter_total"] < base["niter_total"], (lrn["niter_total"], base["niter_total"])
+    # a few percent of relative error on the increment against th1's 100 %
+    assert lrn["niter_total"] < 0.9 * base["niter_total"], (lrn["niter_total"], base["niter_total"])
+
+
+def test_learned_mode_against_extrapolated_mode():
+    G.set_weights(_network())
+    ext = _run(_lib.XC_GUESS_EXTRAPOLATED)
+    lrn = _run(_lib.XC_GUESS_LEARNED)
+    assert lrn["nsub_total"] == ext["nsub_total"]
+    # the network replaces the extrapolation only on the first saturated
+    # sub-step of a column, where the increment of the sub-step that crossed
+    # saturation is a poor predictor
+    assert lrn["niter_total"] < ext["niter_total"], (lrn["niter_total"], ext["niter_total"])

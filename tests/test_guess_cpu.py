@@ -14,6 +14,8 @@ from xcape_gb300 import synthetic as S
 
 from guess_ref import forward
 
+G_P_MID, G_P_SCALE = 55000.0, 45000.0  # guess_mlp.cuh feature scaling
+
 emul = pytest.importorskip("emul")
 if emul.nvcc() is None:
     pytest.skip("nvcc not available", allow_module_level=True)
@@ -36,11 +38,39 @@ def test_host_guess_eval_matches_numpy():
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-5)
 
 
-@pytest.mark.parametrize("guess", [1, 3])
+def emulated_pairs(n, seed):
+    L = emul.lib()
+    f = np.zeros((n, 3), np.float32)
+    y = np.zeros(n, np.float32)
+    it = np.zeros(n, np.int32)
+    L.emu_guess_pairs(n, seed, f.ctypes.data, y.ctypes.data, it.ctypes.data)
+    return f, y, it
+
+
+def test_training_pairs_are_physical():
+    f, y, it = emulated_pairs(20000, 3)
+    p2 = G_P_MID + G_P_SCALE * f[:, 0]
+    assert p2.min() > 9000 and p2.max() < 105000
+    assert np.all(f[:, 2] * 0.02 + 0.01 <= 0.04 + 1e-6)   # qt <= 40 g/kg
+    assert np.all(it > 0), "the plain iteration solves every pair"
+    # the moist-adiabat increment: positive, largest for warm moist parcels
+    assert y.min() > 0 and y.max() < 1.5
+    warm = f[:, 2] > 0.0  # qt > 10 g/kg
+    assert y[warm].mean() > 2 * y[~warm].mean()
+
+
+def test_pairs_are_deterministic():
+    a = emulated_pairs(512, 9)
+    b = emulated_pairs(512, 9)
+    for x, z in zip(a, b):
+        np.testing.assert_array_equal(x, z)
+
+
+@pytest.mark.parametrize("guess", [1, 3, 4])
 def test_emulated_learned_and_secant_modes_vs_fp64(guess):
     from test_kernel_emulation import _emu_cape, _oracle
     plev, t, td, ps, ts, tds = S.pressure_c1(shape=(16, 48))
-    w = G.bf16_round(G.init_weights(5, 1.5))
+    w = G.bf16_round(G.init_weights(5, 0.3))
     got = _emu_cape(2, plev, t, td, ps, ts, tds, 1, 1, guess=guess, guess_w=w)
     ref = _oracle(2, plev, t, td, ps, ts, tds, 1, 1, precision="f64")
     conv = (ref["status"] & 1) == 0

@@ -22,6 +22,7 @@ XC_GUESS_PLAIN = 0
 XC_GUESS_LEARNED = 1
 XC_GUESS_EXTRAPOLATED = 2
 XC_GUESS_SECANT = 3
+XC_GUESS_LEARNED_EVERY = 4
 XC_GUESS_NPARAM = 4481
 
 COL_NOCONV = 1

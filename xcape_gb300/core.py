@@ -44,7 +44,8 @@ _ADIABAT = {"pseudo-liquid": 1, "reversible-liquid": 2, "pseudo-ice": 3, "revers
 _VERTICAL = {"sigma": 1, "model": 1, "pressure": 2}
 _OUTPUT = {"srh": 1, "all": 2}
 _GUESS = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
-          "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT}
+          "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT,
+          "learned-every": _lib.XC_GUESS_LEARNED_EVERY}
 
 
 def _is_torch(a):
@@ -167,8 +168,13 @@ def calc_cape(*args, **kwargs):
     (degC, vertical axis last), ``ps`` (hPa), ``ts``, ``tds`` (degC).
     Keywords: ``source``, ``ml_depth`` (m), ``adiabat``, ``pinc`` (Pa),
     ``method`` (``'cuda'``, ``'dummy'``, ``'fortran'``), ``vertical_lev``, and
-    ``guess`` (``'plain'`` = the reference's first guess of the moist-adiabat
-    iteration, ``'learned'`` = the trained guess network).
+    ``guess``: the moist-adiabat solver. ``'plain'`` is the reference's
+    iteration.  The others keep its stopping test and take secant steps:
+    ``'extrapolated'`` (first guess from the previous sub-step's increment),
+    ``'learned'`` (as extrapolated, with the trained guess network's guess on
+    the first saturated sub-step), ``'secant'`` (the reference's first
+    guess), ``'learned-every'`` (the network's guess on every saturated
+    sub-step).
 
     Returns ``(cape, cin)`` (J/kg, float32) or ``(cape, cin, mulev, zmulev)``
     for ``source='most-unstable'`` (int32 level index counted with the
@@ -245,7 +251,7 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
     if method != "cuda":
         raise ValueError("invalid method")
 
-    if gs == _lib.XC_GUESS_LEARNED:
+    if gs in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY):
         from . import guess as _guess
         _guess.ensure_loaded()
     b = _Batch([t, td], [ps, ts, tds], p, grid)

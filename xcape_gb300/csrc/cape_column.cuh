@@ -79,30 +79,87 @@ struct CapeResult {
 //   SOLVE_ACCEL: same map F, same stopping test |F(x) - x| <= 2e-4 and the
 //                same result th2 = F(x), but the first guess extrapolates
 //                the previous sub-step's increment (scaled by the ratio of
-//                the pressure steps) and, from the second evaluation on,
-//                x moves by a secant step on g(x) = F(x) - x.  The fixed
+//                the pressure steps), the first step divides by 1 - F' with
+//                the slope F' last measured in an earlier sub-step, and
+//                from the second evaluation on x moves by a secant step on
+//                g(x) = F(x) - x.  The fixed
 //                0.3 damping contracts by |1 - 0.3 (1 - F')|, about 0.8 for
 //                the F' ~ -5 of warm saturated sub-steps, and in FP32 it can
 //                lock into a two-value cycle one ulp wide whose step stays
 //                above 2e-4 (the reference then gives up after 100
 //                iterations); the secant step lands on the fixed point.
-//   SOLVE_LEARNED: first guess from the guess network (guess_mlp.cuh) when
-//                the parcel was saturated at the end of the previous
-//                sub-step, th1 otherwise; secant steps as SOLVE_ACCEL.
+//   SOLVE_LEARNED: SOLVE_ACCEL, except on the first sub-step that starts
+//                saturated, where the extrapolation has only the partial
+//                increment of the sub-step that crossed saturation: there
+//                the first guess is th1 plus the guess network's increment
+//                (guess_mlp.cuh).  The network is evaluated once per column,
+//                before the ascent, at the parcel's lifting condensation
+//                level (parcel_lcl_slope), where every thread of a warp
+//                evaluates it together; inside the sub-step loop the
+//                threads that reach saturation at different sub-steps
+//                would evaluate it one after another.
+//   SOLVE_LEARNED_ALL: the network's guess on every sub-step that starts
+//                saturated, th1 on the others; secant steps.
 //   SOLVE_SECANT: first guess th1 (the reference's), secant steps -- the
-//                baseline that shows what the network's guess saves.
+//                method without the network, against which
+//                SOLVE_LEARNED_ALL shows the network's iteration savings.
+// Every mode falls back to its guess without the network when the network's
+// output is out of range.
 constexpr int SOLVE_PLAIN = 0;
 constexpr int SOLVE_ACCEL = 1;
 constexpr int SOLVE_LEARNED = 2;
 constexpr int SOLVE_SECANT = 3;
+constexpr int SOLVE_LEARNED_ALL = 4;
+// A difference quotient of F over points closer than this (K) is too noisy
+// to carry to the next sub-step.
+constexpr float SLOPE_MIN_DX = 1e-3f;
 
 struct SolverState {
   float dth_prev = 0.0f;  // th2 - th1 of the previous sub-step
   float dp_prev = 1.0f;   // its pressure step
+  float slope = 0.0f;     // last difference quotient of F (the map's slope)
   bool have_prev = false;
-  bool saturated = false;       // condensate present at the end of the previous sub-step
-  const float *guess_w = nullptr;  // guess network parameters (SOLVE_LEARNED)
+  bool have_slope = false;
+  bool saturated = false;   // condensate present at the end of the previous sub-step
+  bool sat_start = false;   // the previous sub-step started saturated
+  bool have_lcl = false;    // lcl_y holds the network's output at the parcel's LCL
+  float lcl_y = 0.0f;
+  float lnp = 0.0f;         // ln of the parcel pressure (accelerated modes)
+  const float *guess_w = nullptr;  // guess network parameters (SOLVE_LEARNED*)
 };
+
+// The guess network's output y at the lifting condensation level of a parcel
+// (p, t, td in Pa and K, mixing ratio q): Bolton's (1980) LCL temperature
+// from the temperature and dewpoint, the LCL pressure along the dry
+// adiabat, the features (p_lcl, theta-e, q).  Returns false when the
+// output is out of the network's range.
+XC_HD bool parcel_lcl_slope(const float *w, float p, float t, float td, float q, float &y) {
+  const float tlcl = 56.0f + 1.0f / (1.0f / (td - 56.0f) + logf(t / td) / 800.0f);
+  const float plcl = td < t ? p * powf(tlcl / t, 1.0f / RDDCP) : p;
+  float f0, f1, f2;
+  guess_features(plcl, getthe(p, t, td, q), q, f0, f1, f2);
+  y = guess_eval(w, f0, f1, f2);
+  return y >= GUESS_Y_MIN && y <= GUESS_Y_MAX;
+}
+
+// Dewpoint (K) of mixing ratio q at pressure p (Pa): getqvs solved for T.
+XC_HD float dewpoint_of(float p, float q) {
+  const float a = logf(q * p / (QEPS + q) / 611.2f);
+  return (17.67f * 273.15f - 29.65f * a) / (17.67f - a);
+}
+
+// theta increment of a sub-step from p1 to p2 that starts saturated at
+// (t1, qv1) with total water qt, from the guess network; returns false when
+// the network's output is out of its range.
+XC_HD bool network_increment(const float *w, float p1, float p2, float t1, float qv1, float qt,
+                             float lp, float &dth) {
+  float f0, f1, f2;
+  guess_features(p2, getthe(p1, t1, t1, qv1), qt, f0, f1, f2);
+  const float y = guess_eval(w, f0, f1, f2);
+  if (!(y >= GUESS_Y_MIN && y <= GUESS_Y_MAX)) return false;
+  dth = -GUESS_SLOPE_SCALE * y * lp;
+  return true;
+}
 
 // One sub-step of the moist adiabat (:417-498).  Returns false when the
 // iteration did not converge within 100 steps (:465-474).
@@ -112,16 +169,33 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
                                         SolverState &ss) {
   const float p1 = p2, t1 = t2, th1 = th2, qv1 = qv2, ql1 = ql2, qi1 = qi2;
   p2 = p2 - dp;
-  const float pi2 = powf(p2 * RP00, RDDCP);
-  const float lp = logf(p2 / p1);
+  // The accelerated modes take pi2 and ln(p2/p1) from one logarithm of p2
+  // (ln p1 is the previous sub-step's): one logf and one expf in place of
+  // powf, a divide and logf.  ln(p2/p1) then carries an absolute error of
+  // about 1e-6, and it only scales the dry term (R_m/c_pm - R_d/c_p) ln(p2/p1)
+  // of the exponent, whose prefactor is below 1e-3.
+  constexpr bool ACCEL_MATH = SOLVER != SOLVE_PLAIN;
+  float pi2, lp;
+  if (ACCEL_MATH) {
+    const float lnp2 = logf(p2);
+    lp = lnp2 - ss.lnp;
+    pi2 = expf(RDDCP * (lnp2 - LN_P00));
+    ss.lnp = lnp2;
+  } else {
+    pi2 = powf(p2 * RP00, RDDCP);
+    lp = logf(p2 / p1);
+  }
   float thlast = th1;
   float x_prev = 0.0f, f_prev = 0.0f;
-  if (SOLVER == SOLVE_ACCEL && ss.have_prev) thlast = th1 + ss.dth_prev * (dp / ss.dp_prev);
-  if (SOLVER == SOLVE_LEARNED && ss.saturated) {
-    float f0, f1, f2;
-    guess_features(p2, getthe(p1, t1, t1, qv1), qt, f0, f1, f2);
-    const float t2g = GUESS_T_MID + GUESS_T_SCALE * guess_eval(ss.guess_w, f0, f1, f2);
-    if (t2g > 150.0f && t2g < 350.0f) thlast = t2g / pi2;  // else keep th1
+  constexpr bool EXTRAP = SOLVER == SOLVE_ACCEL || SOLVER == SOLVE_LEARNED;
+  float dth_net;
+  if (SOLVER == SOLVE_LEARNED && ss.saturated && !ss.sat_start && ss.have_lcl) {
+    thlast = th1 - GUESS_SLOPE_SCALE * ss.lcl_y * lp;
+  } else if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
+             network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net)) {
+    thlast = th1 + dth_net;
+  } else if (EXTRAP && ss.have_prev) {
+    thlast = th1 + ss.dth_prev * (dp / ss.dp_prev);
   }
   int i = 0;
   while (true) {
@@ -151,7 +225,15 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     const float lhv = LV1 - LV2 * tbar;
     const float rm = RD + RV * qvbar;
     float expo;
-    if (ICE) {
+    if (ACCEL_MATH) {
+      // the same exponent over one common denominator (one divide)
+      const float qibar = ICE ? 0.5f * (qi1 + qi2) : 0.0f;
+      const float cpm = ICE ? CP + CPV * qvbar + CPL * qlbar + CPI * qibar
+                            : CP + CPV * qvbar + CPL * qlbar;
+      float num = lhv * (ql2 - ql1) + rm * lp * tbar;
+      if (ICE) num += (LS1 - LS2 * tbar) * (qi2 - qi1);
+      expo = num / (cpm * tbar) - RDDCP * lp;
+    } else if (ICE) {
       const float qibar = 0.5f * (qi1 + qi2);
       const float lhs = LS1 - LS2 * tbar;
       const float cpm = CP + CPV * qvbar + CPL * qlbar + CPI * qibar;
@@ -164,36 +246,73 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     th2 = th1 * expf(expo);
     ++niter;
     if (i > 100) return false;
+    // difference quotient of F over the last two evaluations, kept in
+    // [-50, 0.5] so that a noisy quotient cannot throw x far
+    const bool have_q = SOLVER != SOLVE_PLAIN && i >= 2 && thlast != x_prev;
+    float s = 0.0f;
+    if (have_q) s = fmin_f(fmax_f(fast_div(th2 - f_prev, thlast - x_prev), -50.0f), 0.5f);
+    if (EXTRAP && have_q && fabsf(thlast - x_prev) >= SLOPE_MIN_DX) {
+      ss.slope = s;
+      ss.have_slope = true;
+    }
     if (fabsf(th2 - thlast) > CONVERGE) {
-      if (SOLVER != SOLVE_PLAIN && i >= 2 && thlast != x_prev) {
-        // secant step on g(x) = F(x) - x; the slope of F is kept in
-        // [-50, 0.5] so that a noisy difference quotient cannot throw x far
-        float s = (th2 - f_prev) / (thlast - x_prev);
-        s = fmin_f(fmax_f(s, -50.0f), 0.5f);
-        x_prev = thlast;
-        f_prev = th2;
-        thlast = thlast + (th2 - thlast) / (1.0f - s);
+      const float step = th2 - thlast;
+      x_prev = thlast;
+      f_prev = th2;
+      if (have_q) {
+        thlast = thlast + fast_div(step, 1.0f - s);  // secant step on F(x) - x
+      } else if (EXTRAP && ss.have_slope) {
+        thlast = thlast + fast_div(step, 1.0f - ss.slope);  // the last sub-step's slope
       } else {
-        x_prev = thlast;
-        f_prev = th2;
-        thlast = thlast + 0.3f * (th2 - thlast);
+        thlast = thlast + 0.3f * step;
       }
     } else {
       break;
     }
   }
-  if (SOLVER == SOLVE_ACCEL) {
+  if (EXTRAP) {
     ss.dth_prev = th2 - th1;
     ss.dp_prev = dp;
     ss.have_prev = true;
   }
-  if (SOLVER == SOLVE_LEARNED) ss.saturated = ql2 + qi2 > 0.0f;
+  if (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) {
+    ss.sat_start = ss.saturated;
+    ss.saturated = ql2 + qi2 > 0.0f;
+  }
   if (PSEUDO) {  // :487-491
     qt = qv2;
     ql2 = 0.0f;
     qi2 = 0.0f;
   }
   return true;
+}
+
+// Training pair i of the guess network: a saturated pseudo-adiabatic parcel
+// state (p1 in 100..1050 hPa, T1 in a 60 K band whose warm edge cools from
+// 30 degC at 1050 hPa to -40 degC at 100 hPa, never below -80 degC, at most
+// 40 g/kg of water), a pressure step dp log-uniform in 50..2000 Pa, and the
+// plain solver's (the reference's iteration's) solution of that sub-step.
+// Writes the features and the target y of guess_mlp.cuh; returns the
+// iteration count, negative when the plain iteration gave up.
+XC_HD int guess_pair(uint64_t seed, long long i, float *f, float *y) {
+  const float dp = 50.0f * expf(3.6888795f * guess_uniform01(seed, i, 1));  // 50 * 40^u
+  const float p1 = 10000.0f + dp + (95000.0f - dp) * guess_uniform01(seed, i, 0);
+  const float t_hi = 303.15f - 70.0f * (1.0f - p1 / 105000.0f);
+  const float t_lo = fmaxf(193.15f, t_hi - 60.0f);
+  float t1 = t_lo + (t_hi - t_lo) * guess_uniform01(seed, i, 2);
+  float qv1 = getqvs(p1, t1);
+  for (int k = 0; k < 64 && !(qv1 > 0.0f && qv1 <= 0.04f); ++k) {
+    t1 -= 2.0f;
+    qv1 = getqvs(p1, t1);
+  }
+  const float th1 = t1 / powf(p1 * RP00, RDDCP);
+  float p2 = p1, t2 = t1, th2 = th1, qv2 = qv1, ql2 = 0.0f, qi2 = 0.0f, qt = qv1;
+  int niter = 0;
+  SolverState ss;
+  const bool ok = substep<false, true, SOLVE_PLAIN>(dp, p2, t2, th2, qv2, ql2, qi2, qt, niter, ss);
+  guess_features(p2, getthe(p1, t1, t1, qv1), qv1, f[0], f[1], f[2]);
+  *y = (th2 - th1) / (GUESS_SLOPE_SCALE * logf(p1 / p2));
+  return ok ? niter : -niter;
 }
 
 // Running sum with Kahan compensation (SOLVE_ACCEL) or plain FP32 addition in
@@ -312,6 +431,21 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
   long long nsub_total = 0;
   SolverState ss;
   ss.guess_w = guess_w;
+  if (SOLVER == SOLVE_LEARNED) {
+    // the parcel that init_parcel will start at level kmax
+    const Env es = col.env(kmax);
+    float t0, td0, q0;
+    if (source == 3) {
+      q0 = (float)avgqv;
+      t0 = (float)avgth * es.pi;
+      td0 = dewpoint_of(es.p, q0);
+    } else {
+      q0 = es.q;
+      t0 = es.t;
+      td0 = es.td;
+    }
+    ss.have_lcl = parcel_lcl_slope(guess_w, es.p, t0, td0, q0, ss.lcl_y);
+  }
   Acc<SOLVER != SOLVE_PLAIN> cape_acc, cin_acc;
   auto init_parcel = [&](const Env &e) {
     if (source == 3) {
@@ -331,6 +465,7 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
     ql2 = 0.0f;
     qi2 = 0.0f;
     qt = qv2;
+    if (SOLVER != SOLVE_PLAIN) ss.lnp = logf(p2);
   };
   if (kmax == 1) init_parcel(prev);
 

@@ -7,9 +7,9 @@ namespace xc {
 
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
-  extern __shared__ float guess_sm[];  // the guess network, SOLVE_LEARNED only
+  extern __shared__ float guess_sm[];  // the guess network, SOLVE_LEARNED* only
   const float *gw = nullptr;
-  if (SOLVER == SOLVE_LEARNED) {
+  if (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) {
     for (int k = threadIdx.x; k < GUESS_NPARAM; k += blockDim.x) guess_sm[k] = a.guess_w[k];
     __syncthreads();
     gw = guess_sm;
@@ -165,7 +165,8 @@ template <typename T, int GRID, int SOLVER>
 static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaStream_t s) {
   const bool ice = a.adiabat >= 3;
   const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
-  const size_t sm = SOLVER == SOLVE_LEARNED ? sizeof(float) * GUESS_NPARAM : 0;
+  const size_t sm =
+      (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) ? sizeof(float) * GUESS_NPARAM : 0;
   if (ice && pseudo)
     cape_kernel<T, GRID, true, true, SOLVER><<<blocks, threads, sm, s>>>(a);
   else if (ice)
@@ -177,7 +178,8 @@ static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaS
 }
 
 // guess codes (include/xcape_gb300.h): 0 plain, 1 learned, 2 extrapolated,
-// 3 plain first guess with secant steps.
+// 3 plain first guess with secant steps, 4 the network on every saturated
+// sub-step.
 template <typename T, int GRID>
 static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
   const int threads = 128;
@@ -187,7 +189,8 @@ static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
     case 0: launch_cape_s<T, GRID, SOLVE_PLAIN>(a, blocks, threads, s); break;
     case 1: launch_cape_s<T, GRID, SOLVE_LEARNED>(a, blocks, threads, s); break;
     case 2: launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s); break;
-    default: launch_cape_s<T, GRID, SOLVE_SECANT>(a, blocks, threads, s); break;
+    case 3: launch_cape_s<T, GRID, SOLVE_SECANT>(a, blocks, threads, s); break;
+    default: launch_cape_s<T, GRID, SOLVE_LEARNED_ALL>(a, blocks, threads, s); break;
   }
   return cudaGetLastError();
 }

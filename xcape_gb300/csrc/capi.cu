@@ -152,10 +152,10 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   if (rc) return rc;
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
-  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_SECANT)
+  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_EVERY)
     return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
   const float *guess_w = nullptr;
-  if (guess == XC_GUESS_LEARNED) {
+  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY) {
     rc = guess_weights(&guess_w);
     if (rc) return rc;
   }

@@ -1,10 +1,9 @@
 // guess_mlp.cu -- data, training and batched inference of the learned first
 // guess (guess_mlp.cuh), all on the GPU.
 //
-// * guess_pairs_kernel draws saturated parcel states (p 100..1050 hPa,
-//   T -80..40 degC, pressure step 1..25 hPa), solves one sub-step with the
-//   plain solver (the reference's damped iteration, cape_column.cuh) and
-//   stores (features, normalised end temperature, iterations).
+// * guess_pairs_kernel draws saturated parcel states and solves one sub-step
+//   of each with the plain solver (guess_pair in cape_column.cuh), storing
+//   (features, normalised increment, iterations).
 // * guess_train_kernel runs forward and backward passes over a batch: the
 //   64x64 hidden layer on the tensor cores with mma.sync m16n8k16 (BF16
 //   operands, FP32 accumulation), the rest and the whole backward pass in
@@ -23,17 +22,6 @@
 namespace xc {
 
 namespace {
-
-__device__ __forceinline__ uint64_t mix64(uint64_t x) {
-  x += 0x9E3779B97F4A7C15ull;
-  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-  return x ^ (x >> 31);
-}
-__device__ __forceinline__ float uniform01(uint64_t seed, long long i, int k) {
-  const uint64_t h = mix64(seed ^ mix64((uint64_t)i * 8ull + (uint64_t)k));
-  return (float)(h >> 40) * (1.0f / 16777216.0f);
-}
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -129,30 +117,7 @@ __global__ void guess_pairs_kernel(long long n, unsigned long long seed, float *
                                    float *targets, int *iters) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float p2 = 10000.0f + 95000.0f * uniform01(seed, i, 0);
-  const float dp = 100.0f + 2400.0f * uniform01(seed, i, 1);
-  const float p1 = p2 + dp;
-  float T1 = 193.15f + 120.0f * uniform01(seed, i, 2);
-  float qv1 = getqvs(p1, T1);
-  // keep the water content physical (<= 40 g/kg): cool the parcel until it is
-  for (int k = 0; k < 64 && !(qv1 > 0.0f && qv1 <= 0.04f); ++k) {
-    T1 -= 2.0f;
-    qv1 = getqvs(p1, T1);
-  }
-  const float pi1 = powf(p1 * RP00, RDDCP);
-  float p2v = p1, t2 = T1, th2 = T1 / pi1, qv2 = qv1, ql2 = 0.0f, qi2 = 0.0f, qt = qv1;
-  int niter = 0;
-  SolverState ss;
-  const bool ok = substep<false, true, SOLVE_PLAIN>(dp, p2v, t2, th2, qv2, ql2, qi2, qt, niter, ss);
-  const float pi2 = powf(p2v * RP00, RDDCP);
-  const float the = getthe(p1, T1, T1, qv1);
-  float f0, f1, f2;
-  guess_features(p2v, the, qv1, f0, f1, f2);
-  feats[3 * i] = f0;
-  feats[3 * i + 1] = f1;
-  feats[3 * i + 2] = f2;
-  targets[i] = (th2 * pi2 - GUESS_T_MID) / GUESS_T_SCALE;
-  iters[i] = ok ? niter : -niter;
+  iters[i] = guess_pair(seed, i, feats + 3 * i, targets + i);
 }
 
 // One forward/backward pass of the MSE loss over samples [row0, row0 + TB)

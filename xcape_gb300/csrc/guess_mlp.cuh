@@ -1,14 +1,18 @@
 // guess_mlp.cuh -- the learned first guess of the moist-adiabat iteration.
 //
 // A 3 -> 64 -> 64 -> 1 multilayer perceptron (ReLU) maps a saturated parcel's
-// state at the start of a sub-step to the parcel temperature at the end of
-// it:
+// state at the start of a sub-step to its potential temperature at the end
+// of it:
 //   inputs   f0 = (p2 - 55000 Pa) / 45000 Pa     target pressure
-//            f1 = (theta_e - 330 K) / 60 K       parcel theta-e (getthe)
+//            f1 = (theta_e - 320 K) / 40 K       parcel theta-e (getthe)
 //            f2 = 50 qt - 0.5                    total water
-//   output   y, with T2 = 233.15 K + 50 K * y
-// The sub-step guess is then thlast = T2 / pi2.  It is trained on pairs that
-// the plain solver (the reference's damped iteration) produces, with the
+//   output   y, the increment per unit log-pressure:
+//            theta2 = theta1 + 50 K * y * ln(p1 / p2)
+// so the saturated parcel temperature is T2 = theta2 * pi2.  Predicting the
+// increment rather than T2 itself makes the guess error a fraction of one
+// sub-step's change instead of a fraction of the whole temperature range
+// (BF16 weights carry 8 significant bits).  It is trained on pairs that the
+// plain solver (the reference's damped iteration) produces, with the
 // project's own GPU kernels (guess_mlp.cu).
 //
 // Parameters live in one flat float array of GUESS_NPARAM values:
@@ -30,8 +34,10 @@ constexpr int GUESS_OFF_B3 = GUESS_OFF_W3 + GUESS_H;              // 4480
 constexpr int GUESS_NPARAM = GUESS_OFF_B3 + 1;                    // 4481
 
 constexpr float GUESS_P_MID = 55000.0f, GUESS_P_SCALE = 45000.0f;
-constexpr float GUESS_THE_MID = 330.0f, GUESS_THE_SCALE = 60.0f;
-constexpr float GUESS_T_MID = 233.15f, GUESS_T_SCALE = 50.0f;
+constexpr float GUESS_THE_MID = 320.0f, GUESS_THE_SCALE = 40.0f;
+constexpr float GUESS_SLOPE_SCALE = 50.0f;
+// outputs outside this range are not used (the caller keeps its own guess)
+constexpr float GUESS_Y_MIN = -0.2f, GUESS_Y_MAX = 2.0f;
 
 XC_HD void guess_features(float p2, float the, float qt, float &f0, float &f1, float &f2) {
   f0 = (p2 - GUESS_P_MID) / GUESS_P_SCALE;
@@ -41,23 +47,44 @@ XC_HD void guess_features(float p2, float the, float qt, float &f0, float &f1, f
 
 // One evaluation, FP32 arithmetic, weights from any memory space (shared
 // memory in the CAPE kernel).  Returns the normalised output y.
+// The hidden layer is accumulated GUESS_CHUNK output units at a time, each
+// pass recomputing the first layer's activations (64 x 3 FMAs against the
+// 64 x 64 of the second layer), so that only GUESS_CHUNK accumulators are
+// live: the network then fits in the register budget of the CAPE kernel it
+// is inlined into.  Every sum is taken in the order of a plain loop
+// (z_n = b2_n + sum over k ascending, y = b3 + sum over n ascending).
+constexpr int GUESS_CHUNK = 16;
 XC_HD float guess_eval(const float *w, float f0, float f1, float f2) {
-  float h1[GUESS_H];  // fully unrolled loops keep it in registers
-#pragma unroll
-  for (int k = 0; k < GUESS_H; ++k) {
-    const float z = w[GUESS_OFF_B1 + k] + w[GUESS_OFF_W1 + 3 * k] * f0 +
-                    w[GUESS_OFF_W1 + 3 * k + 1] * f1 + w[GUESS_OFF_W1 + 3 * k + 2] * f2;
-    h1[k] = z > 0.0f ? z : 0.0f;
-  }
   float y = w[GUESS_OFF_B3];
-  for (int n = 0; n < GUESS_H; ++n) {
-    const float *row = w + GUESS_OFF_W2 + GUESS_H * n;
-    float z = w[GUESS_OFF_B2 + n];
+  for (int n0 = 0; n0 < GUESS_H; n0 += GUESS_CHUNK) {
+    float z[GUESS_CHUNK];
 #pragma unroll
-    for (int k = 0; k < GUESS_H; ++k) z += row[k] * h1[k];
-    y += w[GUESS_OFF_W3 + n] * (z > 0.0f ? z : 0.0f);
+    for (int j = 0; j < GUESS_CHUNK; ++j) z[j] = w[GUESS_OFF_B2 + n0 + j];
+    for (int k = 0; k < GUESS_H; ++k) {
+      float h = w[GUESS_OFF_B1 + k] + w[GUESS_OFF_W1 + 3 * k] * f0 +
+                w[GUESS_OFF_W1 + 3 * k + 1] * f1 + w[GUESS_OFF_W1 + 3 * k + 2] * f2;
+      h = h > 0.0f ? h : 0.0f;
+#pragma unroll
+      for (int j = 0; j < GUESS_CHUNK; ++j) z[j] += w[GUESS_OFF_W2 + GUESS_H * (n0 + j) + k] * h;
+    }
+#pragma unroll
+    for (int j = 0; j < GUESS_CHUNK; ++j)
+      y += w[GUESS_OFF_W3 + n0 + j] * (z[j] > 0.0f ? z[j] : 0.0f);
   }
   return y;
+}
+
+// Deterministic uniform numbers for the training pairs (splitmix64 hash of
+// (seed, sample, draw)), the same on the host and the device.
+XC_HD uint64_t guess_mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+XC_HD float guess_uniform01(uint64_t seed, long long i, int k) {
+  const uint64_t h = guess_mix64(seed ^ guess_mix64((uint64_t)i * 8ull + (uint64_t)k));
+  return (float)(h >> 40) * (1.0f / 16777216.0f);
 }
 
 }  // namespace xc

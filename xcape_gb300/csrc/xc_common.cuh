@@ -39,6 +39,7 @@ constexpr float REPS = RV / RD;
 constexpr float RDDCP = RD / CP;
 constexpr float CPDG = CP / G;
 constexpr float CONVERGE = 0.0002f;
+constexpr float LN_P00 = 11.5129254649702f;  // ln(P00), for the accelerated solvers
 constexpr float QEPS = 287.04f / 461.5f;  // eps inside getqvs/getqvi
 
 // Column status bits (mirrors include/xcape_gb300.h).
@@ -71,6 +72,17 @@ XC_HD float getthe(float p, float t, float td, float q) {
   }
   return t * powf(100000.0f / p, 0.2854f * (1.0f - 0.28f * q)) *
          expf(((3376.0f / tlcl) - 2.54f) * q * (1.0f + 0.81f * q));
+}
+
+// Approximate divide (a few ulp) for the secant steps of the accelerated
+// solvers, whose quotients only steer the iteration; the map F itself and
+// the stopping test use IEEE operations in every mode.  Exact on the host.
+XC_HD float fast_div(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
 }
 
 // Fortran MIN/MAX as gfortran lowers them for the reference build: the

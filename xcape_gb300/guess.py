@@ -1,11 +1,13 @@
 """The learned first guess of the moist-adiabat iteration.
 
 A 3 -> 64 -> 64 -> 1 ReLU network (``xcape_gb300/csrc/guess_mlp.cuh``) maps a
-saturated parcel's (target pressure, theta-e, total water) to its
-temperature at the end of a sub-step.  ``calc_cape(..., guess='learned')``
-starts each saturated sub-step's iteration there instead of at the previous
-sub-step's theta, and then takes secant steps; the stopping test and the
-result are the reference's.
+saturated parcel's (target pressure, theta-e, total water) to the increment
+of its potential temperature over a sub-step, per unit log-pressure:
+theta2 = theta1 + 50 K * y * ln(p1 / p2).  ``calc_cape(..., guess='learned')``
+starts the first saturated sub-step's iteration there (the later ones
+extrapolate the previous sub-step's increment); ``guess='learned-every'``
+starts every saturated sub-step there.  Both take secant steps; the stopping
+test and the result are the reference's.
 
 Everything runs on the GPU through the library:
   * ``xc_guess_pairs``  -- training pairs, solved by the plain (reference)
@@ -16,7 +18,7 @@ Everything runs on the GPU through the library:
   * ``xc_guess_eval``   -- batched inference.
 The trained weights are stored rounded to BF16 in
 ``xcape_gb300/data/guess_mlp.npz`` with their training metadata, and
-``load()`` hands them to the library (``xc_guess_set_weights``).
+``ensure_loaded()`` hands them to the library (``xc_guess_set_weights``).
 
     python -m xcape_gb300.guess train [--pairs N] [--epochs E] [--out PATH]
 """
@@ -32,7 +34,8 @@ from . import _lib
 NPARAM = _lib.XC_GUESS_NPARAM
 H = 64
 OFF_W1, OFF_B1, OFF_W2, OFF_B2, OFF_W3, OFF_B3 = 0, 192, 256, 4352, 4416, 4480
-T_MID, T_SCALE = 233.15, 50.0
+SLOPE_SCALE = 50.0  # K per unit ln p of the output
+FORMAT_VERSION = 2  # the increment target; version 1 predicted the temperature
 DEFAULT_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_mlp.npz")
 
 _loaded = set()
@@ -65,7 +68,9 @@ def _torch():
 
 
 def make_pairs(n, seed=1):
-    """n training pairs as CUDA tensors (feats [n,3], targets [n], iters [n])."""
+    """n training pairs as CUDA tensors (feats [n,3], targets [n], iters [n]).
+
+    iters is the plain iteration's count, negative where it gave up."""
     torch = _torch()
     f = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     t = torch.empty(n, dtype=torch.float32, device="cuda")
@@ -90,7 +95,7 @@ def gradient(weights, feats, targets):
 
 
 def evaluate(weights, feats):
-    """Network outputs for feats [n, 3] (normalised temperatures)."""
+    """Network outputs for feats [n, 3] (normalised increments y)."""
     torch = _torch()
     w = torch.as_tensor(np.asarray(weights, np.float32)).cuda()
     f = torch.as_tensor(feats).cuda().contiguous() if not hasattr(feats, "data_ptr") else feats
@@ -130,20 +135,24 @@ def train(n_pairs=1 << 21, epochs=12, batch=8192, lr=2e-3, seed=7, log=print):
                       te[b * batch:].data_ptr(), batch, grad.data_ptr(), loss.data_ptr(), stream)
             _lib.call("xc_guess_adam", w.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(),
                       float(lr_ep), step, stream)
-        rmse_k = float(np.sqrt(loss.item() / n_batches)) * T_SCALE
-        curve.append(rmse_k)
+        rms = float(np.sqrt(loss.item() / n_batches))
+        curve.append(rms)
         if log:
-            log(f"epoch {ep + 1}/{epochs}: train RMS error {rmse_k:.4f} K")
+            log(f"epoch {ep + 1}/{epochs}: train RMS error of y {rms:.5f}")
     w_bf = bf16_round(w.cpu().numpy())
     pred = evaluate(w_bf, fv)
-    val_rmse = float(torch.sqrt(torch.mean((pred - tv) ** 2)).item()) * T_SCALE
+    val_rms = float(torch.sqrt(torch.mean((pred - tv) ** 2)).item())
+    val_rel = float((torch.sqrt(torch.mean((pred - tv) ** 2)) /
+                     torch.sqrt(torch.mean(tv ** 2))).item())
     it = iters.cpu().numpy()
-    meta = {"version": 1, "pairs": n_pairs, "epochs": epochs, "batch": batch, "lr": lr,
-            "seed": seed, "train_rms_K": curve, "val_rms_K_bf16": val_rmse,
+    meta = {"version": FORMAT_VERSION, "target": "y = (theta2 - theta1) / (50 K ln(p1/p2))",
+            "pairs": n_pairs, "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
+            "train_rms_y": curve, "val_rms_y_bf16": val_rms, "val_rel_rms_bf16": val_rel,
             "plain_iterations_mean": float(np.abs(it).mean()),
             "plain_gave_up": int((it < 0).sum()), "seconds": time.time() - t0}
     if log:
-        log(f"validation RMS error with BF16 weights: {val_rmse:.4f} K")
+        log(f"validation RMS error of y with BF16 weights: {val_rms:.5f} "
+            f"({100 * val_rel:.2f}% of the RMS target)")
     return w_bf, meta
 
 
@@ -155,7 +164,11 @@ def save(path, weights, meta):
 
 def read(path=DEFAULT_PATH):
     with np.load(path) as z:
-        return z["weights"], json.loads(bytes(z["meta"]).decode())
+        w, meta = z["weights"], json.loads(bytes(z["meta"]).decode())
+    if meta.get("version") != FORMAT_VERSION:
+        raise ValueError(f"{path} holds a guess network of format {meta.get('version')}, "
+                         f"expected {FORMAT_VERSION}; retrain it")
+    return w, meta
 
 
 def set_weights(weights):
