@@ -7,7 +7,12 @@ source='mixed-layer' (ml_depth 500 m), pseudo-liquid adiabat, pinc 500 Pa.
 value = columns per second (both sources computed for every column).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--guess plain|learned] [--workload cape|srh]
+                    [--guess learned|plain|extrapolated|secant|learned-every]
+                    [--workload cape|srh]
+
+The headline is the learned-guess solver (guess='learned'); the same run times
+the plain solver (the reference's iteration) on the same launches for the
+"learned-guess vs plain" ratio, and surface-based parcels for both.
 
 --impl reference times the reference algorithm on the host cores (the CPU
 restatement of the Fortran in oracle/, all host threads, a bounded sample of
@@ -36,6 +41,7 @@ ADIABAT = 1
 METRIC = "CAPE/CIN columns/s at 1M×37 lev: learned-guess vs plain CUDA, |ΔCAPE|≤1 J/kg"
 SRH_METRIC = "SRH columns/s at 1M×50 lev (calc_srh, depth 1000+3000 m)"
 CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
+ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg
 REF_SAMPLE = 32768       # columns per --impl reference step
 
 
@@ -45,7 +51,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--guess", default="plain",
+    ap.add_argument("--guess", default="learned",
                     choices=["plain", "extrapolated", "learned", "secant", "learned-every"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -186,6 +192,31 @@ def cpu_cape(sample, nthreads):
     return sample / (time.perf_counter() - t0)
 
 
+def accuracy_vs_fp64(outs, nthreads):
+    """|dCAPE|, |dCIN| of the timed launches' outputs on the first ACC_SAMPLE
+    columns against the FP64 oracle (the checker), over the columns whose
+    FP64 iteration converges and, for most-unstable parcels, whose source
+    level is the same (theta-e near-ties pick another parcel)."""
+    import oracle as O
+    plev, t, td, ps, ts, tds = cape_inputs(0, ACC_SAMPLE)
+    start = O.pres_lev_pos(plev, ps)
+    res = {"columns": ACC_SAMPLE}
+    for src, code in SOURCES:
+        ref = O.loopcape(plev, t, td, ps, ts, tds, PINC, code, ML_DEPTH, ADIABAT, start=start,
+                         p_is_1d=True, nthreads=nthreads, precision="f64", stats=True)
+        cape, cin, _, mulvl = (x[:ACC_SAMPLE].cpu().numpy() for x in outs[src])
+        ok = (ref["status"] & 1) == 0
+        if code == 2:
+            ok &= mulvl == ref["mulvl"]
+        dc = np.abs(cape[ok].astype(np.float64) - ref["cape"][ok])
+        dn = np.abs(cin[ok].astype(np.float64) - ref["cin"][ok])
+        res[src] = {"compared": int(ok.sum()), "max_abs_dcape": float(dc.max()),
+                    "frac_dcape_le_1": float(np.mean(dc <= 1.0)),
+                    "frac_dcin_le_1_or_0.1pct": float(np.mean(
+                        dn <= np.maximum(1.0, 1e-3 * np.abs(ref["cin"][ok]))))}
+    return res
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm on the host cores."""
     world, rank, _ = dist_env()
@@ -257,11 +288,12 @@ def run_ours(args):
     order = not args.no_order
     launches_per_call = 4 if order else 1  # 3 ordering kernels + the lift
 
-    def launch(src_code, o, counters=None):
+    def launch(src_code, o, counters=None, g=None):
         cape, cin, zout, mulvl = o
         _lib.check(L.xc_loopcape_ex(2, P.data_ptr(), T.data_ptr(), TD.data_ptr(), PS.data_ptr(),
                                     TS.data_ptr(), TDS.data_ptr(), _lib.XC_F32, PINC, src_code,
-                                    ML_DEPTH, ADIABAT, None, NLEV, n2, guess, cape.data_ptr(),
+                                    ML_DEPTH, ADIABAT, None, NLEV, n2,
+                                    guess if g is None else g, cape.data_ptr(),
                                     cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), None,
                                     counters, ws if order else None, ws_bytes if order else 0,
                                     sptr))
@@ -303,15 +335,29 @@ def run_ours(args):
     ms_max = max_over_ranks(dist, ms, dev)
 
     # per-kernel (per-source) average durations, for the roofline
-    per_src_ms = {}
-    for src, code in SOURCES:
+    def time_source(code, o, g=None):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            launch(code, outs[src])
+            launch(code, o, g=g)
         e1.record(stream)
         torch.cuda.synchronize()
-        per_src_ms[src] = e0.elapsed_time(e1) / args.steps
+        return e0.elapsed_time(e1) / args.steps
+
+    per_src_ms = {src: time_source(code, outs[src]) for src, code in SOURCES}
+
+    # the same launches with the plain solver (the reference's iteration), and
+    # surface-based parcels with both, into scratch outputs
+    scratch = [torch.empty_like(x) for x in outs[SOURCES[0][0]]]
+    plain_ms = {}
+    compare = guess != _lib.XC_GUESS_PLAIN
+    if compare:
+        for _ in range(2):
+            launch(SOURCES[0][1], scratch, g=_lib.XC_GUESS_PLAIN)
+        plain_ms = {src: time_source(code, scratch, _lib.XC_GUESS_PLAIN) for src, code in SOURCES}
+    sb_ms = {args.guess: time_source(1, scratch)}
+    if compare:
+        sb_ms["plain"] = time_source(1, scratch, _lib.XC_GUESS_PLAIN)
 
     # end to end through the public API from pinned host memory
     import xcape_gb300 as X
@@ -376,6 +422,12 @@ def run_ours(args):
         "fp32": {"achieved_tflops": fp32_ach, "peak_tflops_nominal": fp32_peak,
                  "frac": fp32_ach / fp32_peak, "iterations": niter, "substeps": nsub},
         "per_source_ms": per_src_ms,
+        "vs_plain": ({"plain_value": cols_all / (sum(plain_ms.values()) / 1e3),
+                      "plain_per_source_ms": plain_ms,
+                      "speedup": sum(plain_ms.values()) / sum(per_src_ms.values()),
+                      "surface_based_ms": sb_ms,
+                      "surface_based_speedup": sb_ms["plain"] / sb_ms[args.guess]}
+                     if compare else {"surface_based_ms": sb_ms}),
         "work": {k: {"substeps": v[0], "iterations": v[1]} for k, v in work.items()},
         "e2e": {"value": cols_all / e2e_dt, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "xcape_gb300.calc_cape(numpy, pinned)"},
@@ -389,6 +441,7 @@ def run_ours(args):
         line["cpu_baseline"] = {"value": v, "unit": "columns/s", "cores": nth, "kind": "port",
                                 "sample": f"first {CPU_SAMPLE} columns, both sources, FP32 "
                                           "oracle (C restatement of the Fortran), OpenMP"}
+        line["accuracy_vs_fp64"] = accuracy_vs_fp64(outs, nth)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -50,7 +50,12 @@ extern "C" int emu_cape(int grid, const void *p, const void *t, const void *td, 
   a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.ps = ps; a.ts = ts; a.tds = tds;
   a.start = grid == 1 ? nullptr : start; a.pinc = pinc; a.source = source; a.ml_depth = ml_depth;
   a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = guess; a.perm = nullptr; a.cape = cape; a.cin = cin;
-  a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr; a.guess_w = guess_w;
+  a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr;
+  // the column code reads the packed copy the kernels keep in shared memory
+  alignas(16) static float packed[GUESS_NPARAM + 3];
+  if (guess_w)
+    for (int k = 0; k < GUESS_NPARAM; ++k) packed[k] = guess_packed_value(guess_w, k);
+  a.guess_w = guess_w ? packed : nullptr;
   if (dtype == 0) {
     if (grid == 1) cape_loop<float, 1>(a, counters);
     else if (grid == 2) cape_loop<float, 2>(a, counters);
@@ -102,6 +107,12 @@ extern "C" void emu_pres_lev_pos(const void *p1d, const void *ps, int dtype, int
 
 extern "C" float emu_guess_eval(const float *w, float f0, float f1, float f2) {
   return guess_eval(w, f0, f1, f2);
+}
+
+extern "C" float emu_guess_eval_packed(const float *w, float f0, float f1, float f2) {
+  alignas(16) float packed[GUESS_NPARAM + 3];
+  for (int k = 0; k < GUESS_NPARAM; ++k) packed[k] = guess_packed_value(w, k);
+  return guess_eval_packed(packed, f0, f1, f2);
 }
 
 extern "C" void emu_guess_pairs(long long n, unsigned long long seed, float *feats,

@@ -36,6 +36,9 @@ def test_host_guess_eval_matches_numpy():
     want = forward(w, x, bf16_hidden=False)[0]
     got = np.array([L.emu_guess_eval(w.ctypes.data, *map(float, r)) for r in x])
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-5)
+    # the packed copy the CAPE kernel reads gives the same sums in the same order
+    packed = np.array([L.emu_guess_eval_packed(w.ctypes.data, *map(float, r)) for r in x])
+    np.testing.assert_array_equal(packed, got)
 
 
 def emulated_pairs(n, seed):

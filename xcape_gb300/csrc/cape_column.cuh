@@ -125,7 +125,7 @@ struct SolverState {
   bool have_lcl = false;    // lcl_y holds the network's output at the parcel's LCL
   float lcl_y = 0.0f;
   float lnp = 0.0f;         // ln of the parcel pressure (accelerated modes)
-  const float *guess_w = nullptr;  // guess network parameters (SOLVE_LEARNED*)
+  const float *guess_w = nullptr;  // packed guess network (guess_packed_value), SOLVE_LEARNED*
 };
 
 // The guess network's output y at the lifting condensation level of a parcel
@@ -138,7 +138,7 @@ XC_HD bool parcel_lcl_slope(const float *w, float p, float t, float td, float q,
   const float plcl = td < t ? p * powf(tlcl / t, 1.0f / RDDCP) : p;
   float f0, f1, f2;
   guess_features(plcl, getthe(p, t, td, q), q, f0, f1, f2);
-  y = guess_eval(w, f0, f1, f2);
+  y = guess_eval_packed(w, f0, f1, f2);
   return y >= GUESS_Y_MIN && y <= GUESS_Y_MAX;
 }
 
@@ -155,7 +155,7 @@ XC_HD bool network_increment(const float *w, float p1, float p2, float t1, float
                              float lp, float &dth) {
   float f0, f1, f2;
   guess_features(p2, getthe(p1, t1, t1, qv1), qt, f0, f1, f2);
-  const float y = guess_eval(w, f0, f1, f2);
+  const float y = guess_eval_packed(w, f0, f1, f2);
   if (!(y >= GUESS_Y_MIN && y <= GUESS_Y_MAX)) return false;
   dth = -GUESS_SLOPE_SCALE * y * lp;
   return true;
@@ -226,13 +226,14 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     const float rm = RD + RV * qvbar;
     float expo;
     if (ACCEL_MATH) {
-      // the same exponent over one common denominator (one divide)
+      // the same exponent over one common denominator (one approximate
+      // divide, a few ulp)
       const float qibar = ICE ? 0.5f * (qi1 + qi2) : 0.0f;
       const float cpm = ICE ? CP + CPV * qvbar + CPL * qlbar + CPI * qibar
                             : CP + CPV * qvbar + CPL * qlbar;
       float num = lhv * (ql2 - ql1) + rm * lp * tbar;
       if (ICE) num += (LS1 - LS2 * tbar) * (qi2 - qi1);
-      expo = num / (cpm * tbar) - RDDCP * lp;
+      expo = fast_div(num, cpm * tbar) - RDDCP * lp;
     } else if (ICE) {
       const float qibar = 0.5f * (qi1 + qi2);
       const float lhs = LS1 - LS2 * tbar;

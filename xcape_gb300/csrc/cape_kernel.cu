@@ -7,10 +7,11 @@ namespace xc {
 
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
-  extern __shared__ float guess_sm[];  // the guess network, SOLVE_LEARNED* only
+  extern __shared__ __align__(16) float guess_sm[];  // packed guess network, SOLVE_LEARNED*
   const float *gw = nullptr;
   if (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) {
-    for (int k = threadIdx.x; k < GUESS_NPARAM; k += blockDim.x) guess_sm[k] = a.guess_w[k];
+    for (int k = threadIdx.x; k < GUESS_NPARAM; k += blockDim.x)
+      guess_sm[k] = guess_packed_value(a.guess_w, k);
     __syncthreads();
     gw = guess_sm;
   }

@@ -74,6 +74,50 @@ XC_HD float guess_eval(const float *w, float f0, float f1, float f2) {
   return y;
 }
 
+// Packed copy of the parameters for the CAPE kernel's shared memory: the
+// first 256 values become one float4 per first-layer unit,
+// {W1[k][0], W1[k][1], W1[k][2], b1[k]}; the rest (W2, b2, w3, b3) keeps the
+// flat offsets, W2's rows being 16-byte aligned.  Element i of the packed
+// array:
+XC_HD float guess_packed_value(const float *w, int i) {
+  if (i >= 4 * GUESS_H) return w[i];
+  const int k = i >> 2, c = i & 3;
+  return c < 3 ? w[GUESS_OFF_W1 + 3 * k + c] : w[GUESS_OFF_B1 + k];
+}
+
+// guess_eval on the packed parameters (16-byte aligned): the same sums in
+// the same order, read four weights per load.
+XC_HD float guess_eval_packed(const float *pk, float f0, float f1, float f2) {
+  float y = pk[GUESS_OFF_B3];
+  for (int n0 = 0; n0 < GUESS_H; n0 += GUESS_CHUNK) {
+    float z[GUESS_CHUNK];
+#pragma unroll
+    for (int j = 0; j < GUESS_CHUNK; ++j) z[j] = pk[GUESS_OFF_B2 + n0 + j];
+    for (int k = 0; k < GUESS_H; k += 4) {
+      float h[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 l = *reinterpret_cast<const float4 *>(pk + 4 * (k + u));
+        const float v = l.w + l.x * f0 + l.y * f1 + l.z * f2;
+        h[u] = v > 0.0f ? v : 0.0f;
+      }
+#pragma unroll
+      for (int j = 0; j < GUESS_CHUNK; ++j) {
+        const float4 r =
+            *reinterpret_cast<const float4 *>(pk + GUESS_OFF_W2 + GUESS_H * (n0 + j) + k);
+        z[j] += r.x * h[0];
+        z[j] += r.y * h[1];
+        z[j] += r.z * h[2];
+        z[j] += r.w * h[3];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < GUESS_CHUNK; ++j)
+      y += pk[GUESS_OFF_W3 + n0 + j] * (z[j] > 0.0f ? z[j] : 0.0f);
+  }
+  return y;
+}
+
 // Deterministic uniform numbers for the training pairs (splitmix64 hash of
 // (seed, sample, draw)), the same on the host and the device.
 XC_HD uint64_t guess_mix64(uint64_t x) {

@@ -74,9 +74,13 @@ XC_HD float getthe(float p, float t, float td, float q) {
          expf(((3376.0f / tlcl) - 2.54f) * q * (1.0f + 0.81f * q));
 }
 
-// Approximate divide (a few ulp) for the secant steps of the accelerated
-// solvers, whose quotients only steer the iteration; the map F itself and
-// the stopping test use IEEE operations in every mode.  Exact on the host.
+// Approximate divide (a few ulp) for the accelerated solvers: their secant
+// quotients and the exponent of their map, whose contract is agreement with
+// the FP64 run within tolerance rather than bit-faithfulness to the FP32
+// Fortran.  Exact on the host.  getqvs/getqvi keep IEEE operations in every
+// mode: builds with approximate exp (__expf) or approximate divides inside
+// them ran 12-18x slower on sm_103a, the warps no longer reconverging after
+// the sub-step (1.2 active threads per executed instruction, measured).
 XC_HD float fast_div(float a, float b) {
 #if defined(__CUDA_ARCH__)
   return __fdividef(a, b);
