@@ -53,7 +53,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--guess", default="learned",
                     choices=["plain", "extrapolated", "learned", "secant", "learned-every"])
-    ap.add_argument("--workload", default="cape", choices=["cape", "srh"])
+    ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve"])
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="length of the request trace of --workload serve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-order", action="store_true",
                     help="launch the lift in natural column order (no ordering workspace)")
@@ -498,12 +500,145 @@ def run_srh(args):
     return 0
 
 
+SERVE_METRIC = "calc_cape serving loop: p50/p99 latency and columns/s, learned vs plain"
+SERVE_RATE = 200.0        # requests per second (Poisson)
+SERVE_POOL = 1 << 20      # columns of each device-resident input pool
+SERVE_BASE = 1 << 17      # distinct synthetic columns tiled into a pool
+
+
+def serve_trace(seconds, seed=4):
+    """The request trace: Poisson arrivals, log-uniform column counts
+    (1e3..1e6), uniform level counts (20..137), mixed grids, sources and
+    adiabats, and where each request's columns sit in the input pools."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / SERVE_RATE)
+        if t >= seconds:
+            return out
+        n2 = int(10 ** rng.uniform(3, 6))
+        out.append({"arrival": t, "n2": n2, "nk": int(rng.integers(20, 138)),
+                    "grid": ("sigma", "pressure")[int(rng.integers(2))],
+                    "source": ("surface", "most-unstable", "mixed-layer")[int(rng.integers(3))],
+                    "adiabat": ("pseudo-liquid", "reversible-liquid", "pseudo-ice",
+                                "reversible-ice")[int(rng.integers(4))],
+                    "c0": int(rng.integers(0, SERVE_POOL - n2 + 1))})
+
+
+def run_serve(args):
+    """--workload serve: calc_cape requests arriving at 200/s, batched on the
+    device (xcape_gb300.batch: one graph launch per batch), for the learned
+    and the plain solver on the same trace."""
+    import torch
+    from xcape_gb300 import synthetic as S
+    from xcape_gb300.batch import CapeBatch
+    world, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nl = 137
+    reps = SERVE_POOL // SERVE_BASE
+
+    def pool(arrs):
+        # tile SERVE_BASE synthetic columns to SERVE_POOL on the device
+        return [torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev).repeat(
+            (reps, 1) if a.ndim == 2 else (reps,)) for a in arrs]
+    sig = S.sigma_c0(shape=(SERVE_BASE,), nlev=nl, seed=31, dtype=np.float32)
+    sig_d = pool([np.reshape(a, (SERVE_BASE, nl)) if np.size(a) == SERVE_BASE * nl
+                  else np.ravel(a) for a in sig])
+    prs = S.pressure_c1(shape=(SERVE_BASE,), nlev=nl, seed=32)
+    plev = torch.from_numpy(np.ascontiguousarray(prs[0], np.float32)).to(dev)
+    prs_d = [plev] + pool([np.reshape(a, (SERVE_BASE, nl)) if np.size(a) == SERVE_BASE * nl
+                           else np.ravel(a) for a in prs[1:]])
+    trace = serve_trace(args.serve_seconds)
+    max_cols = 8 << 20
+
+    def descriptor(b, r):
+        c0, n2, nk = r["c0"], r["n2"], r["nk"]
+        if r["grid"] == "sigma":
+            p, t, td, ps, ts, tds = sig_d
+            P = p[c0:c0 + n2, :nk]
+        else:
+            p, t, td, ps, ts, tds = prs_d
+            P = p[:nk]
+        return b.request(P, t[c0:c0 + n2, :nk], td[c0:c0 + n2, :nk], ps[c0:c0 + n2],
+                         ts[c0:c0 + n2], tds[c0:c0 + n2], source=r["source"],
+                         adiabat=r["adiabat"], vertical_lev=r["grid"])
+
+    def serve(guess):
+        stream = torch.cuda.current_stream(dev)
+        host_out = torch.empty(2 * max_cols, dtype=torch.float32).pin_memory()
+        with CapeBatch(max_requests=4096, max_columns=max_cols, guess=guess) as b:
+            # warm-up: one batch of the first requests
+            b.run([descriptor(b, r) for r in trace[:8]])
+            torch.cuda.synchronize()
+            lat, batches, busy, cols, nxt = [], [], 0.0, 0, 0
+            t0 = time.perf_counter()
+            while nxt < len(trace):
+                now = time.perf_counter() - t0
+                if trace[nxt]["arrival"] > now:
+                    time.sleep(trace[nxt]["arrival"] - now)
+                    continue
+                # admit what has arrived, up to the executor's column capacity
+                take, used = [], 0
+                while nxt < len(trace) and trace[nxt]["arrival"] <= now:
+                    need = (trace[nxt]["n2"] + 31) // 32 * 32
+                    if take and used + need > max_cols:
+                        break
+                    take.append(trace[nxt])
+                    used += need
+                    nxt += 1
+                tb = time.perf_counter()
+                reqs = [descriptor(b, r) for r in take]
+                b.run(reqs)
+                off = 0
+                for q in reqs:  # results back to the host, on the same stream
+                    n = q.cape.numel()
+                    host_out[off:off + n].copy_(q.cape, non_blocking=True)
+                    host_out[max_cols + off:max_cols + off + n].copy_(q.cin, non_blocking=True)
+                    off += n
+                stream.synchronize()
+                done = time.perf_counter() - t0
+                busy += time.perf_counter() - tb
+                batches.append(len(take))
+                cols += sum(r["n2"] for r in take)
+                lat += [done - r["arrival"] for r in take]
+            wall = time.perf_counter() - t0
+        lat_ms = np.array(lat) * 1e3
+        return {"requests": len(lat), "columns": cols, "wall_s": wall,
+                "columns_per_s": cols / wall, "busy_fraction": busy / wall,
+                "columns_per_busy_s": cols / busy,
+                "p50_ms": float(np.percentile(lat_ms, 50)),
+                "p99_ms": float(np.percentile(lat_ms, 99)),
+                "max_ms": float(lat_ms.max()), "batches": len(batches),
+                "mean_requests_per_batch": float(np.mean(batches)),
+                "graph_launches": len(batches)}
+
+    res = {g: serve(g) for g in ("learned", "plain")}
+    line = {"metric": SERVE_METRIC, "impl": "ours", "n_gpus": 1, "workload": "serve",
+            "config": {"rate_per_s": SERVE_RATE, "seconds": args.serve_seconds,
+                       "requests": len(trace), "columns": "log-uniform 1e3..1e6",
+                       "levels": "uniform 20..137", "grids": "sigma, pressure (ragged)",
+                       "sources": "surface, most-unstable, mixed-layer",
+                       "adiabats": "all four", "inputs": "device-resident pools",
+                       "results": "cape, cin copied to pinned host memory"},
+            "learned": res["learned"], "plain": res["plain"],
+            "p99_speedup": res["plain"]["p99_ms"] / res["learned"]["p99_ms"],
+            "busy_throughput_speedup": res["learned"]["columns_per_busy_s"] /
+            res["plain"]["columns_per_busy_s"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "srh":
         return run_srh(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

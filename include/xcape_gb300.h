@@ -64,8 +64,9 @@ extern "C" {
  * damped step 0.3 * (F(x) - x), stop when |F(x) - x| <= 2e-4 K, give up after
  * 100 steps (CAPE_CODE_model_lev.f90:431-480).  The other modes keep the map
  * F, the stopping test and the result th2 = F(x), and change how x moves:
- * a better first guess, then secant steps on F(x) - x, with approximate
- * (a few ulp) hardware exp and divides. */
+ * a better first guess, then secant steps on F(x) - x; they evaluate F with
+ * one logarithm per sub-step for pi2 and ln(p2/p1) and one approximate (a few
+ * ulp) divide in its exponent, and agree with the FP64 run within tolerance. */
 #define XC_GUESS_PLAIN 0
 #define XC_GUESS_LEARNED 1      /* extrapolated, with the guess network's guess on the
                                    first sub-step that starts saturated */
@@ -302,6 +303,65 @@ const char *xc_last_error(void);
 
 /* Library version string. */
 const char *xc_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Ragged batches in one persistent, graph-captured kernel.  No counterpart  */
+/* in the reference, whose unit of work is one f2py call on one array         */
+/* (loopcape_ml, CAPE_CODE_model_lev.f90:4-91; loopcape_pl1d,                 */
+/* CAPE_CODE_pressure_lev.f90:88-169): a batch runs many such calls, each     */
+/* with its own sizes and options, in one launch.                             */
+/* ------------------------------------------------------------------------ */
+
+/* One calc_cape request: float32 DEVICE arrays.
+ *   grid 1 (sigma / model levels): p, t3d, td3d are [n2][ld];
+ *   grid 2 (pressure levels): p is [nk], shared by the request's columns,
+ *          t3d and td3d are [n2][ld]; each column's start level is derived
+ *          from its ps (below-ground levels masked, core.py:286-289).
+ * The first nk of every ld values are a column's levels (ld >= nk; ld = nk
+ * for a dense array).  ps, ts, tds, cape, cin, mulvl, z_out, status: [n2].
+ * pinc, source, ml_depth, adiabat: as xc_loopcape_ml. */
+typedef struct xc_cape_request {
+  int grid;
+  int nk;
+  long long n2;
+  long long ld;
+  const float *p, *t3d, *td3d, *ps, *ts, *tds;
+  float pinc;
+  int source;
+  float ml_depth;
+  int adiabat;
+  float *cape, *cin;
+  int *mulvl;
+  float *z_out;
+  int *status; /* nullable */
+} xc_cape_request;
+
+#define XC_BATCH_MAX_REQUESTS 65536
+
+typedef struct xc_batch xc_batch; /* opaque batch executor */
+
+/* Creates an executor on the current device for batches of up to
+ * max_requests requests and max_columns columns, each request's column
+ * count rounded up to a multiple of 32.  guess: XC_GUESS_PLAIN,
+ * XC_GUESS_LEARNED (needs xc_guess_set_weights first) or
+ * XC_GUESS_EXTRAPOLATED.  It allocates two request tables on the device,
+ * two pinned staging tables, and instantiates two CUDA graphs.  Each graph
+ * uploads a table, clears the work counters and launches the persistent
+ * kernel (one wave of blocks that take 32-column chunks from an atomic
+ * counter). */
+int xc_batch_create(int max_requests, long long max_columns, int guess, xc_batch **out);
+/* Runs one batch: reqs is a HOST array of nreq descriptors.  Every request
+ * is validated first; an invalid request or a batch over the executor's
+ * capacity returns XC_ERR_INVALID with nothing launched.  Otherwise the
+ * descriptors are written to a staging table and its graph is launched on
+ * `stream`.  The outputs are complete when `stream` reaches this point.
+ * Runs alternate between the two tables; a run first waits for the run
+ * before the previous one. */
+int xc_batch_run(xc_batch *b, const xc_cape_request *reqs, int nreq, void *stream);
+/* Sub-steps and fixed-point iterations of the last run (waits for it). */
+int xc_batch_work(xc_batch *b, long long *substeps, long long *iterations);
+/* Waits for the executor's runs and frees it (NULL is a no-op). */
+int xc_batch_destroy(xc_batch *b);
 
 #ifdef __cplusplus
 }

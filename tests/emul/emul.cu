@@ -119,3 +119,17 @@ extern "C" void emu_guess_pairs(long long n, unsigned long long seed, float *fea
                                 float *targets, int *iters) {
   for (long long i = 0; i < n; ++i) iters[i] = guess_pair(seed, i, feats + 3 * i, targets + i);
 }
+
+// Size and field offsets of xc_cape_request, for the ctypes layout check.
+#include <cstddef>
+#include "../../include/xcape_gb300.h"
+extern "C" void emu_request_layout(long long *out) {
+  out[0] = (long long)sizeof(xc_cape_request);
+  out[1] = offsetof(xc_cape_request, n2);
+  out[2] = offsetof(xc_cape_request, ld);
+  out[3] = offsetof(xc_cape_request, p);
+  out[4] = offsetof(xc_cape_request, pinc);
+  out[5] = offsetof(xc_cape_request, adiabat);
+  out[6] = offsetof(xc_cape_request, cape);
+  out[7] = offsetof(xc_cape_request, status);
+}

@@ -1,0 +1,168 @@
+"""GPU tests of the ragged batch executor (xcape_gb300.batch, xc_batch_*).
+
+A batch mixes sigma and pressure-level requests, dense arrays and views of
+the first nk levels of wider arrays, every source and adiabat, empty
+requests and column counts that are not multiples of 32.  Each request's
+outputs must match those of the single-request entry point (xc_loopcape_ex)
+on the same columns: bit for bit with the plain solver (the reference's
+iteration), whose every operation is IEEE and uncontracted where it matters.
+With the accelerated solvers the two kernels inline the same column routine
+into different code, the compiler fuses a few multiply-adds differently, and
+the iteration then stops at another point inside its 2e-4 K tolerance: the
+parcel level and status must still be identical, CAPE and CIN agree within
+max(0.5 J/kg, 2e-4 relative) -- well inside the 1 J/kg contract against FP64.
+"""
+import numpy as np
+import pytest
+
+from xcape_gb300 import _lib
+from xcape_gb300 import synthetic as S
+
+from gpu_util import cape_device, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+POOL_LEVELS = 137
+
+
+@pytest.fixture(scope="module")
+def pools():
+    torch = torch_cuda()
+    sig = S.sigma_c0(shape=(1, 4096), nlev=POOL_LEVELS, seed=21, dtype=np.float32)
+    prs = S.pressure_c1(shape=(1, 6144), nlev=POOL_LEVELS, seed=22)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+    sig_d = [dev(np.reshape(a, (4096, -1)) if a.ndim > 1 and a.shape[-1] == POOL_LEVELS
+                 else np.ravel(a)) for a in sig]
+    prs_d = [dev(prs[0])] + [dev(np.reshape(a, (6144, -1)) if a.ndim > 1 and
+                                 a.shape[-1] == POOL_LEVELS else np.ravel(a)) for a in prs[1:]]
+    return sig, sig_d, prs, prs_d
+
+
+def _spec():
+    # (grid, first column, n2, nk, dense copy?, source, adiabat)
+    return [
+        ("sigma", 0, 3000, 40, True, "surface", "pseudo-liquid"),
+        ("sigma", 100, 1000, 25, False, "most-unstable", "reversible-ice"),
+        ("pressure", 0, 5000, 37, True, "mixed-layer", "pseudo-ice"),
+        ("pressure", 200, 777, 60, False, "surface", "reversible-liquid"),
+        ("sigma", 0, 0, 40, True, "surface", "pseudo-liquid"),
+        ("sigma", 3000, 64, 137, False, "mixed-layer", "pseudo-liquid"),
+        ("pressure", 5000, 33, 137, False, "most-unstable", "pseudo-liquid"),
+    ]
+
+
+def _build(batch, pools, spec):
+    sig, sig_d, prs, prs_d = pools
+    reqs, refs = [], []
+    for grid, c0, n2, nk, dense, source, adiabat in spec:
+        if grid == "sigma":
+            p, t, td, ps, ts, tds = sig_d
+            args_np = [np.reshape(a, (4096, -1))[c0:c0 + n2, :nk] for a in sig[:3]] + \
+                      [np.ravel(a)[c0:c0 + n2] for a in sig[3:]]
+            P, T, TD = (x[c0:c0 + n2, :nk] for x in (p, t, td))
+        else:
+            p, t, td, ps, ts, tds = prs_d
+            args_np = [prs[0][:nk]] + [np.reshape(a, (6144, -1))[c0:c0 + n2, :nk]
+                                       for a in prs[1:3]] + \
+                      [np.ravel(a)[c0:c0 + n2] for a in prs[3:]]
+            P, T, TD = p[:nk], t[c0:c0 + n2, :nk], td[c0:c0 + n2, :nk]
+        if dense:
+            T, TD = T.contiguous(), TD.contiguous()
+            if grid == "sigma":
+                P = P.contiguous()
+        PS, TS, TDS = (x[c0:c0 + n2] for x in (ps, ts, tds))
+        reqs.append(batch.request(P, T, TD, PS, TS, TDS, source=source, adiabat=adiabat,
+                                  vertical_lev=grid))
+        refs.append((grid, args_np, source, adiabat))
+    return reqs, refs
+
+
+def _same(got, want, exact):
+    for k in ("mulvl", "status"):
+        np.testing.assert_array_equal(getattr(got, k).cpu().numpy(), want[k], err_msg=k)
+    for k in ("cape", "cin", "z_out"):
+        g = getattr(got, k).cpu().numpy()
+        if exact:
+            np.testing.assert_array_equal(g, want[k], err_msg=k)
+        else:
+            np.testing.assert_allclose(g, want[k], rtol=2e-4, atol=0.5, err_msg=k)
+
+
+def _reference(ref, guess):
+    grid, a, source, adiabat = ref
+    if a[1].shape[0] == 0:
+        return None
+    return cape_device(1 if grid == "sigma" else 2, *[np.ascontiguousarray(x) for x in a],
+                       source, adiabat, guess=guess, counters=True)
+
+
+@pytest.mark.parametrize("guess", ["plain", "extrapolated", "learned"])
+def test_batch_matches_single_request_entry_point(pools, guess):
+    torch = torch_cuda()
+    from xcape_gb300.batch import CapeBatch
+    code = {"plain": _lib.XC_GUESS_PLAIN, "extrapolated": _lib.XC_GUESS_EXTRAPOLATED,
+            "learned": _lib.XC_GUESS_LEARNED}[guess]
+    with CapeBatch(max_requests=16, max_columns=1 << 16, guess=guess) as b:
+        reqs, refs = _build(b, pools, _spec())
+        b.run(reqs)
+        torch.cuda.synchronize()
+        nsub, niter = b.work()
+        tot_sub = tot_it = 0
+        for r, ref in zip(reqs, refs):
+            want = _reference(ref, code)
+            if want is None:
+                assert r.cape.numel() == 0
+                continue
+            _same(r, want, exact=guess == "plain")
+            tot_sub += want["nsub_total"]
+            tot_it += want["niter_total"]
+        assert nsub == tot_sub
+        if guess == "plain":
+            assert niter == tot_it
+        else:
+            assert abs(niter - tot_it) <= 1e-3 * tot_it
+
+
+def test_batch_replays_with_another_composition(pools):
+    torch = torch_cuda()
+    from xcape_gb300.batch import CapeBatch
+    spec = _spec()
+    with CapeBatch(max_requests=16, max_columns=1 << 16, guess="extrapolated") as b:
+        a1, _ = _build(b, pools, spec)
+        b.run(a1)
+        first = [r.cape.clone() for r in a1]
+        b2, refs2 = _build(b, pools, spec[::-1][:4])
+        b.run(b2)
+        a3, _ = _build(b, pools, spec)
+        b.run(a3)
+        torch.cuda.synchronize()
+        for x, r in zip(first, a3):
+            assert torch.equal(x, r.cape)
+        for r, ref in zip(b2, refs2):
+            want = _reference(ref, _lib.XC_GUESS_EXTRAPOLATED)
+            if want is not None:
+                _same(r, want, exact=False)
+
+
+def test_batch_rejects_invalid_batches_without_launching(pools):
+    torch = torch_cuda()
+    from xcape_gb300.batch import CapeBatch
+    with CapeBatch(max_requests=4, max_columns=4096, guess="plain") as b:
+        reqs, _ = _build(b, pools, _spec()[:1])       # 3000 columns: fits
+        big, _ = _build(b, pools, _spec()[2:3])        # 5000 columns: over max_columns
+        for r in reqs + big:
+            r.cape.fill_(-1.0)
+        with pytest.raises(_lib.XcapeError, match="max_columns"):
+            b.run(reqs + big)
+        with pytest.raises(_lib.XcapeError, match="nreq"):
+            b.run(reqs * 5)
+        bad, _ = _build(b, pools, _spec()[:1])
+        bad[0].desc.adiabat = 7
+        with pytest.raises(_lib.XcapeError):
+            b.run(bad)
+        torch.cuda.synchronize()
+        for r in reqs + big:
+            assert bool((r.cape == -1.0).all())
+        b.run(reqs)
+        torch.cuda.synchronize()
+        assert bool((reqs[0].cape >= 0).all())

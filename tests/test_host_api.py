@@ -146,3 +146,30 @@ def test_python_raises_library_errors():
     with pytest.raises(_lib.XcapeError, match="status 1"):
         _lib.call("xc_loopcape_ml", None, None, None, None, None, None, 0, 500.0, 4, 500.0, 1,
                   10, 4, None, None, None, None, None, None)
+
+
+def test_batch_arguments_are_checked_before_any_cuda_call():
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    # capacity and solver checks come before the device is touched
+    assert L.xc_batch_create(0, 1 << 20, 0, ctypes.byref(h)) == _lib.XC_ERR_INVALID
+    assert L.xc_batch_create(16, 8, 0, ctypes.byref(h)) == _lib.XC_ERR_INVALID
+    assert L.xc_batch_create(16, 1 << 20, _lib.XC_GUESS_SECANT, ctypes.byref(h)) == \
+        _lib.XC_ERR_INVALID
+    assert L.xc_batch_create(16, 1 << 20, 0, None) == _lib.XC_ERR_INVALID
+    assert h.value is None
+    assert L.xc_batch_run(None, None, 0, None) == _lib.XC_ERR_INVALID
+    a, b = ctypes.c_longlong(), ctypes.c_longlong()
+    assert L.xc_batch_work(None, ctypes.byref(a), ctypes.byref(b)) == _lib.XC_ERR_INVALID
+    assert L.xc_batch_destroy(None) == _lib.XC_OK
+
+
+def test_batch_request_descriptor_layout_matches_the_header():
+    emul = pytest.importorskip("emul")
+    if emul.nvcc() is None:
+        pytest.skip("nvcc not available")
+    out = (ctypes.c_longlong * 8)()
+    emul.lib().emu_request_layout(out)
+    R = _lib.CapeRequest
+    assert list(out) == [ctypes.sizeof(R), R.n2.offset, R.ld.offset, R.p.offset, R.pinc.offset,
+                         R.adiabat.offset, R.cape.offset, R.status.offset]

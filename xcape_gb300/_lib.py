@@ -69,7 +69,21 @@ SIGNATURES = {
     "xc_guess_adam": [_vp, _vp, _vp, _vp, _f, _i, _vp],
     "xc_guess_eval": [_vp, _vp, ctypes.c_longlong, _vp, _vp],
     "xc_release_workspace": [],
+    "xc_batch_create": [_i, ctypes.c_longlong, _i, ctypes.POINTER(_vp)],
+    "xc_batch_run": [_vp, _vp, _i, _vp],
+    "xc_batch_work": [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
+    "xc_batch_destroy": [_vp],
 }
+
+XC_BATCH_MAX_REQUESTS = 65536
+
+
+class CapeRequest(ctypes.Structure):
+    """xc_cape_request (include/xcape_gb300.h): one request of a batch."""
+    _fields_ = [("grid", _i), ("nk", _i), ("n2", ctypes.c_longlong), ("ld", ctypes.c_longlong),
+                ("p", _vp), ("t3d", _vp), ("td3d", _vp), ("ps", _vp), ("ts", _vp), ("tds", _vp),
+                ("pinc", _f), ("source", _i), ("ml_depth", _f), ("adiabat", _i),
+                ("cape", _vp), ("cin", _vp), ("mulvl", _vp), ("z_out", _vp), ("status", _vp)]
 
 
 class XcapeError(RuntimeError):

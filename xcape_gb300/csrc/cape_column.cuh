@@ -550,9 +550,10 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
 XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter,
                            const float *guess_w = nullptr) {
-    const T *tin = (const T *)a.t + i * a.nk;
-    const T *tdin = (const T *)a.td + i * a.nk;
-    const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
+    const long long stride = a.ld > 0 ? a.ld : a.nk;
+    const T *tin = (const T *)a.t + i * stride;
+    const T *tdin = (const T *)a.td + i * stride;
+    const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * stride;
     const float ts = ldf((const T *)a.ts + i);
     float cape = 0.0f, cin = 0.0f, zo = 0.0f;
     int mulvl = 0, status = 0;

@@ -562,4 +562,10 @@ int set_error(int code, const char *msg) {
   snprintf(g_err, sizeof(g_err), "%s", msg);
   return code;
 }
+// For the batch executor (batch.cu): the loaded guess network, and the
+// option checks of the single-request entry points.
+int guess_weights_ptr(const float **out) { return guess_weights(out); }
+int check_cape_options(float pinc, int source, float ml_depth, int adiabat) {
+  return check_cape_opts(pinc, source, ml_depth, adiabat);
+}
 }  // namespace xc

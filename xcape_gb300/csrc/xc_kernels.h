@@ -15,6 +15,7 @@ struct CapeArgs {
   int adiabat;
   int nk;
   long long n2;
+  long long ld = 0;        // elements between consecutive columns of p (3-D), t, td; 0: nk
   int guess;
   float *cape, *cin;
   int *mulvl;
