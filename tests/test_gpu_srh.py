@@ -214,3 +214,20 @@ def test_srh_fp32_precision_vs_fp64(depth):
             np.testing.assert_allclose(g, w, rtol=0, atol=0.05)
         for g, w in zip(got[2:], want[2:]):
             np.testing.assert_allclose(g, w, rtol=0, atol=1e-3)
+
+
+@pytest.mark.parametrize("depth", [1000, 3000])
+def test_srh_fp32_staged_tile_matches_unstaged_path(depth):
+    """float32 inputs take the shared-memory tile kernel (srh_tile_kernel);
+    the same values as float64 take the unstaged FP32 column path.  Both run
+    the same operations on the same float values (the translation unit is
+    built without FMA contraction), so every output is bit-identical, for
+    sigma and pressure grids, ragged starts and a partial last tile."""
+    for args, vl in ((S.srh_c2(shape=(37, 41)), "model"),
+                     (S.pressure_srh(shape=(29, 33)), "pressure")):
+        a32 = [np.asarray(x, np.float32) for x in args]
+        a64 = [x.astype(np.float64) for x in a32]
+        got = X.calc_srh(*a32, depth=depth, vertical_lev=vl, output_var="all", precision="fp32")
+        want = X.calc_srh(*a64, depth=depth, vertical_lev=vl, output_var="all", precision="fp32")
+        for g, w in zip(got, want):
+            np.testing.assert_array_equal(g, w)

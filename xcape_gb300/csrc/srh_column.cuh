@@ -154,6 +154,37 @@ struct SrhColumn {
   int base;  // start - 3: the 0-based input index of assembled level j is base + j
 };
 
+// Level readers of the fused path.  GlobalLevels reads the input arrays of
+// one column (the virtual temperature computed from p, t, td as the level
+// is reached); SharedLevels reads rows that srh_tile_kernel staged in shared
+// memory, with the virtual temperature already computed.
+template <bool F32, typename T>
+struct GlobalLevels {
+  typedef typename SrhReal<F32>::type R;
+  const SrhColumn<T> *c;
+  XC_HD R p(int m) const { return F32 ? (R)ldf(c->p + m) : (R)ldd(c->p + m); }
+  XC_HD R tv(int m, R P) const {
+    return F32 ? (R)stdh_tv_f((float)P, ldf(c->t + m), ldf(c->td + m))
+               : (R)stdh_tv((double)P, ldd(c->t + m), ldd(c->td + m));
+  }
+  XC_HD R u(int m) const { return F32 ? (R)ldf(c->u + m) : (R)ldd(c->u + m); }
+  XC_HD R v(int m) const { return F32 ? (R)ldf(c->v + m) : (R)ldd(c->v + m); }
+};
+
+struct SharedLevels {  // FP32 path only
+  const float *P, *TV, *U, *V;
+  XC_HD float p(int m) const { return P[m]; }
+  XC_HD float tv(int m, float) const { return TV[m]; }
+  XC_HD float u(int m) const { return U[m]; }
+  XC_HD float v(int m) const { return V[m]; }
+};
+
+// Surface values and level window of one column.
+struct SrhSurface {
+  double ps, ts, tds, us, vs;
+  int base;  // start - 3: the 0-based input index of assembled level j is base + j
+};
+
 struct SrhPass1 {
   int ktop;
   double utop, vtop;  // interpolated winds at `depth` (level ktop)
@@ -162,9 +193,9 @@ struct SrhPass1 {
 
 // Pass 1 over levels 2..ncl (see the file comment).  F32 selects the FP32
 // height integration (Kahan-compensated) and FP32 helicity inputs.
-template <bool DEC, bool F32, typename T>
-XC_HD SrhPass1 srh_pass1(const SrhColumn<T> &c, int ncl, double depth, double aglh0, float *u6,
-                         float *v6) {
+template <bool DEC, bool F32, typename LV>
+XC_HD SrhPass1 srh_pass1(const LV &lv, const SrhSurface &c, int ncl, double depth, double aglh0,
+                         float *u6, float *v6) {
   typedef typename SrhReal<F32>::type R;
   SrhPass1 r;
   r.ktop = 0;
@@ -180,19 +211,17 @@ XC_HD SrhPass1 srh_pass1(const SrhColumn<T> &c, int ncl, double depth, double ag
   R udprev = (R)c.us, vdprev = (R)c.vs;
   for (int j = 2; j <= ncl; ++j) {
     const int m = c.base + j;
-    R P, Tv, H;
+    const R P = lv.p(m);
+    const R Tv = lv.tv(m, P);
+    R H;
     if (F32) {
-      P = (R)ldf(c.p + m);
-      Tv = (R)stdh_tv_f((float)P, ldf(c.t + m), ldf(c.td + m));
       Hsum.add((R)stdh_dh_f((float)Tv, (float)Tvprev, (float)P, (float)Pprev));
       H = Hsum.s;
     } else {
-      P = (R)ldd(c.p + m);
-      Tv = (R)stdh_tv((double)P, ldd(c.t + m), ldd(c.td + m));
       H = (R)stdh_step((double)Hprev, (double)Tv, (double)Tvprev, (double)P, (double)Pprev);
     }
-    const R ud = F32 ? (R)ldf(c.u + m) : (R)ldd(c.u + m);
-    const R vd = F32 ? (R)ldf(c.v + m) : (R)ldd(c.v + m);
+    const R ud = lv.u(m);
+    const R vd = lv.v(m);
     const float zf = (float)H, uf = (float)ud, vf = (float)vd;
     bunkers_bracket<DEC>(zprev, zf, uprev, uf, vprev, vf, u6, v6);
     if (r.ktop == 0 && H > rdepth) {
@@ -219,45 +248,24 @@ XC_HD SrhPass1 srh_pass1(const SrhColumn<T> &c, int ncl, double depth, double ag
   return r;
 }
 
-// Column i of the fused SRH path (core.py:_calc_srh_numpy :473-542).
-// F32 = false follows the reference's precisions (FP64 stdheight and SREH,
-// FP32 Bunkers); F32 = true runs the stdheight and SREH stages in FP32 with
-// compensated sums.
-template <typename T, int GRID, bool F32 = false>
-XC_HD void srh_column_run(const SrhArgs &a, long long i) {
+// Passes 1 and 2 of column i (levels through `lv`), and its outputs.
+template <bool F32, typename LV>
+XC_HD void srh_column_body(const SrhArgs &a, long long i, const LV &lv, const SrhSurface &c,
+                           int ncl) {
   typedef typename SrhReal<F32>::type R;
-  SrhColumn<T> c;
-  c.p = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
-  c.t = (const T *)a.t + i * a.nk;
-  c.td = (const T *)a.td + i * a.nk;
-  c.u = (const T *)a.u + i * a.nk;
-  c.v = (const T *)a.v + i * a.nk;
-  c.ps = ldd((const T *)a.ps + i);
-  c.ts = ldd((const T *)a.ts + i);
-  c.tds = ldd((const T *)a.tds + i);
-  c.us = ldd((const T *)a.us + i);
-  c.vs = ldd((const T *)a.vs + i);
-  int st = 1;
-  if (GRID == 2) {
-    st = a.start ? ld(a.start + i) : pres_lev_pos_col<T>((const T *)a.p, ld((const T *)a.ps + i), a.nk);
-    st = st < 1 ? 1 : (st > a.nk + 1 ? a.nk + 1 : st);
-  }
-  c.base = st - 3;
-  const int ncl = a.nk - st + 2;
-
   float u6[12], v6[12];
   for (int k = 0; k < 12; ++k) {
     u6[k] = VMSG;
     v6[k] = VMSG;
   }
-  SrhPass1 r = srh_pass1<false, F32>(c, ncl, a.depth, a.aglh0, u6, v6);
+  SrhPass1 r = srh_pass1<false, F32>(lv, c, ncl, a.depth, a.aglh0, u6, v6);
   if ((float)a.aglh0 > r.ztop_f) {
     // Z(1) > Z(NZ): DINTERP2DZ switches to the decreasing-height rule.
     for (int k = 0; k < 12; ++k) {
       u6[k] = VMSG;
       v6[k] = VMSG;
     }
-    r = srh_pass1<true, F32>(c, ncl, a.depth, a.aglh0, u6, v6);
+    r = srh_pass1<true, F32>(lv, c, ncl, a.depth, a.aglh0, u6, v6);
   }
   float rm[2], lm[2], mean[2];
   bunkers_finish((float)c.us, (float)c.vs, u6, v6, rm, lm, mean);
@@ -279,8 +287,8 @@ XC_HD void srh_column_run(const SrhArgs &a, long long i) {
       uk = (R)r.utop;
       vk = (R)r.vtop;
     } else {
-      uk = F32 ? (R)ldf(c.u + c.base + k) : (R)ldd(c.u + c.base + k);
-      vk = F32 ? (R)ldf(c.v + c.base + k) : (R)ldd(c.v + c.base + k);
+      uk = lv.u(c.base + k);
+      vk = lv.v(c.base + k);
     }
     s_rm.add(((uk - cu_rm) * (vk - vprev)) - ((vk - cv_rm) * (uk - uprev)));
     s_lm.add(((uk - cu_lm) * (vk - vprev)) - ((vk - cv_lm) * (uk - uprev)));
@@ -289,6 +297,42 @@ XC_HD void srh_column_run(const SrhArgs &a, long long i) {
   }
   a.srh_rm[i] = -(double)s_rm.s;
   a.srh_lm[i] = -(double)s_lm.s;
+}
+
+// Column i of the fused SRH path (core.py:_calc_srh_numpy :473-542).
+// F32 = false follows the reference's precisions (FP64 stdheight and SREH,
+// FP32 Bunkers); F32 = true runs the stdheight and SREH stages in FP32 with
+// compensated sums.
+template <typename T, int GRID, bool F32 = false>
+XC_HD void srh_column_run(const SrhArgs &a, long long i) {
+  SrhColumn<T> c;
+  c.p = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
+  c.t = (const T *)a.t + i * a.nk;
+  c.td = (const T *)a.td + i * a.nk;
+  c.u = (const T *)a.u + i * a.nk;
+  c.v = (const T *)a.v + i * a.nk;
+  c.ps = ldd((const T *)a.ps + i);
+  c.ts = ldd((const T *)a.ts + i);
+  c.tds = ldd((const T *)a.tds + i);
+  c.us = ldd((const T *)a.us + i);
+  c.vs = ldd((const T *)a.vs + i);
+  int st = 1;
+  if (GRID == 2) {
+    st = a.start ? ld(a.start + i) : pres_lev_pos_col<T>((const T *)a.p, ld((const T *)a.ps + i), a.nk);
+    st = st < 1 ? 1 : (st > a.nk + 1 ? a.nk + 1 : st);
+  }
+  c.base = st - 3;
+  const int ncl = a.nk - st + 2;
+  SrhSurface sf;
+  sf.ps = c.ps;
+  sf.ts = c.ts;
+  sf.tds = c.tds;
+  sf.us = c.us;
+  sf.vs = c.vs;
+  sf.base = c.base;
+  GlobalLevels<F32, T> lv;
+  lv.c = &c;
+  srh_column_body<F32>(a, i, lv, sf, ncl);
 }
 
 // ---- stage columns -----------------------------------------------------------

@@ -1,6 +1,8 @@
 // srh_kernel.cu -- storm-relative helicity kernels for sm_103a: one thread per
 // column running the column routines of srh_column.cuh (the fused
 // stdheight -> Bunkers -> SREH path and the three stage loops on their own).
+#include <stdint.h>
+
 #include "srh_column.cuh"
 
 namespace xc {
@@ -37,6 +39,124 @@ __global__ void sreh_kernel(const double *u, const double *v, const double *aglh
                     sreh_rm, sreh_lm);
 }
 
+// FP32 path for float inputs with the column tile staged in shared memory.
+// One warp per block takes 32 consecutive columns, whose rows (nk levels
+// each) are one contiguous range of every input array.  The warp first walks
+// that range together -- every load a full, coalesced line, 16 bytes per lane
+// where the arrays are 16-byte aligned -- computing the virtual temperature
+// of each (column, level) element as it goes, and stores the rows of p
+// (sigma grids), Tv, u and v in shared memory with an odd row stride S
+// (lanes then read the same level of their own rows in distinct banks).
+// Each lane then runs passes 1 and 2 of its column from those rows
+// (srh_column_body, the code of the FP32 column path).  Without staging,
+// each lane walks its own 200-byte row through the cache, a warp's level
+// load touches 32 lines, and the lines leave L1 before their next levels are
+// read: the kernel fetched 5.4x its algorithmic bytes.
+constexpr int SRH_TILE = 32;
+
+__host__ __device__ inline int srh_tile_stride(int nk) { return nk | 1; }
+
+inline size_t srh_tile_smem(int grid, int nk) {
+  const size_t S = (size_t)srh_tile_stride(nk);
+  return sizeof(float) * (grid == 1 ? 4 * SRH_TILE * S : 3 * SRH_TILE * S + (size_t)nk);
+}
+constexpr size_t SRH_TILE_SMEM_MAX = 200 * 1024;
+
+template <int GRID>
+__device__ __forceinline__ void srh_stage(float *TV, float *U, float *V, float *P, int S, int nk,
+                                          int e, float p, float t, float td, float u, float v) {
+  const int c = e / nk, m = e - c * nk;
+  if (GRID == 1) P[c * S + m] = p;
+  else p = P[m];
+  TV[c * S + m] = stdh_tv_f(p, t, td);
+  U[c * S + m] = u;
+  V[c * S + m] = v;
+}
+
+template <int GRID>
+__global__ void __launch_bounds__(SRH_TILE) srh_tile_kernel(SrhArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  const int nk = a.nk, S = srh_tile_stride(nk);
+  float *TV = sm, *U = TV + SRH_TILE * S, *V = U + SRH_TILE * S, *P = V + SRH_TILE * S;
+  const long long i0 = (long long)blockIdx.x * SRH_TILE;
+  const int lane = threadIdx.x;
+  const int ncols = (int)min((long long)SRH_TILE, a.n2 - i0);
+  const long long e0 = i0 * nk;
+  const int ne = ncols * nk;
+  const float *gp = (const float *)a.p, *gt = (const float *)a.t, *gtd = (const float *)a.td;
+  const float *gu = (const float *)a.u, *gv = (const float *)a.v;
+  if (GRID == 2) {
+    for (int m = lane; m < nk; m += 32) P[m] = __ldg(gp + m);
+    __syncwarp();
+  } else {
+    gp += e0;
+  }
+  gt += e0;
+  gtd += e0;
+  gu += e0;
+  gv += e0;
+  const bool vec = ((((uintptr_t)gt | (uintptr_t)gtd | (uintptr_t)gu | (uintptr_t)gv |
+                      (GRID == 1 ? (uintptr_t)gp : 0)) & 15) == 0);
+  int done = 0;
+  if (vec) {
+    const int nq = ne >> 2;
+#pragma unroll 2
+    for (int q = lane; q < nq; q += 32) {
+      const float4 t4 = __ldg(reinterpret_cast<const float4 *>(gt) + q);
+      const float4 d4 = __ldg(reinterpret_cast<const float4 *>(gtd) + q);
+      const float4 u4 = __ldg(reinterpret_cast<const float4 *>(gu) + q);
+      const float4 v4 = __ldg(reinterpret_cast<const float4 *>(gv) + q);
+      float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (GRID == 1) p4 = __ldg(reinterpret_cast<const float4 *>(gp) + q);
+      const int e = 4 * q;
+      srh_stage<GRID>(TV, U, V, P, S, nk, e, p4.x, t4.x, d4.x, u4.x, v4.x);
+      srh_stage<GRID>(TV, U, V, P, S, nk, e + 1, p4.y, t4.y, d4.y, u4.y, v4.y);
+      srh_stage<GRID>(TV, U, V, P, S, nk, e + 2, p4.z, t4.z, d4.z, u4.z, v4.z);
+      srh_stage<GRID>(TV, U, V, P, S, nk, e + 3, p4.w, t4.w, d4.w, u4.w, v4.w);
+    }
+    done = nq << 2;
+  }
+  for (int e = done + lane; e < ne; e += 32)
+    srh_stage<GRID>(TV, U, V, P, S, nk, e, GRID == 1 ? __ldg(gp + e) : 0.0f, __ldg(gt + e),
+                    __ldg(gtd + e), __ldg(gu + e), __ldg(gv + e));
+  __syncwarp();
+  if (lane >= ncols) return;
+  const long long i = i0 + lane;
+  SrhSurface sf;
+  sf.ps = ldd((const float *)a.ps + i);
+  sf.ts = ldd((const float *)a.ts + i);
+  sf.tds = ldd((const float *)a.tds + i);
+  sf.us = ldd((const float *)a.us + i);
+  sf.vs = ldd((const float *)a.vs + i);
+  int st = 1;
+  if (GRID == 2) {
+    st = a.start ? __ldg(a.start + i)
+                 : pres_lev_pos_col<float>((const float *)a.p, __ldg((const float *)a.ps + i), nk);
+    st = st < 1 ? 1 : (st > nk + 1 ? nk + 1 : st);
+  }
+  sf.base = st - 3;
+  SharedLevels lv;
+  lv.P = GRID == 1 ? P + lane * S : P;
+  lv.TV = TV + lane * S;
+  lv.U = U + lane * S;
+  lv.V = V + lane * S;
+  srh_column_body<true>(a, i, lv, sf, nk - st + 2);
+}
+
+template <int GRID>
+static cudaError_t launch_srh_tile(const SrhArgs &a, size_t smem, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        srh_tile_kernel<GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SRH_TILE_SMEM_MAX);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const unsigned blocks = (unsigned)((a.n2 + SRH_TILE - 1) / SRH_TILE);
+  srh_tile_kernel<GRID><<<blocks, SRH_TILE, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 static unsigned blocks_for(long long n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
@@ -59,6 +179,11 @@ static void launch_srh_p(const SrhArgs &a, unsigned blocks, cudaStream_t s) {
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s) {
   const unsigned blocks = blocks_for(a.n2, 128);
   if (blocks == 0) return cudaSuccess;
+  if (a.precision == 1 && a.dtype == 0) {
+    const size_t smem = srh_tile_smem(a.grid, a.nk);
+    if (smem <= SRH_TILE_SMEM_MAX)
+      return a.grid == 1 ? launch_srh_tile<1>(a, smem, s) : launch_srh_tile<2>(a, smem, s);
+  }
   if (a.precision == 1)
     launch_srh_p<true>(a, blocks, s);
   else
