@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--guess", default="learned",
                     choices=["plain", "extrapolated", "learned", "secant", "learned-every"])
-    ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve"])
+    ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve", "adiabats"])
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the request trace of --workload serve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -631,6 +631,109 @@ def run_serve(args):
     return 0
 
 
+ADIABAT_METRIC = ("CAPE/CIN columns/s at 4M×60 model levels per adiabat: learned-guess vs "
+                  "plain CUDA; iterations saved by the network vs the plain first guess")
+ADIABAT_COLUMNS = 1 << 22   # 4,194,304 columns
+ADIABAT_BASE = 1 << 18      # distinct synthetic columns tiled to ADIABAT_COLUMNS
+ADIABAT_LEVELS = 60
+ADIABAT_NAMES = ("pseudo-liquid", "reversible-liquid", "pseudo-ice", "reversible-ice")
+
+
+def run_adiabats(args):
+    """--workload adiabats: surface-based calc_cape on 4M columns x 60 sigma
+    levels for each adiabat, with the plain solver (the reference's
+    iteration), the learned solver, and, for the network's own contribution,
+    the secant solver from the plain first guess against the same solver from
+    the network's guess on every saturated sub-step (equal stopping test)."""
+    import torch
+    from xcape_gb300 import _lib
+    from xcape_gb300 import guess as G
+    from xcape_gb300 import synthetic as S
+    world, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    G.ensure_loaded()
+    L = _lib.lib()
+    reps = ADIABAT_COLUMNS // ADIABAT_BASE
+    base = S.sigma_c0(shape=(ADIABAT_BASE,), nlev=ADIABAT_LEVELS, seed=3, dtype=np.float32)
+    d = [torch.from_numpy(np.ascontiguousarray(a)).to(dev).repeat((reps, 1) if a.ndim == 2
+                                                                  else (reps,)) for a in base]
+    n2 = ADIABAT_COLUMNS
+    cape, cin, zout = (torch.empty(n2, dtype=torch.float32, device=dev) for _ in range(3))
+    mulvl = torch.empty(n2, dtype=torch.int32, device=dev)
+    ws_bytes = _lib.workspace_bytes(n2)
+    wsbuf = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
+    ws = wsbuf.data_ptr() + (-wsbuf.data_ptr()) % 256
+    stream = torch.cuda.current_stream(dev)
+    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+
+    def launch(adiabat, guess, counters=None):
+        _lib.check(L.xc_loopcape_ex(1, *[x.data_ptr() for x in d], _lib.XC_F32, PINC, 1, ML_DEPTH,
+                                    adiabat, None, ADIABAT_LEVELS, n2, guess, cape.data_ptr(),
+                                    cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), None,
+                                    counters, ws, ws_bytes, stream.cuda_stream))
+
+    def measure(adiabat, guess, steps):
+        cnt.zero_()
+        launch(adiabat, guess, cnt.data_ptr())
+        torch.cuda.synchronize()
+        work = [int(x) for x in cnt.cpu()]
+        for _ in range(2):
+            launch(adiabat, guess)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            launch(adiabat, guess)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, work
+
+    out = {}
+    with ClockSampler(local) as clk:
+        for code, name in enumerate(ADIABAT_NAMES, start=1):
+            r = {}
+            for g, gname, steps in ((_lib.XC_GUESS_PLAIN, "plain", args.steps),
+                                    (_lib.XC_GUESS_LEARNED, "learned", args.steps),
+                                    (_lib.XC_GUESS_SECANT, "secant", 2),
+                                    (_lib.XC_GUESS_LEARNED_EVERY, "learned-every", 1)):
+                ms, work = measure(code, g, steps)
+                r[gname] = {"ms": ms, "substeps": work[0], "iterations": work[1]}
+            r["learned_speedup_vs_plain"] = r["plain"]["ms"] / r["learned"]["ms"]
+            r["network_iterations_saved_vs_plain_guess"] = \
+                1.0 - r["learned-every"]["iterations"] / r["secant"]["iterations"]
+            if not args.no_cpu_baseline:
+                # the learned solver's CAPE on the first columns against FP64 (the checker)
+                launch(code, _lib.XC_GUESS_LEARNED)
+                torch.cuda.synchronize()
+                r["accuracy_vs_fp64"] = _adiabat_accuracy(base, cape, code)
+            out[name] = r
+    line = {"metric": ADIABAT_METRIC, "impl": "ours", "n_gpus": 1, "workload": "adiabats",
+            "unit": "columns/s", "dtype": "f32", "data": "synthetic",
+            "config": {"columns": n2, "levels": ADIABAT_LEVELS, "grid": "sigma 0.995..0.1",
+                       "source": "surface", "pinc": PINC, "distinct_columns": ADIABAT_BASE,
+                       "steps": args.steps},
+            "per_adiabat": out,
+            "learned_value": {k: n2 / (v["learned"]["ms"] / 1e3) for k, v in out.items()},
+            "plain_value": {k: n2 / (v["plain"]["ms"] / 1e3) for k, v in out.items()},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _adiabat_accuracy(base, cape, code, n=4096):
+    import oracle as O
+    p, t, td, ps, ts, tds = (np.asarray(a)[:n] for a in base)
+    ref = O.loopcape(p, t, td, ps, ts, tds, PINC, 1, ML_DEPTH, code, precision="f64",
+                     nthreads=os.cpu_count() or 1, stats=True)
+    got = cape[:n].cpu().numpy().astype(np.float64)
+    ok = (ref["status"] & 1) == 0
+    dc = np.abs(got[ok] - ref["cape"][ok])
+    return {"columns": n, "compared": int(ok.sum()), "max_abs_dcape": float(dc.max()),
+            "frac_dcape_le_1": float(np.mean(dc <= 1.0))}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -639,6 +742,8 @@ def main():
         return run_srh(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "adiabats":
+        return run_adiabats(args)
     return run_ours(args)
 
 

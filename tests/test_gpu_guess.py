@@ -135,3 +135,29 @@ def test_learned_mode_against_extrapolated_mode():
     # sub-step of a column, where the increment of the sub-step that crossed
     # saturation is a poor predictor
     assert lrn["niter_total"] < ext["niter_total"], (lrn["niter_total"], ext["niter_total"])
+
+
+@pytest.mark.parametrize("adiabat", ["pseudo-liquid", "reversible-liquid", "pseudo-ice",
+                                     "reversible-ice"])
+def test_network_saves_iterations_on_every_adiabat(adiabat):
+    """Sigma levels (60), surface parcels, every adiabat: the network's guess
+    (trained on pseudo-liquid sub-steps) on every saturated sub-step needs
+    fewer iterations than the plain first guess with the same secant steps,
+    and the learned solver stays within the CAPE tolerance of FP64."""
+    G.set_weights(_network())
+    p, t, td, ps, ts, tds = S.sigma_c0(shape=(48, 64), nlev=60, seed=9, dtype=np.float32)
+    runs = {g: cape_device(1, p, t, td, ps, ts, tds, "surface", adiabat, guess=g, counters=True)
+            for g in (_lib.XC_GUESS_SECANT, _lib.XC_GUESS_LEARNED_EVERY, _lib.XC_GUESS_LEARNED)}
+    n2 = ps.size
+    code = {"pseudo-liquid": 1, "reversible-liquid": 2, "pseudo-ice": 3, "reversible-ice": 4}
+    ref = O.loopcape(p.reshape(n2, -1), t.reshape(n2, -1), td.reshape(n2, -1), ps.ravel(),
+                     ts.ravel(), tds.ravel(), 500.0, 1, 500.0, code[adiabat], precision="f64",
+                     stats=True)
+    conv = (ref["status"] & 1) == 0
+    for got in runs.values():
+        assert not np.any((got["status"] & 1).astype(bool) & conv)
+        d = np.abs(got["cape"][conv].astype(np.float64) - ref["cape"][conv])
+        assert np.all(d <= np.maximum(1.0, 1e-3 * ref["cape"][conv])), d.max()
+    sec = runs[_lib.XC_GUESS_SECANT]["niter_total"]
+    every = runs[_lib.XC_GUESS_LEARNED_EVERY]["niter_total"]
+    assert every < 0.95 * sec, (adiabat, every, sec)
