@@ -134,6 +134,26 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
                    float *cape, float *cin, int *mulvl, float *z_out, int *status,
                    long long *counters, void *workspace, size_t workspace_bytes, void *stream);
 
+/* xc_loopcape_ex (natural column order, no counters) with the diagnostics
+ * that getcape computes and discards -- the crossing pressure of its
+ * buoyancy sign changes (CAPE_CODE_model_lev.f90:511, :526) and the parcel
+ * theta-e (:505).  No counterpart entry point in the reference.
+ * diag [n2][6] (device, float):
+ *   0 LFC pressure (hPa), 1 LFC height (m): the lowest point of the first
+ *     layer with positive area -- the negative-to-positive crossing, or the
+ *     layer's base when the parcel is already buoyant there;
+ *   2 EL pressure (hPa), 3 EL height (m): the highest positive-to-negative
+ *     crossing, or the last level reached when the parcel is still buoyant;
+ *   4 height (m) and 5 theta-e (K, getthe) of the source parcel.
+ * Each is -999999 where undefined: no positive area (0-3), no ascent, or a
+ * column whose iteration gave up.  guess: XC_GUESS_PLAIN or
+ * XC_GUESS_LEARNED. */
+int xc_loopcape_diag(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                     const void *ts, const void *tds, int dtype, float pinc, int source,
+                     float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
+                     float *cape, float *cin, int *mulvl, float *z_out, int *status, float *diag,
+                     void *stream);
+
 /* Device workspace that lets xc_loopcape_ex order n2 columns. */
 size_t xc_loopcape_workspace_bytes(int n2);
 

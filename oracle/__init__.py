@@ -63,6 +63,14 @@ def lib():
                 f.argtypes = [rp, rp, rp, rp, rp, rp, rt, _int, rt, _int, _i32p, _int, _int,
                               rp, rp, _i32p, rp, _vp, _vp, _vp, _vp, _int]
                 f.restype = None
+            f = getattr(L, f"oc_loopcape_diag_ml_{prec}")
+            f.argtypes = [rp, rp, rp, rp, rp, rp, rt, _int, rt, _int, _int, _int,
+                          rp, rp, _i32p, rp, _vp, rp, _int]
+            f.restype = None
+            f = getattr(L, f"oc_loopcape_diag_pl1d_{prec}")
+            f.argtypes = [rp, rp, rp, rp, rp, rp, rt, _int, rt, _int, _i32p, _int, _int,
+                          rp, rp, _i32p, rp, _vp, rp, _int]
+            f.restype = None
             f = getattr(L, f"oc_bunkers_loop_ml_{prec}")
             f.argtypes = [rp, rp, rp, rp, rp, rp, _int, _int, rp, rp, rp, _int]
             f.restype = None
@@ -97,6 +105,39 @@ def _c(a, dt):
 # ---------------------------------------------------------------------------
 # Column-loop entry points.  2-D arrays are (n2, nk) C-contiguous, i.e. the
 # memory layout of the Fortran (nk, n2) arrays of the f2py interfaces.
+
+DIAG_FIELDS = ("plfc", "zlfc", "pel", "zel", "zsource", "thetae_source")
+
+
+def loopcape_diag(p, t, td, ps, ts, tds, pinc, source, ml_depth, adiabat, start=None,
+                  precision="f32", nthreads=0):
+    """loopcape_ml (start None) or loopcape_pl1d (1-D p) with the diagnostics
+    getcape computes and discards: a dict with cape, cin, mulvl, z_out,
+    status and the DIAG_FIELDS arrays (LFC/EL pressure in hPa and height in
+    m, source height, source theta-e; -999999 where undefined)."""
+    dt = _dt(precision)
+    t = _c(t, dt)
+    n2, nk = t.shape
+    td = _c(td, dt)
+    ps, ts, tds = (_c(np.ravel(x), dt) for x in (ps, ts, tds))
+    cape, cin, zout = (np.empty(n2, dt) for _ in range(3))
+    mulvl = np.empty(n2, np.int32)
+    status = np.zeros(n2, np.int32)
+    diag = np.empty((n2, 6), dt)
+    L = lib()
+    if start is None:
+        getattr(L, f"oc_loopcape_diag_ml_{precision}")(
+            _c(p, dt), t, td, ps, ts, tds, pinc, source, ml_depth, adiabat, nk, n2, cape, cin,
+            mulvl, zout, status.ctypes.data, diag, nthreads)
+    else:
+        getattr(L, f"oc_loopcape_diag_pl1d_{precision}")(
+            t, td, _c(np.ravel(p), dt), ps, ts, tds, pinc, source, ml_depth, adiabat,
+            _c(np.ravel(start), np.int32), nk, n2, cape, cin, mulvl, zout, status.ctypes.data,
+            diag, nthreads)
+    out = dict(cape=cape, cin=cin, mulvl=mulvl, z_out=zout, status=status)
+    out.update({k: diag[:, j] for j, k in enumerate(DIAG_FIELDS)})
+    return out
+
 
 def loopcape(p, t, td, ps, ts, tds, pinc, source, ml_depth, adiabat, start=None, p_is_1d=False,
              precision="f32", nthreads=0, stats=False):

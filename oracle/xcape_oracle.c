@@ -97,6 +97,13 @@ static real getqvi(real p, real t) {
   return eps * es / (p - es);
 }
 
+/* Dewpoint (K) of mixing ratio q at pressure p (Pa): getqvs solved for t. */
+static real dewpoint_of(real p, real q) {
+  const real eps = LIT(287.04) / LIT(461.5);
+  const real a = R_LOG(q * p / (eps + q) / LIT(611.2));
+  return (LIT(17.67) * LIT(273.15) - LIT(29.65) * a) / (LIT(17.67) - a);
+}
+
 /* CAPE_CODE_model_lev.f90:604-620; x**(-1) is 1/x. */
 static real getthe(real p, real t, real td, real q) {
   real tlcl;
@@ -116,7 +123,8 @@ static real getthe(real p, real t, real td, real q) {
 static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_B, real ts_B,
                     real tds_B, real pinc, int source, real ml_depth, int adiabat, int nk_in,
                     real *cape_out, real *cin_out, int *mulvl_out, real *z_out_out,
-                    int *nsub_out, int *niter_out, int *status_out, float *bmin_out) {
+                    int *nsub_out, int *niter_out, int *status_out, float *bmin_out,
+                    real *diag_out) {
   /* CAPE_CODE_model_lev.f90:188-211 */
   const real g = LIT(9.81);
   const real p00 = LIT(100000.0);
@@ -155,6 +163,20 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
   int doit, ice, not_converged;
   int nsub = 0, niter = 0, status = 0;
   double bmin = INFINITY; /* smallest |buoyancy| met by the ascent (test statistic) */
+  /* Diagnostics the reference computes and discards (the crossing pressure
+   * ps of :511 and :526, the parcel's theta-e): LFC and EL pressure (hPa)
+   * and height (m), source height and theta-e.  LFC: the lowest point of the
+   * first layer with positive area -- the neg->pos crossing, or the layer's
+   * base when the parcel is already buoyant there.  EL: the highest pos->neg
+   * crossing, or the last level reached when the parcel is still buoyant
+   * there.  All -999999 when the parcel never has positive area, when the
+   * ascent does not run, or when the iteration gives up. */
+  const real dmiss = LIT(-999999.);
+  real d_plfc = dmiss, d_zlfc = dmiss, d_pel = dmiss, d_zel = dmiss, d_zsrc = dmiss,
+       d_the = dmiss;
+  int have_lfc = 0, ascended = 0;
+  if (diag_out)
+    for (int d = 0; d < 6; ++d) diag_out[d] = dmiss;
 
   /* :220-225 -- surface first, then the 3-D levels; then :232-240 */
   for (k = 1; k <= nk; ++k) {
@@ -263,6 +285,11 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
     bmin = fabs((double)b2);
   }
   (void)thv2;
+  if (diag_out) {
+    d_zsrc = z[kmax];
+    d_the = (source == 3) ? getthe(p2, t2, dewpoint_of(p2, qv2), qv2)
+                          : getthe(p[kmax], t[kmax], td[kmax], q[kmax]);
+  }
   ql2 = LIT(0.0);
   qi2 = LIT(0.0);
   qt = qv2;
@@ -354,6 +381,33 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
     if (fabs((double)b2) < bmin) bmin = fabs((double)b2);
     dz = -cpdg * LIT(0.5) * (thv[k] + thv[k - 1]) * (pi[k] - pi[k - 1]);
 
+    if (diag_out) {
+      ascended = 1;
+      if ((b2 >= LIT(0.0)) && (b1 < LIT(0.0))) {
+        const real w = (LIT(0.0) - b1) / (b2 - b1);
+        if (!have_lfc) {
+          d_plfc = (p[k - 1] + (p[k] - p[k - 1]) * w) / LIT(100.0);
+          d_zlfc = z[k - 1] + dz * w;
+          have_lfc = 1;
+        }
+      } else if ((b2 < LIT(0.0)) && (b1 > LIT(0.0))) {
+        const real w = (LIT(0.0) - b1) / (b2 - b1);
+        if (!have_lfc) {
+          d_plfc = p[k - 1] / LIT(100.0);
+          d_zlfc = z[k - 1];
+          have_lfc = 1;
+        }
+        d_pel = (p[k - 1] + (p[k] - p[k - 1]) * w) / LIT(100.0);
+        d_zel = z[k - 1] + dz * w;
+      } else if (b2 >= LIT(0.0)) {
+        if (!have_lfc) {
+          d_plfc = p[k - 1] / LIT(100.0);
+          d_zlfc = z[k - 1];
+          have_lfc = 1;
+        }
+      }
+    }
+
     /* :509-547 */
     if ((b2 >= LIT(0.0)) && (b1 < LIT(0.0))) {
       frac = b2 / (b2 - b1);
@@ -379,6 +433,21 @@ static void getcape(const real *p_A, const real *t_A, const real *td_A, real ps_
     z_out = z[k];
   }
 
+  if (diag_out && have_lfc && b2 >= LIT(0.0)) {
+    d_pel = p[k] / LIT(100.0);
+    d_zel = z[k];
+  }
+  if (diag_out) {
+    if (ascended) {
+      diag_out[0] = have_lfc ? d_plfc : dmiss;
+      diag_out[1] = have_lfc ? d_zlfc : dmiss;
+      diag_out[2] = have_lfc ? d_pel : dmiss;
+      diag_out[3] = have_lfc ? d_zel : dmiss;
+      diag_out[4] = d_zsrc;
+      diag_out[5] = d_the;
+    }
+  }
+
 done:
   *cape_out = cape;
   *cin_out = cin;
@@ -392,21 +461,23 @@ done:
 }
 
 /* loopcape_ml, CAPE_CODE_model_lev.f90:76-89: the ts > 0 gate. */
-OC_EXPORT void SFX(oc_loopcape_ml)(const real *p3d, const real *t3d, const real *td3d,
-                                   const real *ps, const real *ts, const real *tds, real pinc,
-                                   int source, real ml_depth, int adiabat, int nk, int n2,
-                                   real *cape, real *cin, int *mulvl, real *z_out, int *nsub,
-                                   int *niter, int *status, float *bmin, int nthreads) {
+static void loopcape_ml_common(const real *p3d, const real *t3d, const real *td3d,
+                               const real *ps, const real *ts, const real *tds, real pinc,
+                               int source, real ml_depth, int adiabat, int nk, int n2, real *cape,
+                               real *cin, int *mulvl, real *z_out, int *nsub, int *niter,
+                               int *status, float *bmin, real *diag, int nthreads) {
   set_threads(nthreads);
   long i;
 #pragma omp parallel for schedule(dynamic, 64)
   for (i = 0; i < n2; ++i) {
     if (bmin) bmin[i] = INFINITY;
+    if (diag)
+      for (int d = 0; d < 6; ++d) diag[6 * i + d] = LIT(-999999.);
     if (ts[i] > LIT(0.0)) {
       getcape(p3d + (size_t)i * nk, t3d + (size_t)i * nk, td3d + (size_t)i * nk, ps[i], ts[i],
               tds[i], pinc, source, ml_depth, adiabat, nk, &cape[i], &cin[i], &mulvl[i],
               &z_out[i], nsub ? &nsub[i] : 0, niter ? &niter[i] : 0, status ? &status[i] : 0,
-              bmin ? &bmin[i] : 0);
+              bmin ? &bmin[i] : 0, diag ? diag + 6 * i : 0);
     } else {
       cape[i] = LIT(0.0);
       cin[i] = LIT(0.0);
@@ -419,6 +490,27 @@ OC_EXPORT void SFX(oc_loopcape_ml)(const real *p3d, const real *t3d, const real 
   }
 }
 
+OC_EXPORT void SFX(oc_loopcape_ml)(const real *p3d, const real *t3d, const real *td3d,
+                                   const real *ps, const real *ts, const real *tds, real pinc,
+                                   int source, real ml_depth, int adiabat, int nk, int n2,
+                                   real *cape, real *cin, int *mulvl, real *z_out, int *nsub,
+                                   int *niter, int *status, float *bmin, int nthreads) {
+  loopcape_ml_common(p3d, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, nk, n2, cape,
+                     cin, mulvl, z_out, nsub, niter, status, bmin, 0, nthreads);
+}
+
+/* loopcape_ml with the diagnostics of getcape: diag [n2][6] = LFC pressure
+ * (hPa), LFC height (m), EL pressure, EL height, source height, source
+ * theta-e (K); -999999 where undefined. */
+OC_EXPORT void SFX(oc_loopcape_diag_ml)(const real *p3d, const real *t3d, const real *td3d,
+                                        const real *ps, const real *ts, const real *tds,
+                                        real pinc, int source, real ml_depth, int adiabat, int nk,
+                                        int n2, real *cape, real *cin, int *mulvl, real *z_out,
+                                        int *status, real *diag, int nthreads) {
+  loopcape_ml_common(p3d, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, nk, n2, cape,
+                     cin, mulvl, z_out, 0, 0, status, 0, diag, nthreads);
+}
+
 /* loopcape_pl1d (CAPE_CODE_pressure_lev.f90:151-167) when p_stride == 0 and
  * loopcape_pl (:66-82) when p_stride == nk: column i uses levels
  * start(i)..nk of its profile. */
@@ -426,19 +518,22 @@ static void loopcape_pl_common(const real *p3d, long p_stride, const real *t3d, 
                                const real *ps, const real *ts, const real *tds, real pinc,
                                int source, real ml_depth, int adiabat, const int *start, int nk,
                                int n2, real *cape, real *cin, int *mulvl, real *z_out, int *nsub,
-                               int *niter, int *status, float *bmin, int nthreads) {
+                               int *niter, int *status, float *bmin, real *diag, int nthreads) {
   set_threads(nthreads);
   long i;
 #pragma omp parallel for schedule(dynamic, 64)
   for (i = 0; i < n2; ++i) {
     int st = start[i];
     if (bmin) bmin[i] = INFINITY;
+    if (diag)
+      for (int d = 0; d < 6; ++d) diag[6 * i + d] = LIT(-999999.);
     if (ts[i] > LIT(0.0) && st >= 1 && st <= nk) {
       int nk_pl_in = nk - st + 1;
       getcape(p3d + (size_t)i * p_stride + (st - 1), t3d + (size_t)i * nk + (st - 1),
               td3d + (size_t)i * nk + (st - 1), ps[i], ts[i], tds[i], pinc, source, ml_depth,
               adiabat, nk_pl_in, &cape[i], &cin[i], &mulvl[i], &z_out[i], nsub ? &nsub[i] : 0,
-              niter ? &niter[i] : 0, status ? &status[i] : 0, bmin ? &bmin[i] : 0);
+              niter ? &niter[i] : 0, status ? &status[i] : 0, bmin ? &bmin[i] : 0,
+              diag ? diag + 6 * i : 0);
     } else {
       cape[i] = LIT(0.0);
       cin[i] = LIT(0.0);
@@ -458,7 +553,18 @@ OC_EXPORT void SFX(oc_loopcape_pl1d)(const real *t3d, const real *td3d, const re
                                      real *z_out, int *nsub, int *niter, int *status,
                                      float *bmin, int nthreads) {
   loopcape_pl_common(p1d, 0, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, start, nk,
-                     n2, cape, cin, mulvl, z_out, nsub, niter, status, bmin, nthreads);
+                     n2, cape, cin, mulvl, z_out, nsub, niter, status, bmin, 0, nthreads);
+}
+
+/* loopcape_pl1d with the diagnostics (see oc_loopcape_diag_ml). */
+OC_EXPORT void SFX(oc_loopcape_diag_pl1d)(const real *t3d, const real *td3d, const real *p1d,
+                                          const real *ps, const real *ts, const real *tds,
+                                          real pinc, int source, real ml_depth, int adiabat,
+                                          const int *start, int nk, int n2, real *cape,
+                                          real *cin, int *mulvl, real *z_out, int *status,
+                                          real *diag, int nthreads) {
+  loopcape_pl_common(p1d, 0, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, start, nk,
+                     n2, cape, cin, mulvl, z_out, 0, 0, status, 0, diag, nthreads);
 }
 
 OC_EXPORT void SFX(oc_loopcape_pl)(const real *p3d, const real *t3d, const real *td3d,
@@ -468,7 +574,7 @@ OC_EXPORT void SFX(oc_loopcape_pl)(const real *p3d, const real *t3d, const real 
                                    int *nsub, int *niter, int *status, float *bmin,
                                    int nthreads) {
   loopcape_pl_common(p3d, nk, t3d, td3d, ps, ts, tds, pinc, source, ml_depth, adiabat, start, nk,
-                     n2, cape, cin, mulvl, z_out, nsub, niter, status, bmin, nthreads);
+                     n2, cape, cin, mulvl, z_out, nsub, niter, status, bmin, 0, nthreads);
 }
 
 /* ---------------------------------------------------------------------- */

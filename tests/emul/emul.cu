@@ -10,17 +10,17 @@
 
 using namespace xc;
 
-template <typename T, int GRID, int SOLVER>
-static void cape_loop_s(const CapeArgs &a, long long *counters) {
+template <typename T, int GRID, int SOLVER, bool DIAG>
+static void cape_loop_d(const CapeArgs &a, long long *counters) {
   const bool ice = a.adiabat >= 3, pseudo = (a.adiabat == 1 || a.adiabat == 3);
   long long s = 0, it = 0;
   for (long long i = 0; i < a.n2; ++i) {
     int nsub = 0, niter = 0;
     const float *w = a.guess_w;
-    if (ice && pseudo) cape_column_run<T, GRID, true, true, SOLVER>(a, i, nsub, niter, w);
-    else if (ice) cape_column_run<T, GRID, true, false, SOLVER>(a, i, nsub, niter, w);
-    else if (pseudo) cape_column_run<T, GRID, false, true, SOLVER>(a, i, nsub, niter, w);
-    else cape_column_run<T, GRID, false, false, SOLVER>(a, i, nsub, niter, w);
+    if (ice && pseudo) cape_column_run<T, GRID, true, true, SOLVER, DIAG>(a, i, nsub, niter, w);
+    else if (ice) cape_column_run<T, GRID, true, false, SOLVER, DIAG>(a, i, nsub, niter, w);
+    else if (pseudo) cape_column_run<T, GRID, false, true, SOLVER, DIAG>(a, i, nsub, niter, w);
+    else cape_column_run<T, GRID, false, false, SOLVER, DIAG>(a, i, nsub, niter, w);
     s += nsub;
     it += niter;
   }
@@ -28,6 +28,12 @@ static void cape_loop_s(const CapeArgs &a, long long *counters) {
     counters[0] += s;
     counters[1] += it;
   }
+}
+
+template <typename T, int GRID, int SOLVER>
+static void cape_loop_s(const CapeArgs &a, long long *counters) {
+  if (a.diag) cape_loop_d<T, GRID, SOLVER, true>(a, counters);
+  else cape_loop_d<T, GRID, SOLVER, false>(a, counters);
 }
 
 template <typename T, int GRID>
@@ -45,8 +51,9 @@ extern "C" int emu_cape(int grid, const void *p, const void *t, const void *td, 
                         const void *ts, const void *tds, int dtype, float pinc, int source,
                         float ml_depth, int adiabat, const int *start, int nk, long long n2,
                         float *cape, float *cin, int *mulvl, float *z_out, int *status,
-                        long long *counters, int guess, const float *guess_w) {
+                        long long *counters, int guess, const float *guess_w, float *diag) {
   CapeArgs a;
+  a.diag = diag;
   a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.ps = ps; a.ts = ts; a.tds = tds;
   a.start = grid == 1 ? nullptr : start; a.pinc = pinc; a.source = source; a.ml_depth = ml_depth;
   a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = guess; a.perm = nullptr; a.cape = cape; a.cin = cin;

@@ -25,7 +25,7 @@ ADIABATS = (1, 2, 3, 4)
 
 
 def _emu_cape(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0,
-              start=None, guess=0, guess_w=None):
+              start=None, guess=0, guess_w=None, diag=False):
     L = emul.lib()
     f64 = any(np.asarray(a).dtype == np.float64 for a in (p, t, td, ps, ts, tds))
     dt = np.float64 if f64 else np.float32
@@ -39,12 +39,15 @@ def _emu_cape(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth
                status=np.empty(n2, np.int32))
     cnt = np.zeros(2, np.int64)
     gw = None if guess_w is None else np.ascontiguousarray(guess_w, np.float32)
+    dg = np.zeros((n2, 6), np.float32) if diag else None
     L.emu_cape(grid, *[a.ctypes.data for a in arrs], int(f64), pinc, source, ml_depth, adiabat,
                None if st is None else st.ctypes.data, nk, n2, out["cape"].ctypes.data,
                out["cin"].ctypes.data, out["mulvl"].ctypes.data, out["z_out"].ctypes.data,
                out["status"].ctypes.data, cnt.ctypes.data, guess,
-               None if gw is None else gw.ctypes.data)
+               None if gw is None else gw.ctypes.data, dg.ctypes.data if dg is not None else None)
     out["counters"] = cnt
+    if dg is not None:
+        out.update({k: dg[:, j] for j, k in enumerate(O.DIAG_FIELDS)})
     return out
 
 
@@ -230,3 +233,29 @@ def test_emulated_fp32_srh_vs_fp64_oracle(soundings, depth):
             np.testing.assert_allclose(g, np.ravel(w), rtol=0, atol=0.05)
         for g, w in zip(got[2:], want[2:]):
             np.testing.assert_allclose(g, np.ravel(w), rtol=0, atol=1e-3)
+
+
+@pytest.mark.parametrize("adiabat", (1, 4))
+@pytest.mark.parametrize("source", SOURCES)
+def test_emulated_diagnostics_bit_exact(source, adiabat):
+    """The LFC/EL/source diagnostics of the column code (DIAG) against the
+    oracle's restatement of the same definitions, sigma and pressure grids."""
+    p, t, td, ps, ts, tds = S.sigma_c0(shape=(12, 24))
+    got = _emu_cape(1, p, t, td, ps, ts, tds, source, adiabat, diag=True)
+    nk = t.shape[-1]
+    want = O.loopcape_diag(np.reshape(p, (-1, nk)), np.reshape(t, (-1, nk)),
+                           np.reshape(td, (-1, nk)), ps, ts, tds, 500.0, source, 500.0, adiabat)
+    plev, t2, td2, ps2, ts2, tds2 = S.pressure_c1(shape=(16, 24))
+    got2 = _emu_cape(2, plev, t2, td2, ps2, ts2, tds2, source, adiabat, diag=True)
+    want2 = O.loopcape_diag(plev, np.reshape(t2, (-1, 37)), np.reshape(td2, (-1, 37)), ps2, ts2,
+                            tds2, 500.0, source, 500.0, adiabat,
+                            start=O.pres_lev_pos(plev, ps2.ravel()))
+    for g, w in ((got, want), (got2, want2)):
+        for k in ("cape", "cin", "mulvl", "z_out", "status") + O.DIAG_FIELDS:
+            np.testing.assert_array_equal(g[k], w[k], err_msg=k)
+        pos = g["cape"] > 0
+        assert pos.any()
+        # LFC below EL; undefined without positive area
+        assert np.all(g["plfc"][pos] >= g["pel"][pos])
+        assert np.all(g["zlfc"][pos] <= g["zel"][pos])
+        assert np.all(g["plfc"][g["cape"] == 0] == -999999)

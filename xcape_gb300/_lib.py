@@ -48,6 +48,8 @@ SIGNATURES = {
     "xc_loopcape_pl": [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i] + [_vp] * 5 + [_vp],
     "xc_loopcape_ex": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 6
     + [_vp, ctypes.c_size_t, _vp],
+    "xc_loopcape_diag": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 6
+    + [_vp],
     "xc_loopcape_ex_host": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 5
     + [_vp],
     "xc_loopcape_ex_noalloc": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i]

@@ -273,6 +273,67 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
     return tuple(res)
 
 
+DIAG_FIELDS = ("plfc", "zlfc", "pel", "zel", "zsource", "thetae_source")
+
+
+def calc_cape_diagnostics(p, t, td, ps, ts, tds, source="surface", ml_depth=500.0,
+                          adiabat="pseudo-liquid", pinc=500.0, vertical_lev="sigma",
+                          guess="plain"):
+    """calc_cape with the diagnostics the reference's getcape computes and
+    discards (CAPE_CODE_model_lev.f90:505, :511, :526), in one pass on the GPU.
+
+    Arguments as ``calc_cape`` (numpy arrays, or CUDA tensors used in place);
+    ``guess`` is ``'plain'`` or ``'learned'``.  Returns a dict of arrays shaped
+    like ``ps``: ``cape``, ``cin``, ``mulev``, ``zmulev`` (as calc_cape), and
+    ``plfc``, ``zlfc`` (level of free convection: the lowest point of the first
+    layer with positive area, hPa and m), ``pel``, ``zel`` (equilibrium level:
+    the highest positive-to-negative crossing, or the last level reached while
+    still buoyant), ``zsource`` and ``thetae_source`` (height and theta-e of the
+    lifted parcel's source).  -999999 where undefined.
+    """
+    src = _option(_SOURCE, source, "source")
+    adi = _option(_ADIABAT, adiabat, "adiabat")
+    vl = _option(_VERTICAL, vertical_lev, "vertical_lev")
+    gs = _option(_GUESS, guess, "guess")
+    if gs not in (_lib.XC_GUESS_PLAIN, _lib.XC_GUESS_LEARNED):
+        raise ValueError("calc_cape_diagnostics: guess must be 'plain' or 'learned'")
+    if gs == _lib.XC_GUESS_LEARNED:
+        from . import guess as _guess
+        _guess.ensure_loaded()
+    _check_same([t, td])
+    _check_same([ps, ts, tds])
+    shape = tuple(t.shape)
+    if len(p.shape) == 1 and vl == _lib.GRID_PRESSURE_1D:
+        grid = _lib.GRID_PRESSURE_1D
+        if p.shape[0] != shape[-1]:
+            raise ValueError("1-D p must have one value per level of t")
+    elif tuple(p.shape) == shape and vl == _lib.GRID_SIGMA:
+        grid = _lib.GRID_SIGMA
+    else:
+        raise ValueError("Input arrays must have the same shape.")
+    import torch
+    host = not any(_is_torch(a) for a in (p, t, td, ps, ts, tds))
+    if host:
+        p, t, td, ps, ts, tds = (torch.from_numpy(np.ascontiguousarray(a)).cuda()
+                                 for a in (p, t, td, ps, ts, tds))
+    b = _Batch([t, td], [ps, ts, tds], p, grid)
+    cape, cin, zout = (b.empty(b.n2, "f4") for _ in range(3))
+    mulvl = b.empty(b.n2, "i4")
+    diag = b.empty(6 * b.n2, "f4")
+    _lib.call("xc_loopcape_diag", grid, b.ptr(b.p), b.ptr(b.levels[0]), b.ptr(b.levels[1]),
+              b.ptr(b.surface[0]), b.ptr(b.surface[1]), b.ptr(b.surface[2]), b.dtype,
+              float(pinc), src, float(ml_depth), adi, None, b.nk, b.n2, gs, b.ptr(cape),
+              b.ptr(cin), b.ptr(mulvl), b.ptr(zout), None, b.ptr(diag), b.stream)
+    shp = _out_shape(shape)
+    out = {"cape": cape, "cin": cin, "mulev": mulvl, "zmulev": zout}
+    d = diag.reshape(b.n2, 6)
+    out.update({k: d[:, j] for j, k in enumerate(DIAG_FIELDS)})
+    out = {k: v.reshape(shp) for k, v in out.items()}
+    if host:
+        out = {k: v.cpu().numpy() for k, v in out.items()}
+    return out
+
+
 # ---------------------------------------------------------------------------
 # SRH
 

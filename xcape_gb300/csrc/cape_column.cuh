@@ -334,10 +334,27 @@ struct Acc {
 };
 
 // getcape on one assembled column of ncl levels (surface included).
-template <bool ICE, bool PSEUDO, int SOLVER, typename T, int GRID>
+// Diagnostics that getcape computes and discards (the crossing pressure ps
+// of :511 and :526, the parcel theta-e), written to dg[6] when DIAG:
+//   dg[0], dg[1]  LFC pressure (hPa) and height (m): the lowest point of the
+//                 first layer with positive area -- the neg->pos crossing, or
+//                 the layer's base when the parcel is already buoyant there;
+//   dg[2], dg[3]  EL pressure and height: the highest pos->neg crossing, or
+//                 the last level reached when the parcel is still buoyant;
+//   dg[4], dg[5]  height (m) and theta-e (K, getthe) of the source parcel.
+// All -999999 when the parcel never has positive area (LFC/EL), when the
+// ascent does not run or when the iteration gives up.
+constexpr float DIAG_MISSING = -999999.f;
+constexpr int DIAG_N = 6;
+
+template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
 XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
-                                  int source, float ml_depth, const float *guess_w = nullptr) {
+                                  int source, float ml_depth, const float *guess_w = nullptr,
+                                  float *dg = nullptr) {
   CapeResult r;
+  float d_plfc = DIAG_MISSING, d_zlfc = DIAG_MISSING, d_pel = DIAG_MISSING,
+        d_zel = DIAG_MISSING, d_zsrc = DIAG_MISSING, d_the = DIAG_MISSING;
+  bool have_lfc = false, ascended = false;
   r.mulvl = -999999;  // :252-253
   r.z_out = -999999.f;
   r.cape = 0.0f;
@@ -468,14 +485,26 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
     qt = qv2;
     if (SOLVER != SOLVE_PLAIN) ss.lnp = logf(p2);
   };
-  if (kmax == 1) init_parcel(prev);
+  auto source_diag = [&](const Env &e) {
+    if (DIAG) {
+      d_zsrc = z;
+      d_the = source == 3 ? getthe(p2, t2, dewpoint_of(p2, qv2), qv2) : getthe(e.p, e.t, e.td, e.q);
+    }
+  };
+  if (kmax == 1) {
+    init_parcel(prev);
+    source_diag(prev);
+  }
+  float p_last = 0.0f;
 
   for (int k = 2; k <= ncl; ++k) {
     const Env cur = col.env(k);
     const float dz = -CPDG * 0.5f * (cur.thv + prev.thv) * (cur.pi - prev.pi);
+    const float z_low = z;
     z = z + dz;
     if (k == kmax) {
       init_parcel(cur);
+      source_diag(cur);
     } else if (k > kmax) {
       const float b1 = b2;
       float dp = prev.p - cur.p;
@@ -512,6 +541,33 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
       // :501-503
       const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2 + ql2 + qi2);
       b2 = G * (thv2 - cur.thv) / cur.thv;
+      if (DIAG) {
+        ascended = true;
+        p_last = cur.p;
+        if ((b2 >= 0.0f) && (b1 < 0.0f)) {
+          const float w = (0.0f - b1) / (b2 - b1);
+          if (!have_lfc) {
+            d_plfc = (prev.p + (cur.p - prev.p) * w) / 100.0f;
+            d_zlfc = z_low + dz * w;
+            have_lfc = true;
+          }
+        } else if ((b2 < 0.0f) && (b1 > 0.0f)) {
+          const float w = (0.0f - b1) / (b2 - b1);
+          if (!have_lfc) {
+            d_plfc = prev.p / 100.0f;
+            d_zlfc = z_low;
+            have_lfc = true;
+          }
+          d_pel = (prev.p + (cur.p - prev.p) * w) / 100.0f;
+          d_zel = z_low + dz * w;
+        } else if (b2 >= 0.0f) {
+          if (!have_lfc) {
+            d_plfc = prev.p / 100.0f;
+            d_zlfc = z_low;
+            have_lfc = true;
+          }
+        }
+      }
       // :509-547
       float parea;
       if ((b2 >= 0.0f) && (b1 < 0.0f)) {
@@ -540,6 +596,18 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
   }
   r.cape = cape_acc.s;
   r.cin = cin_acc.s;
+  if (DIAG && ascended) {
+    if (have_lfc && b2 >= 0.0f) {
+      d_pel = p_last / 100.0f;
+      d_zel = r.z_out;
+    }
+    dg[0] = have_lfc ? d_plfc : DIAG_MISSING;
+    dg[1] = have_lfc ? d_zlfc : DIAG_MISSING;
+    dg[2] = have_lfc ? d_pel : DIAG_MISSING;
+    dg[3] = have_lfc ? d_zel : DIAG_MISSING;
+    dg[4] = d_zsrc;
+    dg[5] = d_the;
+  }
   return r;
 }
 
@@ -547,9 +615,13 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
 // One column of loopcape_ml / loopcape_pl1d / loopcape_pl
 // (CAPE_CODE_model_lev.f90:76-89, CAPE_CODE_pressure_lev.f90:66-82, 151-167):
 // the ts > 0 gate, the start level, getcape, and the outputs of column i.
-template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
+template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN,
+          bool DIAG = false>
 XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter,
                            const float *guess_w = nullptr) {
+    float dg[DIAG_N];
+    if (DIAG)
+      for (int d = 0; d < DIAG_N; ++d) dg[d] = DIAG_MISSING;
     const long long stride = a.ld > 0 ? a.ld : a.nk;
     const T *tin = (const T *)a.t + i * stride;
     const T *tdin = (const T *)a.td + i * stride;
@@ -579,7 +651,8 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
         col.base = start - 3;
         const int ncl = a.nk - start + 2;
         CapeResult r =
-            getcape_col<ICE, PSEUDO, SOLVER>(col, ncl, a.pinc, a.source, a.ml_depth, guess_w);
+            getcape_col<ICE, PSEUDO, SOLVER, DIAG>(col, ncl, a.pinc, a.source, a.ml_depth, guess_w,
+                                                   dg);
         cape = r.cape;
         cin = r.cin;
         zo = r.z_out;
@@ -594,6 +667,8 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
     a.mulvl[i] = mulvl;
     a.z_out[i] = zo;
     if (a.status) a.status[i] = status;
+    if (DIAG)
+      for (int d = 0; d < DIAG_N; ++d) a.diag[DIAG_N * i + d] = dg[d];
 }
 
 }  // namespace xc

@@ -201,6 +201,58 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   return XC_OK;
 }
 
+int xc_loopcape_diag(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                     const void *ts, const void *tds, int dtype, float pinc, int source,
+                     float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
+                     float *cape, float *cin, int *mulvl, float *z_out, int *status, float *diag,
+                     void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  rc = check_cape_opts(pinc, source, ml_depth, adiabat);
+  if (rc) return rc;
+  if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1, 2 or 3");
+  if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
+  if (guess != XC_GUESS_PLAIN && guess != XC_GUESS_LEARNED)
+    return fail(XC_ERR_INVALID, "xc_loopcape_diag: guess must be XC_GUESS_PLAIN or _LEARNED");
+  const float *guess_w = nullptr;
+  if (guess == XC_GUESS_LEARNED) {
+    rc = guess_weights(&guess_w);
+    if (rc) return rc;
+  }
+  if (n2 == 0) return XC_OK;
+  if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out || !diag)
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  xc::CapeArgs a;
+  a.grid = grid;
+  a.dtype = dtype;
+  a.p = p;
+  a.t = t3d;
+  a.td = td3d;
+  a.ps = ps;
+  a.ts = ts;
+  a.tds = tds;
+  a.start = grid == 1 ? nullptr : start_3d;
+  a.pinc = pinc;
+  a.source = source;
+  a.ml_depth = ml_depth;
+  a.adiabat = adiabat;
+  a.nk = nk;
+  a.n2 = n2;
+  a.guess = guess;
+  a.cape = cape;
+  a.cin = cin;
+  a.mulvl = mulvl;
+  a.z_out = z_out;
+  a.status = status;
+  a.counters = nullptr;
+  a.perm = nullptr;
+  a.guess_w = guess_w;
+  a.diag = diag;
+  const cudaError_t e = xc::launch_cape_diag(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cape diagnostics kernel launch");
+  return XC_OK;
+}
+
 int xc_loopcape_ml(const void *p3d, const void *t3d, const void *td3d, const void *ps,
                    const void *ts, const void *tds, int dtype, float pinc, int source,
                    float ml_depth, int adiabat, int nk, int n2, float *cape, float *cin,

@@ -24,6 +24,7 @@ struct CapeArgs {
   long long *counters;     // nullable: [0] += sub-steps, [1] += iterations
   const int *perm;         // nullable: thread t computes column perm[t]
   const float *guess_w;    // guess network parameters (device), guess == XC_GUESS_LEARNED
+  float *diag = nullptr;   // nullable: [n2][6] diagnostics (cape_column.cuh, getcape_col)
 };
 
 // Guess network (guess_mlp.cu).
@@ -39,6 +40,7 @@ cudaError_t launch_guess_eval(const float *w, const float *feats, long long n, f
                               cudaStream_t s);
 
 cudaError_t launch_cape(const CapeArgs &a, cudaStream_t s);
+cudaError_t launch_cape_diag(const CapeArgs &a, cudaStream_t s);  // cape_diag.cu
 
 // Column ordering (cape_kernel.cu): a counting sort of the columns by
 // (start level, surface dewpoint) so that the 32 columns of a warp need
