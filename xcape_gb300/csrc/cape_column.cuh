@@ -133,11 +133,15 @@ struct SolverState {
 // from the temperature and dewpoint, the LCL pressure along the dry
 // adiabat, the features (p_lcl, theta-e, q).  Returns false when the
 // output is out of the network's range.
-XC_HD bool parcel_lcl_slope(const float *w, float p, float t, float td, float q, float &y) {
+XC_HD void lcl_features(float p, float t, float td, float q, float &f0, float &f1, float &f2) {
   const float tlcl = 56.0f + 1.0f / (1.0f / (td - 56.0f) + logf(t / td) / 800.0f);
   const float plcl = td < t ? p * powf(tlcl / t, 1.0f / RDDCP) : p;
-  float f0, f1, f2;
   guess_features(plcl, getthe(p, t, td, q), q, f0, f1, f2);
+}
+
+XC_HD bool parcel_lcl_slope(const float *w, float p, float t, float td, float q, float &y) {
+  float f0, f1, f2;
+  lcl_features(p, t, td, q, f0, f1, f2);
   y = guess_eval_packed(w, f0, f1, f2);
   return y >= GUESS_Y_MIN && y <= GUESS_Y_MAX;
 }
@@ -347,22 +351,22 @@ struct Acc {
 constexpr float DIAG_MISSING = -999999.f;
 constexpr int DIAG_N = 6;
 
-template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
-XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
-                                  int source, float ml_depth, const float *guess_w = nullptr,
-                                  float *dg = nullptr) {
-  CapeResult r;
-  float d_plfc = DIAG_MISSING, d_zlfc = DIAG_MISSING, d_pel = DIAG_MISSING,
-        d_zel = DIAG_MISSING, d_zsrc = DIAG_MISSING, d_the = DIAG_MISSING;
-  bool have_lfc = false, ascended = false;
-  r.mulvl = -999999;  // :252-253
-  r.z_out = -999999.f;
-  r.cape = 0.0f;
-  r.cin = 0.0f;
-  r.status = 0;
-  r.nsub = 0;
-  r.niter = 0;
+// The lifted parcel's source (:252-352): its level kmax, the mixed-layer
+// means (FP64 accumulation, :183), the most-unstable level (mulvl,
+// -999999 otherwise) and whether the ascent runs at all.
+struct SourceSel {
+  int kmax;
+  int mulvl;
+  double avgth, avgqv;
+  bool ascend;
+};
 
+template <typename T, int GRID>
+XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int source,
+                              float ml_depth) {
+  SourceSel sel;
+  sel.mulvl = -999999;  // :252-253
+  sel.ascend = true;
   int kmax = 1;
   double avgth = 0.0, avgqv = 0.0;
 
@@ -381,7 +385,7 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
           const float q = getqvs(p, td);
           const float the = getthe(p, t, td, q);
           if (the > maxthe) {
-            r.mulvl = j;
+            sel.mulvl = j;
             maxthe = the;
             kmax = j;
           }
@@ -433,13 +437,59 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
       // Top-most level inside the mixed layer: the ascent starts at the top
       // and never runs (k < nk fails), so cape = cin = 0 and the sentinels
       // stay.
-      return r;
+      sel.ascend = false;
     } else {
       avgth = acc_th / (double)ml_depth;
       avgqv = acc_qv / (double)ml_depth;
       kmax = 1;
     }
   }
+  sel.kmax = kmax;
+  sel.avgth = avgth;
+  sel.avgqv = avgqv;
+  return sel;
+}
+
+// The source parcel's state (p, t, td in Pa and K, mixing ratio q): the
+// environment at kmax, or the mixed-layer means at the surface with the
+// dewpoint of the mean mixing ratio.
+template <typename T, int GRID>
+XC_HD void source_parcel(const ColumnReader<T, GRID> &col, const SourceSel &sel, int source,
+                         float &p, float &t, float &td, float &q) {
+  const Env es = col.env(sel.kmax);
+  p = es.p;
+  if (source == 3) {
+    q = (float)sel.avgqv;
+    t = (float)sel.avgth * es.pi;
+    td = dewpoint_of(es.p, q);
+  } else {
+    q = es.q;
+    t = es.t;
+    td = es.td;
+  }
+}
+
+// The ascent (:355-559) from a selected source.  SOLVE_LEARNED takes the
+// guess network's output at the parcel's LCL from `net_y` when guess_w is
+// null (the CAPE kernel evaluates it for a whole warp on the tensor cores),
+// and evaluates it here otherwise; a non-finite net_y means none.
+template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
+XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pinc, int source,
+                            const SourceSel &sel, const float *guess_w, float *dg,
+                            float net_y) {
+  CapeResult r;
+  float d_plfc = DIAG_MISSING, d_zlfc = DIAG_MISSING, d_pel = DIAG_MISSING,
+        d_zel = DIAG_MISSING, d_zsrc = DIAG_MISSING, d_the = DIAG_MISSING;
+  bool have_lfc = false, ascended = false;
+  r.mulvl = sel.mulvl;
+  r.z_out = -999999.f;
+  r.cape = 0.0f;
+  r.cin = 0.0f;
+  r.status = 0;
+  r.nsub = 0;
+  r.niter = 0;
+  const int kmax = sel.kmax;
+  const double avgth = sel.avgth, avgqv = sel.avgqv;
 
   // Ascent (:355-559).  Levels below kmax only integrate z.
   Env prev = col.env(1);
@@ -450,19 +500,15 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
   SolverState ss;
   ss.guess_w = guess_w;
   if (SOLVER == SOLVE_LEARNED) {
-    // the parcel that init_parcel will start at level kmax
-    const Env es = col.env(kmax);
-    float t0, td0, q0;
-    if (source == 3) {
-      q0 = (float)avgqv;
-      t0 = (float)avgth * es.pi;
-      td0 = dewpoint_of(es.p, q0);
+    if (guess_w) {
+      // the parcel that init_parcel will start at level kmax
+      float p0, t0, td0, q0;
+      source_parcel(col, sel, source, p0, t0, td0, q0);
+      ss.have_lcl = parcel_lcl_slope(guess_w, p0, t0, td0, q0, ss.lcl_y);
     } else {
-      q0 = es.q;
-      t0 = es.t;
-      td0 = es.td;
+      ss.lcl_y = net_y;
+      ss.have_lcl = net_y >= GUESS_Y_MIN && net_y <= GUESS_Y_MAX;
     }
-    ss.have_lcl = parcel_lcl_slope(guess_w, es.p, t0, td0, q0, ss.lcl_y);
   }
   Acc<SOLVER != SOLVE_PLAIN> cape_acc, cin_acc;
   auto init_parcel = [&](const Env &e) {
@@ -609,6 +655,25 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
     dg[5] = d_the;
   }
   return r;
+}
+
+template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
+XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
+                                  int source, float ml_depth, const float *guess_w = nullptr,
+                                  float *dg = nullptr) {
+  const SourceSel sel = select_source(col, ncl, source, ml_depth);
+  if (!sel.ascend) {
+    CapeResult r;
+    r.mulvl = sel.mulvl;
+    r.z_out = -999999.f;
+    r.cape = 0.0f;
+    r.cin = 0.0f;
+    r.status = 0;
+    r.nsub = 0;
+    r.niter = 0;
+    return r;
+  }
+  return ascend_col<ICE, PSEUDO, SOLVER, DIAG>(col, ncl, pinc, source, sel, guess_w, dg, 0.0f);
 }
 
 

@@ -1,21 +1,18 @@
 // cape_kernel.cu -- CAPE/CIN kernels for sm_103a: one thread per column,
 // running getcape_col (cape_column.cuh).
+#include <cuda_bf16.h>
+#include <stddef.h>
+#include <stdint.h>
+
 #include "cape_column.cuh"
 #include "xc_kernels.h"
 
 namespace xc {
 
-// The learned solver is capped at 64 registers (8 resident blocks of 128
-// threads per SM, as the others reach by themselves): measured 5 % faster
-// than its natural 78 registers at 6 blocks; the others are not capped (the
-// extrapolated one measured 1 % slower capped).
-template <int SOLVER>
-struct CapeMinBlocks {
-  static constexpr int value = SOLVER == SOLVE_LEARNED ? 8 : 1;
-};
-
+// One thread per column.  The learned solver runs in cape_learned_kernel
+// (below), which evaluates its guess network per warp on the tensor cores.
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER>
-__global__ void __launch_bounds__(128, CapeMinBlocks<SOLVER>::value) cape_kernel(CapeArgs a) {
+__global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
   extern __shared__ __align__(16) float guess_sm[];  // packed guess network, SOLVE_LEARNED*
   const float *gw = nullptr;
   if (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) {
@@ -39,6 +36,220 @@ __global__ void __launch_bounds__(128, CapeMinBlocks<SOLVER>::value) cape_kernel
     }
     if ((threadIdx.x & 31) == 0) {
       atomicAdd((unsigned long long *)&a.counters[0], (unsigned long long)s);
+      atomicAdd((unsigned long long *)&a.counters[1], (unsigned long long)it);
+    }
+  }
+}
+
+// ---- the learned solver: the guess network on the tensor cores, per warp ----
+//
+// cape_learned_kernel (6 resident blocks of 128 threads per SM: 80 registers,
+// 26 KB of shared memory; measured faster than 8 blocks at 64 registers with
+// spills, and than 91 registers uncapped) runs each column in three phases: (1) every lane selects
+// its parcel's source and forms the network's inputs at the parcel's LCL;
+// (2) the warp, converged (__syncwarp), evaluates the network for its 32
+// columns at once -- the 64x64 hidden layer as 2 x 8 x 4 mma.sync.m16n8k16
+// (BF16 operands, FP32 accumulation, as in training); (3) every lane runs
+// the ascent with that output (ascend_col).  No lane leaves before phase 2:
+// lanes without a column (past n2, ts <= 0, bad start, no ascent) take part
+// with zero inputs and discard the result.
+struct WarpNetSmem {
+  float4 l1[GUESS_H];                               // {W1[k][0..2], b1[k]}
+  float b2[GUESS_H], w3[GUESS_H], b3;
+  alignas(16) uint32_t w2[GUESS_H * GUESS_H / 2];   // W2 as bf16 pairs, swizzled rows
+  alignas(16) uint32_t h[4][32 * GUESS_H / 2];      // per warp: H1 rows as bf16 pairs
+  float y[4][32];
+};
+// the H1 rows are written 16 bytes at a time
+static_assert(offsetof(WarpNetSmem, h) % 16 == 0, "H1 tile must be 16-byte aligned");
+static_assert((32 * GUESS_H / 2 * sizeof(uint32_t)) % 16 == 0, "H1 tile rows");
+
+// 32-bit word w (a bf16 pair) of 64-wide row r, XOR-swizzled so that the
+// fragment loads of 8 consecutive rows hit 8 different bank groups.
+__device__ __forceinline__ int swz(int r, int w) { return r * 32 + (w ^ ((r & 7) << 2)); }
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ void load_warp_net(WarpNetSmem &s, const float *w) {
+  for (int k = threadIdx.x; k < GUESS_H; k += blockDim.x) {
+    s.l1[k] = make_float4(w[GUESS_OFF_W1 + 3 * k], w[GUESS_OFF_W1 + 3 * k + 1],
+                          w[GUESS_OFF_W1 + 3 * k + 2], w[GUESS_OFF_B1 + k]);
+    s.b2[k] = w[GUESS_OFF_B2 + k];
+    s.w3[k] = w[GUESS_OFF_W3 + k];
+  }
+  if (threadIdx.x == 0) s.b3 = w[GUESS_OFF_B3];
+  for (int e = threadIdx.x; e < GUESS_H * GUESS_H / 2; e += blockDim.x) {
+    const int n = e / (GUESS_H / 2), wd = e % (GUESS_H / 2);
+    s.w2[swz(n, wd)] = bf16x2(w[GUESS_OFF_W2 + n * GUESS_H + 2 * wd],
+                              w[GUESS_OFF_W2 + n * GUESS_H + 2 * wd + 1]);
+  }
+}
+
+// The network's output for the calling lane's inputs; all 32 lanes of the
+// warp must call it together.
+__device__ float warp_guess_eval(WarpNetSmem &s, float f0, float f1, float f2) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *H = s.h[warp];
+  // layer 1 (FP32), the lane's row of H1 as bf16 pairs, four words per store
+  for (int w4 = 0; w4 < GUESS_H / 2; w4 += 4) {
+    uint4 v;
+    uint32_t *pv = reinterpret_cast<uint32_t *>(&v);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float4 la = s.l1[2 * (w4 + u)], lb = s.l1[2 * (w4 + u) + 1];
+      float ha = la.w + la.x * f0 + la.y * f1 + la.z * f2;
+      float hb = lb.w + lb.x * f0 + lb.y * f1 + lb.z * f2;
+      pv[u] = bf16x2(ha > 0.0f ? ha : 0.0f, hb > 0.0f ? hb : 0.0f);
+    }
+    *reinterpret_cast<uint4 *>(&H[swz(lane, w4)]) = v;
+  }
+  __syncwarp();
+  const int gid = lane >> 2, tig = lane & 3;
+  float yp[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // rows gid, gid + 8, 16 + gid, 24 + gid
+  for (int nt = 0; nt < GUESS_H / 8; ++nt) {
+    float acc[2][4] = {{0.0f, 0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f, 0.0f}};
+    const int n = nt * 8 + gid;
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const int wd = ks * 8 + tig;
+      const uint32_t b0 = s.w2[swz(n, wd)], b1 = s.w2[swz(n, wd + 4)];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        const int r = mt * 16 + gid;
+        const uint32_t a[4] = {H[swz(r, wd)], H[swz(r + 8, wd)], H[swz(r, wd + 4)],
+                               H[swz(r + 8, wd + 4)]};
+        mma16816(acc[mt], a, b0, b1);
+      }
+    }
+    const int c = nt * 8 + tig * 2;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      const float z0 = acc[mt][0] + s.b2[c], z1 = acc[mt][1] + s.b2[c + 1];
+      const float z2 = acc[mt][2] + s.b2[c], z3 = acc[mt][3] + s.b2[c + 1];
+      yp[2 * mt] += s.w3[c] * (z0 > 0.0f ? z0 : 0.0f) + s.w3[c + 1] * (z1 > 0.0f ? z1 : 0.0f);
+      yp[2 * mt + 1] += s.w3[c] * (z2 > 0.0f ? z2 : 0.0f) + s.w3[c + 1] * (z3 > 0.0f ? z3 : 0.0f);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    yp[j] += __shfl_xor_sync(0xffffffffu, yp[j], 1);
+    yp[j] += __shfl_xor_sync(0xffffffffu, yp[j], 2);
+  }
+  if (tig == 0) {
+    s.y[warp][gid] = yp[0] + s.b3;
+    s.y[warp][gid + 8] = yp[1] + s.b3;
+    s.y[warp][16 + gid] = yp[2] + s.b3;
+    s.y[warp][24 + gid] = yp[3] + s.b3;
+  }
+  __syncwarp();
+  const float y = s.y[warp][lane];
+  __syncwarp();  // the tile is rewritten by the warp's next call
+  return y;
+}
+
+template <typename T, int GRID, bool ICE, bool PSEUDO>
+__global__ void __launch_bounds__(128, 6) cape_learned_kernel(CapeArgs a) {
+  __shared__ WarpNetSmem net;
+  load_warp_net(net, a.guess_w);
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < a.n2;
+  const long long i = active ? (a.perm ? (long long)__ldg(a.perm + t) : t) : 0;
+  // phase 1: the column's start, gate and source (cape_column_run, getcape_col)
+  ColumnReader<T, GRID> col;
+  int ncl = 0, start = 1, status = 0;
+  bool run = false;
+  SourceSel sel;
+  sel.kmax = 1;
+  sel.mulvl = 0;
+  sel.avgth = sel.avgqv = 0.0;
+  sel.ascend = false;
+  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
+  if (active) {
+    const T *tin = (const T *)a.t + i * a.nk;
+    const T *tdin = (const T *)a.td + i * a.nk;
+    const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
+    const float ts = ldf((const T *)a.ts + i);
+    if (GRID != 1)
+      start = a.start ? __ldg(a.start + i)
+                      : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
+    if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
+      if (start < 1 || start > a.nk) {
+        status = COL_BADSTART;
+      } else {
+        col.p = pin;
+        col.t = tin;
+        col.td = tdin;
+        col.ps = ldf((const T *)a.ps + i);
+        col.ts = ts;
+        col.tds = ldf((const T *)a.tds + i);
+        col.base = start - 3;
+        ncl = a.nk - start + 2;
+        sel = select_source(col, ncl, a.source, a.ml_depth);
+        if (sel.ascend) {
+          float p0, t0, td0, q0;
+          source_parcel(col, sel, a.source, p0, t0, td0, q0);
+          lcl_features(p0, t0, td0, q0, f0, f1, f2);
+          run = true;
+        }
+      }
+    }
+  }
+  // phase 2: the network for the warp's 32 columns
+  __syncwarp();
+  const float y = warp_guess_eval(net, f0, f1, f2);
+  // phase 3: the ascent
+  float cape = 0.0f, cin = 0.0f, zo = 0.0f;
+  int mulvl = 0, nsub = 0, niter = 0;
+  if (active && status == 0 && ldf((const T *)a.ts + i) > 0.0f) {
+    CapeResult r;
+    if (run) {
+      r = ascend_col<ICE, PSEUDO, SOLVE_LEARNED, false>(col, ncl, a.pinc, a.source, sel, nullptr,
+                                                        nullptr, y);
+    } else {
+      r.mulvl = sel.mulvl;
+      r.z_out = -999999.f;
+      r.cape = 0.0f;
+      r.cin = 0.0f;
+      r.status = 0;
+      r.nsub = 0;
+      r.niter = 0;
+    }
+    cape = r.cape;
+    cin = r.cin;
+    zo = r.z_out;
+    mulvl = r.mulvl;
+    status = r.status;
+    nsub = r.nsub;
+    niter = r.niter;
+  }
+  if (active) {
+    a.cape[i] = cape;
+    a.cin[i] = cin;
+    a.mulvl[i] = mulvl;
+    a.z_out[i] = zo;
+    if (a.status) a.status[i] = status;
+  }
+  if (a.counters) {
+    long long sb = nsub, it = niter;
+    for (int o = 16; o > 0; o >>= 1) {
+      sb += __shfl_down_sync(0xffffffffu, sb, o);
+      it += __shfl_down_sync(0xffffffffu, it, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd((unsigned long long *)&a.counters[0], (unsigned long long)sb);
       atomicAdd((unsigned long long *)&a.counters[1], (unsigned long long)it);
     }
   }
@@ -187,6 +398,16 @@ static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaS
     cape_kernel<T, GRID, false, false, SOLVER><<<blocks, threads, sm, s>>>(a);
 }
 
+template <typename T, int GRID>
+static void launch_learned(const CapeArgs &a, unsigned blocks, int threads, cudaStream_t s) {
+  const bool ice = a.adiabat >= 3;
+  const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
+  if (ice && pseudo) cape_learned_kernel<T, GRID, true, true><<<blocks, threads, 0, s>>>(a);
+  else if (ice) cape_learned_kernel<T, GRID, true, false><<<blocks, threads, 0, s>>>(a);
+  else if (pseudo) cape_learned_kernel<T, GRID, false, true><<<blocks, threads, 0, s>>>(a);
+  else cape_learned_kernel<T, GRID, false, false><<<blocks, threads, 0, s>>>(a);
+}
+
 // guess codes (include/xcape_gb300.h): 0 plain, 1 learned, 2 extrapolated,
 // 3 plain first guess with secant steps, 4 the network on every saturated
 // sub-step.
@@ -197,7 +418,7 @@ static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
   if (blocks == 0) return cudaSuccess;
   switch (a.guess) {
     case 0: launch_cape_s<T, GRID, SOLVE_PLAIN>(a, blocks, threads, s); break;
-    case 1: launch_cape_s<T, GRID, SOLVE_LEARNED>(a, blocks, threads, s); break;
+    case 1: launch_learned<T, GRID>(a, blocks, threads, s); break;
     case 2: launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s); break;
     case 3: launch_cape_s<T, GRID, SOLVE_SECANT>(a, blocks, threads, s); break;
     default: launch_cape_s<T, GRID, SOLVE_LEARNED_ALL>(a, blocks, threads, s); break;
