@@ -43,9 +43,11 @@ __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
 
 // ---- the learned solver: the guess network on the tensor cores, per warp ----
 //
-// cape_learned_kernel (6 resident blocks of 128 threads per SM: 80 registers,
-// 26 KB of shared memory; measured faster than 8 blocks at 64 registers with
-// spills, and than 91 registers uncapped) runs each column in three phases: (1) every lane selects
+// cape_learned_kernel (7 resident blocks of 128 threads per SM: 72 registers,
+// 26 KB of shared memory; measured on a 262k-column slice at 0.820 ms against
+// 0.839 ms with 6 blocks (80 registers), 0.894 ms with 8 (64 registers,
+// spills) and 0.854 ms uncapped (91 registers)) runs each column in three
+// phases: (1) every lane selects
 // its parcel's source and forms the network's inputs at the parcel's LCL;
 // (2) the warp, converged (__syncwarp), evaluates the network for its 32
 // columns at once -- the 64x64 hidden layer as 2 x 8 x 4 mma.sync.m16n8k16
@@ -160,7 +162,7 @@ __device__ float warp_guess_eval(WarpNetSmem &s, float f0, float f1, float f2) {
 }
 
 template <typename T, int GRID, bool ICE, bool PSEUDO>
-__global__ void __launch_bounds__(128, 6) cape_learned_kernel(CapeArgs a) {
+__global__ void __launch_bounds__(128, 7) cape_learned_kernel(CapeArgs a) {
   __shared__ WarpNetSmem net;
   load_warp_net(net, a.guess_w);
   __syncthreads();
