@@ -58,6 +58,8 @@ extern "C" {
 /* Per-column status bits (optional `status` output). */
 #define XC_COL_NOCONV 1   /* moist-adiabat iteration passed 100 steps: cape=cin=0 */
 #define XC_COL_BADSTART 2 /* start_3d outside 1..nk: outputs zero              */
+#define XC_COL_TOOMANYSTEPS 4 /* the ascent would take more than 2^22 sub-steps, or
+                                 a pressure step is not finite: cape = cin = 0   */
 
 /* Moist-adiabat solver of xc_loopcape_ex (`guess` argument).
  * XC_GUESS_PLAIN is the reference's iteration: first guess thlast = th1,

@@ -293,3 +293,47 @@ def test_cape_full_size_pressure_workload():
     compare_cape({k: v[idx] for k, v in a.items()}, want, what="full-size sample")
     assert np.all(a["cape"] >= 0) and np.all(a["cin"] >= 0)
     del torch
+
+
+def test_nonfinite_inputs_match_oracle():
+    """NaN and infinite inputs on the GPU: every launch ends, NaN appears
+    where the oracle's NaN is, finite results agree, and the only columns
+    flagged too-many-sub-steps (bit 4, zero outputs) are ones with a NaN
+    pressure, whose sub-step count the reference leaves undefined."""
+    from cases import with_nonfinite
+    p, t, td, ps, ts, tds = with_nonfinite()
+    for source in ("surface", "most-unstable", "mixed-layer"):
+        got = cape_device(1, p, t, td, ps, ts, tds, source, "pseudo-liquid")
+        n2 = ps.size
+        want = O.loopcape(p.reshape(n2, -1), t.reshape(n2, -1), td.reshape(n2, -1), ps.ravel(),
+                          ts.ravel(), tds.ravel(), 500.0, SOURCES[source], 500.0, 1, stats=True)
+        flagged = (got["status"] & 4) != 0
+        nan_p = np.isnan(p.reshape(n2, -1)).any(axis=1) | np.isnan(ps.ravel())
+        assert np.all(nan_p[flagged])
+        keep = ~flagged & ((want["status"] & 1) == 0) & ((got["status"] & 1) == 0)
+        for k in ("cape", "cin"):
+            g, w = got[k][keep], want[k][keep]
+            assert np.array_equal(np.isnan(g), np.isnan(w)), k
+            fin = ~np.isnan(w)
+            assert np.all(np.abs(g[fin].astype(np.float64) - w[fin]) <=
+                          np.maximum(1.0, 1e-3 * np.abs(w[fin]))), k
+
+
+@pytest.mark.parametrize("guess", [0, 1])
+def test_tall_columns(guess):
+    """1,000 sigma levels per column (the 4,096-level limit's order of
+    magnitude; ~2,000 sub-steps per column): plain solver against the FP32
+    oracle, learned solver against FP64."""
+    from xcape_gb300 import guess as G
+    if guess == 1:
+        G.ensure_loaded()
+    p, t, td, ps, ts, tds = S.sigma_c0(shape=(4, 64), nlev=1000, seed=17, dtype=np.float32)
+    got = cape_device(1, p, t, td, ps, ts, tds, "surface", "pseudo-liquid", guess=guess)
+    n2 = ps.size
+    want = O.loopcape(p.reshape(n2, -1), t.reshape(n2, -1), td.reshape(n2, -1), ps.ravel(),
+                      ts.ravel(), tds.ravel(), 500.0, 1, 500.0, 1, stats=True,
+                      precision="f32" if guess == 0 else "f64")
+    ok = ((want["status"] & 1) == 0) & ((got["status"] & 1) == 0)
+    assert ok.mean() > 0.95
+    d = np.abs(got["cape"][ok].astype(np.float64) - want["cape"][ok])
+    assert np.all(d <= np.maximum(1.0, 1e-3 * want["cape"][ok])), d.max()

@@ -16,6 +16,8 @@ import pytest
 import oracle as O
 from xcape_gb300 import synthetic as S
 
+from cases import with_nonfinite
+
 emul = pytest.importorskip("emul")
 if emul.nvcc() is None:
     pytest.skip("nvcc not available", allow_module_level=True)
@@ -259,3 +261,23 @@ def test_emulated_diagnostics_bit_exact(source, adiabat):
         assert np.all(g["plfc"][pos] >= g["pel"][pos])
         assert np.all(g["zlfc"][pos] <= g["zel"][pos])
         assert np.all(g["plfc"][g["cape"] == 0] == -999999)
+
+
+@pytest.mark.parametrize("source", SOURCES)
+def test_emulated_nonfinite_inputs_bit_exact(source):
+    """NaN and infinite inputs: the column code ends (the iteration and
+    sub-step caps bound every loop) and reproduces the oracle bit for bit,
+    NaN for NaN -- except where a pressure is NaN.  There the sub-step count
+    1 + int(dp/pinc) (CAPE_CODE_model_lev.f90:410-415) converts NaN to an
+    integer, which Fortran and C leave undefined (x86 gives INT_MIN and
+    skips the sub-steps, aarch64 gives 0); the kernels flag such a column
+    (status bit 4, too many sub-steps) and return zero."""
+    p, t, td, ps, ts, tds = with_nonfinite()
+    got = _emu_cape(1, p, t, td, ps, ts, tds, source, 1)
+    want = _oracle(1, p, t, td, ps, ts, tds, source, 1)
+    nan_p = np.isnan(p.reshape(64, -1)).any(axis=1) | np.isnan(ps.ravel())
+    flagged = (got["status"] & 4) != 0
+    assert np.all(nan_p[flagged]) and flagged.any()
+    assert np.all(got["cape"][flagged] == 0) and np.all(got["cin"][flagged] == 0)
+    for k in ("cape", "cin", "mulvl", "z_out"):
+        np.testing.assert_array_equal(got[k][~flagged], want[k][~flagged], err_msg=k)
