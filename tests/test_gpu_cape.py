@@ -337,3 +337,19 @@ def test_tall_columns(guess):
     assert ok.mean() > 0.95
     d = np.abs(got["cape"][ok].astype(np.float64) - want["cape"][ok])
     assert np.all(d <= np.maximum(1.0, 1e-3 * want["cape"][ok])), d.max()
+
+
+@pytest.mark.parametrize("guess", ["plain", "learned"])
+def test_host_path_chunks_match_device_path(guess):
+    """numpy inputs go through the pipelined host entry point (chunks of
+    131,072+ columns alternating between two streams); the results equal
+    those of the device entry point on the same arrays, bit for bit."""
+    import torch
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(216, 1440))  # 311,040 columns: 3 chunks
+    host = X.calc_cape(plev, t, td, ps, ts, tds, source="most-unstable",
+                       vertical_lev="pressure", guess=guess)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (plev, t, td, ps, ts, tds)]
+    ref = X.calc_cape(*dev, source="most-unstable", vertical_lev="pressure", guess=guess)
+    torch.cuda.synchronize()
+    for h, d in zip(host, ref):
+        np.testing.assert_array_equal(h, d.cpu().numpy())

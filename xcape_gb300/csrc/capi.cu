@@ -56,6 +56,50 @@ struct Workspace {
 std::mutex g_ws_mu;
 std::vector<Workspace> g_ws;
 
+// Two non-blocking streams per device for the pipelined host paths (chunk
+// c + 1's copies overlap chunk c's kernels), and an event that chains them
+// to the caller's stream.  Created on first use, kept for the process.
+struct Pipeline {
+  cudaStream_t s[2] = {nullptr, nullptr};
+  cudaEvent_t start = nullptr;
+  cudaEvent_t done[2] = {nullptr, nullptr};  // a chunk's outputs are in the staging buffer
+  char *pinned = nullptr;                      // pinned output staging, grow-only
+  size_t pinned_cap = 0;
+};
+std::vector<Pipeline> g_pipe;
+
+int pipeline_get(Pipeline **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if ((int)g_pipe.size() <= dev) g_pipe.resize(dev + 1);
+  Pipeline &pl = g_pipe[dev];
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+    if (!pl.s[k]) e = cudaStreamCreateWithFlags(&pl.s[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !pl.done[k])
+      e = cudaEventCreateWithFlags(&pl.done[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess && !pl.start) e = cudaEventCreateWithFlags(&pl.start, cudaEventDisableTiming);
+  if (e != cudaSuccess) return cuda_fail(e, "creating the host-path streams");
+  *out = &pl;
+  return XC_OK;
+}
+
+int pipeline_pinned(Pipeline *pl, size_t bytes) {
+  if (pl->pinned_cap >= bytes) return XC_OK;
+  if (pl->pinned) cudaFreeHost(pl->pinned);
+  pl->pinned = nullptr;
+  pl->pinned_cap = 0;
+  const cudaError_t e = cudaMallocHost((void **)&pl->pinned, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(XC_ERR_NOMEM, "cudaMallocHost(%zu) for the host-path staging: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  pl->pinned_cap = bytes;
+  return XC_OK;
+}
+
 int ws_get(size_t bytes, void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -282,6 +326,11 @@ int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const voi
                         nullptr, nullptr, 0, stream);
 }
 
+// Columns per chunk of the pipelined host path: at least this many, at most
+// HOST_CHUNKS chunks.
+constexpr int HOST_CHUNK_MIN = 131072;
+constexpr int HOST_CHUNKS = 8;
+
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
                         const void *ps, const void *ts, const void *tds, int dtype, float pinc,
                         int source, float ml_depth, int adiabat, const int *start_3d, int nk,
@@ -294,53 +343,125 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1, 2 or 3");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
   if (n2 == 0) return XC_OK;
+  // The columns go through in chunks, alternating between two streams that
+  // each own a set of chunk buffers: the copies of one chunk overlap the
+  // kernels of the other.  Outputs come back into pinned staging (a copy
+  // into pageable memory would block this thread) and are moved into the
+  // caller's arrays while the GPU works on the later chunks.  Each column
+  // is still computed by one thread and written to its own index, so the
+  // chunking changes no result.
+  int nchunk = (n2 + HOST_CHUNK_MIN - 1) / HOST_CHUNK_MIN;
+  if (nchunk > HOST_CHUNKS) nchunk = HOST_CHUNKS;
+  const int C = ((n2 + nchunk - 1) / nchunk + 255) / 256 * 256;  // columns per chunk
   const size_t es = dtype == XC_F32 ? 4 : 8;
-  const size_t n3 = (size_t)n2 * nk;
-  const size_t p_bytes = (grid == 2 ? (size_t)nk : n3) * es;
+  const size_t c3 = (size_t)C * nk;
+  const bool has_start = grid != 1 && start_3d;
   std::lock_guard<std::mutex> lk(g_ws_mu);
+  Pipeline *pl = nullptr;
+  rc = pipeline_get(&pl);
+  if (rc) return rc;
+  const int nslot = nchunk > 1 ? 2 : 1;
+  struct Slot {
+    size_t p, t, td, ps, ts, tds, st, cape, cin, mu, z, stat, ord;
+  } sl[2];
+  const size_t ord_bytes = xc::order_workspace_bytes(C);
   Carver cv;
-  const size_t o_p = cv.take(p_bytes), o_t = cv.take(n3 * es), o_td = cv.take(n3 * es);
-  const size_t o_ps = cv.take(n2 * es), o_ts = cv.take(n2 * es), o_tds = cv.take(n2 * es);
-  const size_t o_st = (grid != 1 && start_3d) ? cv.take(n2 * 4) : 0;
-  const size_t o_cape = cv.take(n2 * 4), o_cin = cv.take(n2 * 4), o_mu = cv.take(n2 * 4),
-               o_z = cv.take(n2 * 4);
-  const size_t o_stat = status ? cv.take(n2 * 4) : 0;
-  const size_t ord_bytes = xc::order_workspace_bytes(n2);
-  const size_t o_ord = cv.take(ord_bytes);
+  for (int k = 0; k < nslot; ++k) {
+    sl[k].p = cv.take((grid == 2 ? (size_t)nk : c3) * es);
+    sl[k].t = cv.take(c3 * es);
+    sl[k].td = cv.take(c3 * es);
+    sl[k].ps = cv.take((size_t)C * es);
+    sl[k].ts = cv.take((size_t)C * es);
+    sl[k].tds = cv.take((size_t)C * es);
+    sl[k].st = has_start ? cv.take((size_t)C * 4) : 0;
+    sl[k].cape = cv.take((size_t)C * 4);
+    sl[k].cin = cv.take((size_t)C * 4);
+    sl[k].mu = cv.take((size_t)C * 4);
+    sl[k].z = cv.take((size_t)C * 4);
+    sl[k].stat = status ? cv.take((size_t)C * 4) : 0;
+    sl[k].ord = cv.take(ord_bytes);
+  }
   void *base = nullptr;
   rc = ws_get(cv.off, &base);
   if (rc) return rc;
   char *b = (char *)base;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaSuccess;
-#define H2D(off, src, bytes)                                                         \
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, s)
-  H2D(o_p, p, p_bytes);
-  H2D(o_t, t3d, n3 * es);
-  H2D(o_td, td3d, n3 * es);
-  H2D(o_ps, ps, n2 * es);
-  H2D(o_ts, ts, n2 * es);
-  H2D(o_tds, tds, n2 * es);
-  if (grid != 1 && start_3d) H2D(o_st, start_3d, n2 * 4);
-#undef H2D
-  if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
-  rc = xc_loopcape_ex(grid, b + o_p, b + o_t, b + o_td, b + o_ps, b + o_ts, b + o_tds, dtype, pinc,
-                      source, ml_depth, adiabat,
-                      (grid != 1 && start_3d) ? (const int *)(b + o_st) : nullptr, nk, n2, guess,
-                      (float *)(b + o_cape), (float *)(b + o_cin), (int *)(b + o_mu),
-                      (float *)(b + o_z), status ? (int *)(b + o_stat) : nullptr, nullptr,
-                      b + o_ord, ord_bytes, s);
+  const int nout = status ? 5 : 4;
+  const size_t slot_out = (size_t)nout * C * 4;
+  rc = pipeline_pinned(pl, slot_out * nslot);
   if (rc) return rc;
-#define D2H(dst, off, bytes)                                                         \
-  if (e == cudaSuccess) e = cudaMemcpyAsync((dst), b + (off), (bytes), cudaMemcpyDeviceToHost, s)
-  D2H(cape, o_cape, n2 * 4);
-  D2H(cin, o_cin, n2 * 4);
-  D2H(mulvl, o_mu, n2 * 4);
-  D2H(z_out, o_z, n2 * 4);
-  if (status) D2H(status, o_stat, n2 * 4);
+  // moves chunk c's outputs from its slot's staging into the caller's arrays
+  auto finish = [&](int c) -> int {
+    const int k = c % nslot;
+    const long long c0 = (long long)c * C;
+    const size_t nc = (size_t)((n2 - c0) < C ? (n2 - c0) : C);
+    const cudaError_t we = cudaEventSynchronize(pl->done[k]);
+    if (we != cudaSuccess) return cuda_fail(we, "device-to-host copy");
+    const char *h = pl->pinned + k * slot_out;
+    memcpy(cape + c0, h, nc * 4);
+    memcpy(cin + c0, h + (size_t)C * 4, nc * 4);
+    memcpy(mulvl + c0, h + (size_t)2 * C * 4, nc * 4);
+    memcpy(z_out + c0, h + (size_t)3 * C * 4, nc * 4);
+    if (status) memcpy(status + c0, h + (size_t)4 * C * 4, nc * 4);
+    return XC_OK;
+  };
+  cudaError_t e = cudaEventRecord(pl->start, (cudaStream_t)stream);
+  for (int k = 0; k < nslot && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(pl->s[k], pl->start, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "ordering the host path after the caller's stream");
+  const char *hp = (const char *)p, *ht = (const char *)t3d, *htd = (const char *)td3d;
+  const char *hps = (const char *)ps, *hts = (const char *)ts, *htds = (const char *)tds;
+  int issued = 0;
+  for (int c = 0; c < nchunk; ++c) {
+    const long long c0 = (long long)c * C;
+    if (c0 >= n2) break;
+    const int nc = (int)((n2 - c0) < C ? (n2 - c0) : C);
+    const int k = c % nslot;
+    if (c >= nslot) {  // the slot's staging still holds chunk c - nslot
+      rc = finish(c - nslot);
+      if (rc) return rc;
+    }
+    const Slot &q = sl[k];
+    cudaStream_t s = pl->s[k];
+    const size_t r3 = (size_t)nc * nk * es, off3 = (size_t)c0 * nk * es, off1 = (size_t)c0 * es;
+#define H2D(off, src, bytes)                                                         \
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, s)
+    if (grid == 2) {
+      H2D(q.p, hp, (size_t)nk * es);
+    } else {
+      H2D(q.p, hp + off3, r3);
+    }
+    H2D(q.t, ht + off3, r3);
+    H2D(q.td, htd + off3, r3);
+    H2D(q.ps, hps + off1, (size_t)nc * es);
+    H2D(q.ts, hts + off1, (size_t)nc * es);
+    H2D(q.tds, htds + off1, (size_t)nc * es);
+    if (has_start) H2D(q.st, start_3d + c0, (size_t)nc * 4);
+#undef H2D
+    if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
+    rc = xc_loopcape_ex(grid, b + q.p, b + q.t, b + q.td, b + q.ps, b + q.ts, b + q.tds, dtype,
+                        pinc, source, ml_depth, adiabat, has_start ? (const int *)(b + q.st) : nullptr,
+                        nk, nc, guess, (float *)(b + q.cape), (float *)(b + q.cin),
+                        (int *)(b + q.mu), (float *)(b + q.z),
+                        status ? (int *)(b + q.stat) : nullptr, nullptr, b + q.ord, ord_bytes, s);
+    if (rc) return rc;
+    char *h = pl->pinned + k * slot_out;
+#define D2H(j, off)                                                                  \
+    if (e == cudaSuccess)                                                            \
+      e = cudaMemcpyAsync(h + (size_t)(j) * C * 4, b + (off), (size_t)nc * 4,        \
+                          cudaMemcpyDeviceToHost, s)
+    D2H(0, q.cape);
+    D2H(1, q.cin);
+    D2H(2, q.mu);
+    D2H(3, q.z);
+    if (status) D2H(4, q.stat);
 #undef D2H
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_fail(e, "device-to-host copy");
+    if (e == cudaSuccess) e = cudaEventRecord(pl->done[k], s);
+    if (e != cudaSuccess) return cuda_fail(e, "device-to-host copy");
+    issued = c + 1;
+  }
+  for (int c = issued - nslot < 0 ? 0 : issued - nslot; c < issued; ++c) {
+    rc = finish(c);
+    if (rc) return rc;
+  }
   return XC_OK;
 }
 
