@@ -360,6 +360,10 @@ def run_ours(args):
     sb_ms = {args.guess: time_source(1, scratch)}
     if compare:
         sb_ms["plain"] = time_source(1, scratch, _lib.XC_GUESS_PLAIN)
+    # every rank times its own shard: the job's time is the slowest rank's
+    per_src_ms = {k: max_over_ranks(dist, v, dev) for k, v in per_src_ms.items()}
+    plain_ms = {k: max_over_ranks(dist, v, dev) for k, v in plain_ms.items()}
+    sb_ms = {k: max_over_ranks(dist, v, dev) for k, v in sb_ms.items()}
 
     # end to end through the public API from pinned host memory
     import xcape_gb300 as X
