@@ -65,6 +65,12 @@ struct ColumnReader {
     level(j, a, b, c);
     return make_env(a, b, c);
   }
+  // level j >= 2 (above the surface): loops over those levels then need no
+  // surface values, which frees their registers
+  XC_HD Env env_above(int j) const {
+    const int m = base + j;
+    return make_env(ldf(p + m), ldf(t + m), ldf(td + m));
+  }
 };
 
 struct CapeResult {
@@ -92,7 +98,8 @@ struct CapeResult {
 //                saturated, where the extrapolation has only the partial
 //                increment of the sub-step that crossed saturation: there
 //                the first guess is th1 plus the guess network's increment
-//                (guess_mlp.cuh).  The network is evaluated once per column,
+//                (guess_mlp.cuh), entered as the extrapolation history when
+//                the parcel saturates.  The network is evaluated once per column,
 //                before the ascent, at the parcel's lifting condensation
 //                level (parcel_lcl_slope), where every thread of a warp
 //                evaluates it together; inside the sub-step loop the
@@ -120,10 +127,10 @@ struct SolverState {
   float slope = 0.0f;     // last difference quotient of F (the map's slope)
   bool have_prev = false;
   bool have_slope = false;
-  bool saturated = false;   // condensate present at the end of the previous sub-step
-  bool sat_start = false;   // the previous sub-step started saturated
-  bool have_lcl = false;    // lcl_y holds the network's output at the parcel's LCL
-  float lcl_y = 0.0f;
+  bool saturated = false;   // (SOLVE_LEARNED_ALL) condensate at the end of the last sub-step
+  // (SOLVE_LEARNED) the network's output at the parcel's LCL until the
+  // parcel first saturates, NaN once used or when there is none
+  float lcl_y = NAN;
   float lnp = 0.0f;         // ln of the parcel pressure (accelerated modes)
   const float *guess_w = nullptr;  // packed guess network (guess_packed_value), SOLVE_LEARNED*
 };
@@ -193,9 +200,7 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   float x_prev = 0.0f, f_prev = 0.0f;
   constexpr bool EXTRAP = SOLVER == SOLVE_ACCEL || SOLVER == SOLVE_LEARNED;
   float dth_net;
-  if (SOLVER == SOLVE_LEARNED && ss.saturated && !ss.sat_start && ss.have_lcl) {
-    thlast = th1 - GUESS_SLOPE_SCALE * ss.lcl_y * lp;
-  } else if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
+  if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
              network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net)) {
     thlast = th1 + dth_net;
   } else if (EXTRAP && ss.have_prev) {
@@ -280,10 +285,13 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     ss.dp_prev = dp;
     ss.have_prev = true;
   }
-  if (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) {
-    ss.sat_start = ss.saturated;
-    ss.saturated = ql2 + qi2 > 0.0f;
+  if (SOLVER == SOLVE_LEARNED && ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y) {
+    // the parcel has just saturated: the increment extrapolated into the
+    // next sub-step is the network's, not this sub-step's partial one
+    ss.dth_prev = -GUESS_SLOPE_SCALE * ss.lcl_y * lp;
+    ss.lcl_y = NAN;
   }
+  if (SOLVER == SOLVE_LEARNED_ALL) ss.saturated = ql2 + qi2 > 0.0f;
   if (PSEUDO) {  // :487-491
     qt = qv2;
     ql2 = 0.0f;
@@ -403,7 +411,7 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
     double acc_th = 0.0, acc_qv = 0.0;
     Env last = prev;
     for (int j = 2; j <= ncl; ++j) {
-      const Env e = col.env(j);
+      const Env e = col.env_above(j);
       const float dz = -CPDG * 0.5f * (e.thv + prev.thv) * (e.pi - prev.pi);
       const float z = zprev + dz;
       if (j == 2) z2 = z;
@@ -504,10 +512,10 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
       // the parcel that init_parcel will start at level kmax
       float p0, t0, td0, q0;
       source_parcel(col, sel, source, p0, t0, td0, q0);
-      ss.have_lcl = parcel_lcl_slope(guess_w, p0, t0, td0, q0, ss.lcl_y);
-    } else {
+      float y;
+      if (parcel_lcl_slope(guess_w, p0, t0, td0, q0, y)) ss.lcl_y = y;
+    } else if (net_y >= GUESS_Y_MIN && net_y <= GUESS_Y_MAX) {
       ss.lcl_y = net_y;
-      ss.have_lcl = net_y >= GUESS_Y_MIN && net_y <= GUESS_Y_MAX;
     }
   }
   Acc<SOLVER != SOLVE_PLAIN> cape_acc, cin_acc;
@@ -544,7 +552,7 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
   float p_last = 0.0f;
 
   for (int k = 2; k <= ncl; ++k) {
-    const Env cur = col.env(k);
+    const Env cur = col.env_above(k);
     const float dz = -CPDG * 0.5f * (cur.thv + prev.thv) * (cur.pi - prev.pi);
     const float z_low = z;
     z = z + dz;

@@ -44,10 +44,9 @@ __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
 // ---- the learned solver: the guess network on the tensor cores, per warp ----
 //
 // cape_learned_kernel (7 resident blocks of 128 threads per SM: 72 registers,
-// 26 KB of shared memory; measured on a 262k-column slice at 0.820 ms against
-// 0.839 ms with 6 blocks (80 registers), 0.894 ms with 8 (64 registers,
-// spills) and 0.854 ms uncapped (91 registers)) runs each column in three
-// phases: (1) every lane selects
+// 9.7 KB of shared memory: the lanes' column reads need L1, and an unused
+// 26 KB of shared memory slowed the extrapolated kernel by 7.5 %) runs each
+// column in three phases: (1) every lane selects
 // its parcel's source and forms the network's inputs at the parcel's LCL;
 // (2) the warp, converged (__syncwarp), evaluates the network for its 32
 // columns at once -- the 64x64 hidden layer as 2 x 8 x 4 mma.sync.m16n8k16
@@ -59,12 +58,7 @@ struct WarpNetSmem {
   float4 l1[GUESS_H];                               // {W1[k][0..2], b1[k]}
   float b2[GUESS_H], w3[GUESS_H], b3;
   alignas(16) uint32_t w2[GUESS_H * GUESS_H / 2];   // W2 as bf16 pairs, swizzled rows
-  alignas(16) uint32_t h[4][32 * GUESS_H / 2];      // per warp: H1 rows as bf16 pairs
-  float y[4][32];
 };
-// the H1 rows are written 16 bytes at a time
-static_assert(offsetof(WarpNetSmem, h) % 16 == 0, "H1 tile must be 16-byte aligned");
-static_assert((32 * GUESS_H / 2 * sizeof(uint32_t)) % 16 == 0, "H1 tile rows");
 
 // 32-bit word w (a bf16 pair) of 64-wide row r, XOR-swizzled so that the
 // fragment loads of 8 consecutive rows hit 8 different bank groups.
@@ -99,26 +93,42 @@ __device__ void load_warp_net(WarpNetSmem &s, const float *w) {
   }
 }
 
+// Element (row with inputs f, column k) of the first layer, relu'd.
+__device__ __forceinline__ float l1_unit(const WarpNetSmem &s, const float (&f)[3], int k) {
+  const float4 l = s.l1[k];
+  const float h = l.w + l.x * f[0] + l.y * f[1] + l.z * f[2];
+  return h > 0.0f ? h : 0.0f;
+}
+
 // The network's output for the calling lane's inputs; all 32 lanes of the
-// warp must call it together.
-__device__ float warp_guess_eval(WarpNetSmem &s, float f0, float f1, float f2) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *H = s.h[warp];
-  // layer 1 (FP32), the lane's row of H1 as bf16 pairs, four words per store
-  for (int w4 = 0; w4 < GUESS_H / 2; w4 += 4) {
-    uint4 v;
-    uint32_t *pv = reinterpret_cast<uint32_t *>(&v);
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const float4 la = s.l1[2 * (w4 + u)], lb = s.l1[2 * (w4 + u) + 1];
-      float ha = la.w + la.x * f0 + la.y * f1 + la.z * f2;
-      float hb = lb.w + lb.x * f0 + lb.y * f1 + lb.z * f2;
-      pv[u] = bf16x2(ha > 0.0f ? ha : 0.0f, hb > 0.0f ? hb : 0.0f);
-    }
-    *reinterpret_cast<uint4 *>(&H[swz(lane, w4)]) = v;
-  }
-  __syncwarp();
+// warp must call it together.  Rows of the hidden-layer product are the
+// warp's lanes; each lane builds the A fragments it holds (rows gid,
+// gid + 8, 16 + gid, 24 + gid of the 32 x 64 activation matrix, fetched as
+// inputs by shuffle) in registers, so no activation tile goes through
+// shared memory.
+__device__ float warp_guess_eval(const WarpNetSmem &s, float f0, float f1, float f2) {
+  const int lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
+  uint32_t a[2][4][4];  // [M tile][k step][fragment register]
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+    float lo[3], hi[3];
+    const int rlo = mt * 16 + gid, rhi = rlo + 8;
+    lo[0] = __shfl_sync(0xffffffffu, f0, rlo);
+    lo[1] = __shfl_sync(0xffffffffu, f1, rlo);
+    lo[2] = __shfl_sync(0xffffffffu, f2, rlo);
+    hi[0] = __shfl_sync(0xffffffffu, f0, rhi);
+    hi[1] = __shfl_sync(0xffffffffu, f1, rhi);
+    hi[2] = __shfl_sync(0xffffffffu, f2, rhi);
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const int c = ks * 16 + tig * 2;
+      a[mt][ks][0] = bf16x2(l1_unit(s, lo, c), l1_unit(s, lo, c + 1));
+      a[mt][ks][1] = bf16x2(l1_unit(s, hi, c), l1_unit(s, hi, c + 1));
+      a[mt][ks][2] = bf16x2(l1_unit(s, lo, c + 8), l1_unit(s, lo, c + 9));
+      a[mt][ks][3] = bf16x2(l1_unit(s, hi, c + 8), l1_unit(s, hi, c + 9));
+    }
+  }
   float yp[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // rows gid, gid + 8, 16 + gid, 24 + gid
   for (int nt = 0; nt < GUESS_H / 8; ++nt) {
     float acc[2][4] = {{0.0f, 0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f, 0.0f}};
@@ -127,13 +137,8 @@ __device__ float warp_guess_eval(WarpNetSmem &s, float f0, float f1, float f2) {
     for (int ks = 0; ks < 4; ++ks) {
       const int wd = ks * 8 + tig;
       const uint32_t b0 = s.w2[swz(n, wd)], b1 = s.w2[swz(n, wd + 4)];
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        const int r = mt * 16 + gid;
-        const uint32_t a[4] = {H[swz(r, wd)], H[swz(r + 8, wd)], H[swz(r, wd + 4)],
-                               H[swz(r + 8, wd + 4)]};
-        mma16816(acc[mt], a, b0, b1);
-      }
+      mma16816(acc[0], a[0][ks], b0, b1);
+      mma16816(acc[1], a[1][ks], b0, b1);
     }
     const int c = nt * 8 + tig * 2;
 #pragma unroll
@@ -149,16 +154,13 @@ __device__ float warp_guess_eval(WarpNetSmem &s, float f0, float f1, float f2) {
     yp[j] += __shfl_xor_sync(0xffffffffu, yp[j], 1);
     yp[j] += __shfl_xor_sync(0xffffffffu, yp[j], 2);
   }
-  if (tig == 0) {
-    s.y[warp][gid] = yp[0] + s.b3;
-    s.y[warp][gid + 8] = yp[1] + s.b3;
-    s.y[warp][16 + gid] = yp[2] + s.b3;
-    s.y[warp][24 + gid] = yp[3] + s.b3;
-  }
-  __syncwarp();
-  const float y = s.y[warp][lane];
-  __syncwarp();  // the tile is rewritten by the warp's next call
-  return y;
+  // row `lane` is held (whole) by the lanes of quad (lane & 7), in yp[j]
+  const int src = (lane & 7) * 4, j = ((lane >> 4) << 1) | ((lane >> 3) & 1);
+  const float v0 = __shfl_sync(0xffffffffu, yp[0], src);
+  const float v1 = __shfl_sync(0xffffffffu, yp[1], src);
+  const float v2 = __shfl_sync(0xffffffffu, yp[2], src);
+  const float v3 = __shfl_sync(0xffffffffu, yp[3], src);
+  return (j == 0 ? v0 : j == 1 ? v1 : j == 2 ? v2 : v3) + s.b3;
 }
 
 template <typename T, int GRID, bool ICE, bool PSEUDO>
