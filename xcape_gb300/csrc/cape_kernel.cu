@@ -43,10 +43,9 @@ __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
 
 // ---- the learned solver: the guess network on the tensor cores, per warp ----
 //
-// cape_learned_kernel (7 resident blocks of 128 threads per SM: 72 registers,
-// 9.7 KB of shared memory: the lanes' column reads need L1, and an unused
-// 26 KB of shared memory slowed the extrapolated kernel by 7.5 %) runs each
-// column in three phases: (1) every lane selects
+// cape_learned_kernel (7 resident blocks of 128 threads per SM, 72
+// registers, 9.7 KB of shared memory: the weights only, the activations stay
+// in registers) runs each column in three phases: (1) every lane selects
 // its parcel's source and forms the network's inputs at the parcel's LCL;
 // (2) the warp, converged (__syncwarp), evaluates the network for its 32
 // columns at once -- the 64x64 hidden layer as 2 x 8 x 4 mma.sync.m16n8k16
