@@ -41,6 +41,9 @@ ADIABAT = 1
 METRIC = "CAPE/CIN columns/s at 1M×37 lev: learned-guess vs plain CUDA, |ΔCAPE|≤1 J/kg"
 SRH_METRIC = "SRH columns/s at 1M×50 lev (calc_srh, depth 1000+3000 m)"
 CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
+# DRAM bytes (read + write) of one most-unstable launch of the lift on this
+# workload, from `ncu --set full` captures of `bench.py --profile`.
+NCU_TRAFFIC = {"learned": 787_232_256, "plain": 725_900_000}
 ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg
 REF_SAMPLE = 32768       # columns per --impl reference step
 
@@ -422,8 +425,14 @@ def run_ours(args):
                    "column_order": "start level x surface dewpoint" if order else "natural",
                    "l2": "inputs (307 MB) larger than L2 (129 MB), no flush"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
-                     "kernel": f"cape_kernel ({top})", "peak_kind": peak_kind,
+                     "frac": achieved / hbm_peak,
+                     "traffic": NCU_TRAFFIC.get(args.guess),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one "
+                                       "most-unstable launch of this workload"
+                     if args.guess in NCU_TRAFFIC else None,
+                     "kernel": (f"cape_learned_kernel ({top})" if args.guess == "learned"
+                                else f"cape_kernel ({top})"),
+                     "peak_kind": peak_kind,
                      "note": "compute-bound kernel: see fp32 entry"},
         "fp32": {"achieved_tflops": fp32_ach, "peak_tflops_nominal": fp32_peak,
                  "frac": fp32_ach / fp32_peak, "iterations": niter, "substeps": nsub},

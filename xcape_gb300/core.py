@@ -193,8 +193,11 @@ def calc_cape(*args, **kwargs):
 
 
 def _calc_cape_gufunc(*args, **kwargs):
-    """dask arrays: one library call per chunk of columns (core.py:237-258,
-    with the pressure signature taking the 1-D ``p`` as a core dimension)."""
+    """dask arrays: one library call per chunk of columns (core.py:237-258).
+    The 1-D ``p`` of pressure levels is bound to every chunk's call rather
+    than passed as a gufunc argument (the reference's pressure signature
+    lists seven inputs for six arrays, core.py:245-247); the level axis is
+    the trailing core dimension, so no ``axis`` argument is passed."""
     import dask.array as da
     vertical_lev = kwargs.get("vertical_lev", "sigma")
     signature = "(i),(i),(i),(),(),()->(),()"
@@ -209,10 +212,10 @@ def _calc_cape_gufunc(*args, **kwargs):
         def f(t, td, ps, ts, tds, **kw):
             return _calc_cape_numpy(p_np, t, td, ps, ts, tds, **kw)
         sig = signature.replace("(i),(i),(i)", "(i),(i)", 1)
-        return da.apply_gufunc(f, sig, *rest, output_dtypes=output_dtypes, axis=-1,
+        return da.apply_gufunc(f, sig, *rest, output_dtypes=output_dtypes,
                                vectorize=False, **kwargs)
     return da.apply_gufunc(_calc_cape_numpy, signature, *args, output_dtypes=output_dtypes,
-                           axis=-1, vectorize=False, **kwargs)
+                           vectorize=False, **kwargs)
 
 
 def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-liquid",
@@ -373,9 +376,9 @@ def _calc_srh_gufunc(*args, **kwargs):
         def f(*a, **kw):
             return _calc_srh_numpy(p_np, *a, **kw)
         return da.apply_gufunc(f, signature.replace("(i),", "", 1), *args[1:],
-                               output_dtypes=output_dtypes, axis=-1, vectorize=False, **kwargs)
+                               output_dtypes=output_dtypes, vectorize=False, **kwargs)
     return da.apply_gufunc(_calc_srh_numpy, signature, *args, output_dtypes=output_dtypes,
-                           axis=-1, vectorize=False, **kwargs)
+                           vectorize=False, **kwargs)
 
 
 _SRH_PRECISION = {"reference": 0, "fp32": 1}
