@@ -248,14 +248,9 @@ cudaError_t launch_guess_pairs(long long n, unsigned long long seed, float *feat
 cudaError_t launch_guess_grad(const float *w, const float *feats, const float *targets,
                               long long batch0, long long nb, float *grad, float *loss,
                               cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(guess_train_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TrainSmem));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static std::atomic<int> attr[kMaxAttrDevices];
+  const cudaError_t ae = smem_attr_once((const void *)guess_train_kernel, (int)sizeof(TrainSmem), attr);
+  if (ae != cudaSuccess) return ae;
   const unsigned blocks = (unsigned)((nb + TB - 1) / TB);
   if (blocks == 0) return cudaSuccess;
   guess_train_kernel<<<blocks, TB, sizeof(TrainSmem), s>>>(w, feats, targets, batch0, nb, grad,
@@ -274,14 +269,9 @@ cudaError_t launch_guess_adam(float *w, float *grad, float *m, float *v, float l
 
 cudaError_t launch_guess_eval(const float *w, const float *feats, long long n, float *out,
                               cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(guess_eval_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TrainSmem));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static std::atomic<int> attr[kMaxAttrDevices];
+  const cudaError_t ae = smem_attr_once((const void *)guess_eval_kernel, (int)sizeof(TrainSmem), attr);
+  if (ae != cudaSuccess) return ae;
   const unsigned blocks = (unsigned)((n + TB - 1) / TB);
   if (blocks == 0) return cudaSuccess;
   guess_eval_kernel<<<blocks, TB, sizeof(TrainSmem), s>>>(w, feats, n, out);

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include "srh_column.cuh"
+#include "xc_kernels.h"
 
 namespace xc {
 
@@ -145,13 +146,10 @@ __global__ void __launch_bounds__(SRH_TILE) srh_tile_kernel(SrhArgs a) {
 
 template <int GRID>
 static cudaError_t launch_srh_tile(const SrhArgs &a, size_t smem, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(
-        srh_tile_kernel<GRID>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SRH_TILE_SMEM_MAX);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static std::atomic<int> attr[kMaxAttrDevices];
+  const cudaError_t e =
+      smem_attr_once((const void *)srh_tile_kernel<GRID>, (int)SRH_TILE_SMEM_MAX, attr);
+  if (e != cudaSuccess) return e;
   const unsigned blocks = (unsigned)((a.n2 + SRH_TILE - 1) / SRH_TILE);
   srh_tile_kernel<GRID><<<blocks, SRH_TILE, smem, s>>>(a);
   return cudaGetLastError();

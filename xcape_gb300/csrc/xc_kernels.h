@@ -1,5 +1,6 @@
 // xc_kernels.h -- launch interface between the C ABI (capi.cu) and the kernels.
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 
 namespace xc {
@@ -56,6 +57,23 @@ cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStre
 
 // Records msg as the calling thread's xc_last_error() text (capi.cu).
 int set_error(int code, const char *msg);
+
+// Raises `func`'s dynamic shared-memory limit to `bytes` on the current
+// device, once per device (the attribute is per device; setting it again is
+// harmless, so concurrent first calls need no lock).  done: a per-call-site
+// array of kMaxAttrDevices flags.
+constexpr int kMaxAttrDevices = 64;
+inline cudaError_t smem_attr_once(const void *func, int bytes, std::atomic<int> *done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxAttrDevices && done[dev].load(std::memory_order_acquire))
+    return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && dev >= 0 && dev < kMaxAttrDevices)
+    done[dev].store(1, std::memory_order_release);
+  return e;
+}
 cudaError_t launch_pres_lev_pos(const void *p1d, const void *ps, int dtype, int nk, long long n2,
                                 int *start, cudaStream_t s);
 
