@@ -44,7 +44,15 @@ CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
 # DRAM bytes (read + write) of one most-unstable launch of the lift on this
 # workload, from `ncu --set full` captures of `bench.py --profile`.
 NCU_TRAFFIC = {"learned": 787_232_256, "plain": 725_900_000}
+# The lift is bound by the SM issue rate, not by HBM: issue-slot activity of
+# the same captures (smsp__issue_active, % of peak over active cycles) and the
+# tensor pipe's share (the learned kernel's guess network).
+NCU_ISSUE = {"learned": {"issue_active": 0.860, "tensor_pipe_active": 0.0052,
+                         "threads_per_warp_instruction": 25.76},
+             "plain": {"issue_active": 0.892, "tensor_pipe_active": 0.0,
+                       "threads_per_warp_instruction": 27.12}}
 ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg
+CPU_SAMPLE_1T = 8192     # columns per single-core CPU-baseline measurement
 REF_SAMPLE = 32768       # columns per --impl reference step
 
 
@@ -434,6 +442,9 @@ def run_ours(args):
                                 else f"cape_kernel ({top})"),
                      "peak_kind": peak_kind,
                      "note": "compute-bound kernel: see fp32 entry"},
+        "issue_roofline": dict(NCU_ISSUE.get(args.guess, {}),
+                               source="ncu --set full, one most-unstable launch")
+        if args.guess in NCU_ISSUE else None,
         "fp32": {"achieved_tflops": fp32_ach, "peak_tflops_nominal": fp32_peak,
                  "frac": fp32_ach / fp32_peak, "iterations": niter, "substeps": nsub},
         "per_source_ms": per_src_ms,
@@ -453,9 +464,12 @@ def run_ours(args):
         import oracle  # noqa: F401
         nth = os.cpu_count() or 1
         v = cpu_cape(CPU_SAMPLE, nth)
+        v1 = cpu_cape(CPU_SAMPLE_1T, 1)
         line["cpu_baseline"] = {"value": v, "unit": "columns/s", "cores": nth, "kind": "port",
                                 "sample": f"first {CPU_SAMPLE} columns, both sources, FP32 "
-                                          "oracle (C restatement of the Fortran), OpenMP"}
+                                          "oracle (C restatement of the Fortran), OpenMP",
+                                "single_core": {"value": v1, "cores": 1,
+                                                "sample": f"first {CPU_SAMPLE_1T} columns"}}
         line["accuracy_vs_fp64"] = accuracy_vs_fp64(outs, nth)
     print(json.dumps(line), flush=True)
     if dist:
