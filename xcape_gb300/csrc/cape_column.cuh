@@ -85,10 +85,10 @@ struct CapeResult {
 //   SOLVE_ACCEL: same map F, same stopping test |F(x) - x| <= 2e-4 and the
 //                same result th2 = F(x), but the first guess extrapolates
 //                the previous sub-step's increment (scaled by the ratio of
-//                the pressure steps), the first step divides by 1 - F' with
-//                the slope F' last measured in an earlier sub-step, and
-//                from the second evaluation on x moves by a secant step on
-//                g(x) = F(x) - x.  The fixed
+//                the pressure steps), the first step is a Newton step on
+//                g(x) = F(x) - x with F' differentiated analytically at the
+//                first evaluation, and from the second evaluation on x
+//                moves by a secant step on g.  The fixed
 //                0.3 damping contracts by |1 - 0.3 (1 - F')|, about 0.8 for
 //                the F' ~ -5 of warm saturated sub-steps, and in FP32 it can
 //                lock into a two-value cycle one ulp wide whose step stays
@@ -117,16 +117,11 @@ constexpr int SOLVE_ACCEL = 1;
 constexpr int SOLVE_LEARNED = 2;
 constexpr int SOLVE_SECANT = 3;
 constexpr int SOLVE_LEARNED_ALL = 4;
-// A difference quotient of F over points closer than this (K) is too noisy
-// to carry to the next sub-step.
-constexpr float SLOPE_MIN_DX = 1e-3f;
 
 struct SolverState {
   float dth_prev = 0.0f;  // th2 - th1 of the previous sub-step
   float dp_prev = 1.0f;   // its pressure step
-  float slope = 0.0f;     // last difference quotient of F (the map's slope)
   bool have_prev = false;
-  bool have_slope = false;
   bool saturated = false;   // (SOLVE_LEARNED_ALL) condensate at the end of the last sub-step
   // (SOLVE_LEARNED) the network's output at the parcel's LCL until the
   // parcel first saturates, NaN once used or when there is none
@@ -172,8 +167,23 @@ XC_HD bool network_increment(const float *w, float p1, float p2, float t1, float
   return true;
 }
 
+// d qsat / dT of qsat = QEPS es / (p - es), es = 611.2 exp(a (T - 273.15) / (T - b))
+// (getqvs: a = 17.67, b = 29.65; getqvi: a = 21.8745584, b = 7.66), from the
+// values the evaluation already has: qsat p / (p - es) * k / (T - b)^2 with
+// k = a (273.15 - b) and tb = T - b.
+XC_HD float dqsat_dt(float qsat, float p, float es, float tb, float k) {
+  return fast_div(qsat * p * k, (p - es) * tb * tb);
+}
+
 // One sub-step of the moist adiabat (:417-498).  Returns false when the
 // iteration did not converge within 100 steps (:465-474).
+//
+// The accelerated modes (SOLVE_ACCEL, SOLVE_LEARNED) take their first step
+// from the first guess x0 as a Newton step on F(x) - x, with the slope F'(x0)
+// of the map differentiated analytically at the first evaluation: through
+// t2 = x pi2, the saturation mixing ratio (dqsat_dt), the condensate split
+// and the exponent.  Secant steps follow.  The stopping test is the
+// reference's.
 template <bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
 XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
                                         float &ql2, float &qi2, float &qt, int &niter,
@@ -206,6 +216,8 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   } else if (EXTRAP && ss.have_prev) {
     thlast = th1 + ss.dth_prev * (dp / ss.dp_prev);
   }
+  // (EXTRAP) d/dt2 of qv2, ql2, qi2 and of the exponent at the first evaluation
+  float dq = 0.0f, dql = 0.0f, dqi = 0.0f, dex = 0.0f;
   int i = 0;
   while (true) {
     i = i + 1;
@@ -214,11 +226,36 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     if (ICE) {
       fliq = fmax_f(fmin_f((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
       fice = 1.0f - fliq;
-      qsat = fliq * getqvs(p2, t2) + fice * getqvi(p2, t2);
+      if (EXTRAP) {
+        float esl, esi;
+        const float qvs = getqvs_es(p2, t2, esl), qvi = getqvi_es(p2, t2, esi);
+        qsat = fliq * qvs + fice * qvi;
+        if (i == 1 && qt > qsat) {
+          // saturated: qv2 = qsat, ql2 = fliq (qt - qsat), qi2 = fice (qt - qsat)
+          const float dfl = (t2 > 233.15f && t2 < 273.15f) ? 1.0f / (273.15f - 233.15f) : 0.0f;
+          dq = dfl * (qvs - qvi) +
+               fliq * dqsat_dt(qvs, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f)) +
+               fice * dqsat_dt(qvi, p2, esi, t2 - 7.66f, 21.8745584f * (273.15f - 7.66f));
+          const float c = dfl * (qt - qsat);
+          dql = c - fliq * dq;
+          dqi = -c - fice * dq;
+        }
+      } else {
+        qsat = fliq * getqvs(p2, t2) + fice * getqvi(p2, t2);
+      }
     } else {
       fliq = 1.0f;
       fice = 0.0f;
-      qsat = getqvs(p2, t2);
+      if (EXTRAP) {
+        float esl;
+        qsat = getqvs_es(p2, t2, esl);
+        if (i == 1 && qt > qsat) {
+          dq = dqsat_dt(qsat, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f));
+          dql = -dq;
+        }
+      } else {
+        qsat = getqvs(p2, t2);
+      }
     }
     qv2 = fmin_f(qt, qsat);
     if (ICE) {
@@ -242,7 +279,19 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
                             : CP + CPV * qvbar + CPL * qlbar;
       float num = lhv * (ql2 - ql1) + rm * lp * tbar;
       if (ICE) num += (LS1 - LS2 * tbar) * (qi2 - qi1);
-      expo = fast_div(num, cpm * tbar) - RDDCP * lp;
+      const float den = cpm * tbar;
+      const float r = fast_div(num, den);
+      expo = r - RDDCP * lp;
+      if (EXTRAP && i == 1) {
+        // d expo / d t2 = (num' - r den') / den, tbar' = 1/2
+        float dnum = lhv * dql - 0.5f * LV2 * (ql2 - ql1) + lp * (0.5f * RV * dq * tbar + 0.5f * rm);
+        float dcpm = CPV * dq + CPL * dql;
+        if (ICE) {
+          dnum += (LS1 - LS2 * tbar) * dqi - 0.5f * LS2 * (qi2 - qi1);
+          dcpm += CPI * dqi;
+        }
+        dex = fast_div(dnum - r * (0.5f * dcpm * tbar + 0.5f * cpm), den);
+      }
     } else if (ICE) {
       const float qibar = 0.5f * (qi1 + qi2);
       const float lhs = LS1 - LS2 * tbar;
@@ -261,18 +310,16 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     const bool have_q = SOLVER != SOLVE_PLAIN && i >= 2 && thlast != x_prev;
     float s = 0.0f;
     if (have_q) s = fmin_f(fmax_f(fast_div(th2 - f_prev, thlast - x_prev), -50.0f), 0.5f);
-    if (EXTRAP && have_q && fabsf(thlast - x_prev) >= SLOPE_MIN_DX) {
-      ss.slope = s;
-      ss.have_slope = true;
-    }
     if (fabsf(th2 - thlast) > CONVERGE) {
       const float step = th2 - thlast;
       x_prev = thlast;
       f_prev = th2;
       if (have_q) {
         thlast = thlast + fast_div(step, 1.0f - s);  // secant step on F(x) - x
-      } else if (EXTRAP && ss.have_slope) {
-        thlast = thlast + fast_div(step, 1.0f - ss.slope);  // the last sub-step's slope
+      } else if (EXTRAP) {
+        // Newton step with F'(x0) = F(x0) pi2 d expo / d t2, in the same range
+        const float fp = fmin_f(fmax_f(th2 * pi2 * dex, -50.0f), 0.5f);
+        thlast = thlast + fast_div(step, 1.0f - fp);
       } else {
         thlast = thlast + 0.3f * step;
       }

@@ -57,6 +57,18 @@ XC_HD float getqvs(float p, float t) {
   float es = 611.2f * expf(17.67f * (t - 273.15f) / (t - 29.65f));
   return QEPS * es / (p - es);
 }
+// getqvs / getqvi that also return the saturation vapour pressure (the same
+// operations, so the same result), for the slope of the moist-adiabat map.
+XC_HD float getqvs_es(float p, float t, float &es_out) {
+  const float es = 611.2f * expf(17.67f * (t - 273.15f) / (t - 29.65f));
+  es_out = es;
+  return QEPS * es / (p - es);
+}
+XC_HD float getqvi_es(float p, float t, float &es_out) {
+  const float es = 611.2f * expf(21.8745584f * (t - 273.15f) / (t - 7.66f));
+  es_out = es;
+  return QEPS * es / (p - es);
+}
 // CAPE_CODE_model_lev.f90:587-598
 XC_HD float getqvi(float p, float t) {
   float es = 611.2f * expf(21.8745584f * (t - 273.15f) / (t - 7.66f));
