@@ -228,7 +228,7 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
       fice = 1.0f - fliq;
       if (EXTRAP) {
         float esl, esi;
-        const float qvs = getqvs_es(p2, t2, esl), qvi = getqvi_es(p2, t2, esi);
+        const float qvs = getqvs_fast(p2, t2, esl), qvi = getqvi_fast(p2, t2, esi);
         qsat = fliq * qvs + fice * qvi;
         if (i == 1 && qt > qsat) {
           // saturated: qv2 = qsat, ql2 = fliq (qt - qsat), qi2 = fice (qt - qsat)
@@ -248,7 +248,7 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
       fice = 0.0f;
       if (EXTRAP) {
         float esl;
-        qsat = getqvs_es(p2, t2, esl);
+        qsat = getqvs_fast(p2, t2, esl);
         if (i == 1 && qt > qsat) {
           dq = dqsat_dt(qsat, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f));
           dql = -dq;
@@ -302,7 +302,7 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
       const float cpm = CP + CPV * qvbar + CPL * qlbar;
       expo = lhv * (ql2 - ql1) / (cpm * tbar) + (rm / cpm - RDDCP) * lp;
     }
-    th2 = th1 * expf(expo);
+    th2 = th1 * (ACCEL_MATH ? fast_exp(expo) : expf(expo));
     ++niter;
     if (i > 100) return false;
     // difference quotient of F over the last two evaluations, kept in

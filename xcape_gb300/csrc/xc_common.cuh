@@ -57,18 +57,6 @@ XC_HD float getqvs(float p, float t) {
   float es = 611.2f * expf(17.67f * (t - 273.15f) / (t - 29.65f));
   return QEPS * es / (p - es);
 }
-// getqvs / getqvi that also return the saturation vapour pressure (the same
-// operations, so the same result), for the slope of the moist-adiabat map.
-XC_HD float getqvs_es(float p, float t, float &es_out) {
-  const float es = 611.2f * expf(17.67f * (t - 273.15f) / (t - 29.65f));
-  es_out = es;
-  return QEPS * es / (p - es);
-}
-XC_HD float getqvi_es(float p, float t, float &es_out) {
-  const float es = 611.2f * expf(21.8745584f * (t - 273.15f) / (t - 7.66f));
-  es_out = es;
-  return QEPS * es / (p - es);
-}
 // CAPE_CODE_model_lev.f90:587-598
 XC_HD float getqvi(float p, float t) {
   float es = 611.2f * expf(21.8745584f * (t - 273.15f) / (t - 7.66f));
@@ -87,18 +75,39 @@ XC_HD float getthe(float p, float t, float td, float q) {
 }
 
 // Approximate divide (a few ulp) for the accelerated solvers: their secant
-// quotients and the exponent of their map, whose contract is agreement with
-// the FP64 run within tolerance rather than bit-faithfulness to the FP32
-// Fortran.  Exact on the host.  getqvs/getqvi keep IEEE operations in every
-// mode: builds with approximate exp (__expf) or approximate divides inside
-// them ran 12-18x slower on sm_103a, the warps no longer reconverging after
-// the sub-step (1.2 active threads per executed instruction, measured).
+// quotients, the saturation mixing ratio and the exponent of their map, whose
+// contract is agreement with the FP64 run within tolerance rather than
+// bit-faithfulness to the FP32 Fortran.  Exact on the host.
 XC_HD float fast_div(float a, float b) {
 #if defined(__CUDA_ARCH__)
   return __fdividef(a, b);
 #else
   return a / b;
 #endif
+}
+// Approximate exp for the same solvers: ex2.approx of x log2(e), a relative
+// error of a few ulp plus the rounding of x log2(e).  expf on the host.
+XC_HD float fast_exp(float x) {
+#if defined(__CUDA_ARCH__)
+  return __expf(x);
+#else
+  return expf(x);
+#endif
+}
+
+// getqvs / getqvi of the accelerated solvers: the same formulas with the
+// approximate exp and divides (the host build computes exactly what getqvs /
+// getqvi do), also returning the saturation vapour pressure es for the
+// slope of the moist-adiabat map.
+XC_HD float getqvs_fast(float p, float t, float &es_out) {
+  const float es = 611.2f * fast_exp(fast_div(17.67f * (t - 273.15f), t - 29.65f));
+  es_out = es;
+  return fast_div(QEPS * es, p - es);
+}
+XC_HD float getqvi_fast(float p, float t, float &es_out) {
+  const float es = 611.2f * fast_exp(fast_div(21.8745584f * (t - 273.15f), t - 7.66f));
+  es_out = es;
+  return fast_div(QEPS * es, p - es);
 }
 
 // Fortran MIN/MAX as gfortran lowers them for the reference build: the
