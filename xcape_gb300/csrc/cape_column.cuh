@@ -26,27 +26,51 @@ struct Env {
   float p, t, td, pi, q, th, thv;
 };
 
+// FAST (the accelerated solvers): pi from exp(RDDCP ln(p/P00)), q from
+// getqvs_fast and the two quotients from approximate divides.
+template <bool FAST = false>
 XC_HD Env make_env(float pin, float tin, float tdin) {
   Env e;
   e.p = 100.0f * pin;
   e.t = 273.15f + tin;
   e.td = 273.15f + tdin;
-  e.pi = powf(e.p * RP00, RDDCP);
-  e.q = getqvs(e.p, e.td);
-  e.th = e.t / e.pi;
-  e.thv = e.th * (1.0f + REPS * e.q) / (1.0f + e.q);
+  if (FAST) {
+    float es;
+    e.pi = fast_exp(RDDCP * fast_log(e.p * RP00));
+    e.q = getqvs_fast(e.p, e.td, es);
+    e.th = fast_div(e.t, e.pi);
+    e.thv = fast_div(e.th * (1.0f + REPS * e.q), 1.0f + e.q);
+  } else {
+    e.pi = powf(e.p * RP00, RDDCP);
+    e.q = getqvs(e.p, e.td);
+    e.th = e.t / e.pi;
+    e.thv = e.th * (1.0f + REPS * e.q) / (1.0f + e.q);
+  }
   return e;
 }
 
 // Reader of one assembled column: level 1 is the surface, level j >= 2 is
 // the 1-based input level start + j - 2, i.e. 0-based index start - 3 + j.
+// The array pointers are those of all columns (the kernel's arguments) and
+// one 64-bit offset locates the column, so that a column costs the ascent
+// one register pair instead of three pointers.
 template <typename T, int GRID>
 struct ColumnReader {
-  const T *p;   // GRID 1/3: this column's p; GRID 2: shared p1d
-  const T *t;   // this column's t
-  const T *td;  // this column's td
+  const T *p;   // GRID 1/3: p of all columns; GRID 2: the shared p1d
+  const T *t;   // t of all columns
+  const T *td;  // td of all columns
   float ps, ts, tds;
-  int base;     // start - 3, so that the 0-based input index of level j is base + j
+  long long cbase;  // column offset + start - 3: t, td (and GRID 1/3 p) of level j at cbase + j
+  int base;         // start - 3: the GRID 2 p of level j at base + j
+
+  XC_HD void set(const T *p_all, const T *t_all, const T *td_all, long long col_off, int start) {
+    p = p_all;
+    t = t_all;
+    td = td_all;
+    cbase = col_off + start - 3;
+    base = start - 3;
+  }
+  XC_HD const T *p_at(int j) const { return GRID == 2 ? p + (base + j) : p + (cbase + j); }
 
   XC_HD void level(int j, float &pin, float &tin, float &tdin) const {
     if (j == 1) {
@@ -54,22 +78,22 @@ struct ColumnReader {
       tin = ts;
       tdin = tds;
     } else {
-      int m = base + j;
-      pin = ldf(p + m);
-      tin = ldf(t + m);
-      tdin = ldf(td + m);
+      pin = ldf(p_at(j));
+      tin = ldf(t + (cbase + j));
+      tdin = ldf(td + (cbase + j));
     }
   }
+  template <bool FAST = false>
   XC_HD Env env(int j) const {
     float a, b, c;
     level(j, a, b, c);
-    return make_env(a, b, c);
+    return make_env<FAST>(a, b, c);
   }
   // level j >= 2 (above the surface): loops over those levels then need no
   // surface values, which frees their registers
+  template <bool FAST = false>
   XC_HD Env env_above(int j) const {
-    const int m = base + j;
-    return make_env(ldf(p + m), ldf(t + m), ldf(td + m));
+    return make_env<FAST>(ldf(p_at(j)), ldf(t + (cbase + j)), ldf(td + (cbase + j)));
   }
 };
 
@@ -119,9 +143,9 @@ constexpr int SOLVE_SECANT = 3;
 constexpr int SOLVE_LEARNED_ALL = 4;
 
 struct SolverState {
-  float dth_prev = 0.0f;  // th2 - th1 of the previous sub-step
-  float dp_prev = 1.0f;   // its pressure step
-  bool have_prev = false;
+  // (SOLVE_ACCEL, SOLVE_LEARNED) (th2 - th1) / dp of the previous sub-step;
+  // 0 before the first, so that the first guess is th1
+  float rate = 0.0f;
   bool saturated = false;   // (SOLVE_LEARNED_ALL) condensate at the end of the last sub-step
   // (SOLVE_LEARNED) the network's output at the parcel's LCL until the
   // parcel first saturates, NaN once used or when there is none
@@ -191,16 +215,18 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   const float p1 = p2, t1 = t2, th1 = th2, qv1 = qv2, ql1 = ql2, qi1 = qi2;
   p2 = p2 - dp;
   // The accelerated modes take pi2 and ln(p2/p1) from one logarithm of p2
-  // (ln p1 is the previous sub-step's): one logf and one expf in place of
-  // powf, a divide and logf.  ln(p2/p1) then carries an absolute error of
-  // about 1e-6, and it only scales the dry term (R_m/c_pm - R_d/c_p) ln(p2/p1)
-  // of the exponent, whose prefactor is below 1e-3.
+  // (ln p1 is the previous sub-step's), with the approximate log and exp, in
+  // place of powf, a divide and logf.  The log's error (3 ulp of ln p2 at
+  // most, about 3e-6) enters ln(p2/p1) only through the dry term
+  // (R_m/c_pm - R_d/c_p) ln(p2/p1) of the exponent, whose prefactor is below
+  // 0.02, and pi2 = exp(R_d/c_p (ln p2 - ln P00)) as a relative error of
+  // about 1e-6 in t2, which the next sub-step's map does not carry forward.
   constexpr bool ACCEL_MATH = SOLVER != SOLVE_PLAIN;
   float pi2, lp;
   if (ACCEL_MATH) {
-    const float lnp2 = logf(p2);
+    const float lnp2 = fast_log(p2);
     lp = lnp2 - ss.lnp;
-    pi2 = expf(RDDCP * (lnp2 - LN_P00));
+    pi2 = fast_exp(RDDCP * (lnp2 - LN_P00));
     ss.lnp = lnp2;
   } else {
     pi2 = powf(p2 * RP00, RDDCP);
@@ -213,8 +239,8 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
              network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net)) {
     thlast = th1 + dth_net;
-  } else if (EXTRAP && ss.have_prev) {
-    thlast = th1 + ss.dth_prev * (dp / ss.dp_prev);
+  } else if (EXTRAP) {
+    thlast = th1 + ss.rate * dp;
   }
   // (EXTRAP) d/dt2 of qv2, ql2, qi2 and of the exponent at the first evaluation
   float dq = 0.0f, dql = 0.0f, dqi = 0.0f, dex = 0.0f;
@@ -226,11 +252,11 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     if (ICE) {
       fliq = fmax_f(fmin_f((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
       fice = 1.0f - fliq;
-      if (EXTRAP) {
+      if (ACCEL_MATH) {
         float esl, esi;
         const float qvs = getqvs_fast(p2, t2, esl), qvi = getqvi_fast(p2, t2, esi);
         qsat = fliq * qvs + fice * qvi;
-        if (i == 1 && qt > qsat) {
+        if (EXTRAP && i == 1 && qt > qsat) {
           // saturated: qv2 = qsat, ql2 = fliq (qt - qsat), qi2 = fice (qt - qsat)
           const float dfl = (t2 > 233.15f && t2 < 273.15f) ? 1.0f / (273.15f - 233.15f) : 0.0f;
           dq = dfl * (qvs - qvi) +
@@ -246,10 +272,10 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     } else {
       fliq = 1.0f;
       fice = 0.0f;
-      if (EXTRAP) {
+      if (ACCEL_MATH) {
         float esl;
         qsat = getqvs_fast(p2, t2, esl);
-        if (i == 1 && qt > qsat) {
+        if (EXTRAP && i == 1 && qt > qsat) {
           dq = dqsat_dt(qsat, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f));
           dql = -dq;
         }
@@ -328,14 +354,12 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     }
   }
   if (EXTRAP) {
-    ss.dth_prev = th2 - th1;
-    ss.dp_prev = dp;
-    ss.have_prev = true;
+    ss.rate = fast_div(th2 - th1, dp);
   }
   if (SOLVER == SOLVE_LEARNED && ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y) {
     // the parcel has just saturated: the increment extrapolated into the
     // next sub-step is the network's, not this sub-step's partial one
-    ss.dth_prev = -GUESS_SLOPE_SCALE * ss.lcl_y * lp;
+    ss.rate = -GUESS_SLOPE_SCALE * ss.lcl_y * fast_div(lp, dp);
     ss.lcl_y = NAN;
   }
   if (SOLVER == SOLVE_LEARNED_ALL) ss.saturated = ql2 + qi2 > 0.0f;
@@ -412,11 +436,12 @@ constexpr int DIAG_N = 6;
 struct SourceSel {
   int kmax;
   int mulvl;
-  double avgth, avgqv;
+  float avgth, avgqv;  // the FP64 means, rounded once (every use is in FP32)
   bool ascend;
 };
 
-template <typename T, int GRID>
+// FAST: the accelerated solvers' environment (make_env) in the mixed layer.
+template <bool FAST, typename T, int GRID>
 XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int source,
                               float ml_depth) {
   SourceSel sel;
@@ -451,14 +476,14 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
     // :284-339 -- mixed layer.  One upward pass evaluates the do-while
     // accumulation (:313-322) and the two guards (:287, :295), which need
     // z(2) and z(nk).
-    Env prev = col.env(1);
+    Env prev = col.template env<FAST>(1);
     const Env e1 = prev;
     float zprev = 0.0f, z2 = 0.0f;
     bool active = true;
     double acc_th = 0.0, acc_qv = 0.0;
     Env last = prev;
     for (int j = 2; j <= ncl; ++j) {
-      const Env e = col.env_above(j);
+      const Env e = col.template env_above<FAST>(j);
       const float dz = -CPDG * 0.5f * (e.thv + prev.thv) * (e.pi - prev.pi);
       const float z = zprev + dz;
       if (j == 2) z2 = z;
@@ -500,22 +525,22 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
     }
   }
   sel.kmax = kmax;
-  sel.avgth = avgth;
-  sel.avgqv = avgqv;
+  sel.avgth = (float)avgth;
+  sel.avgqv = (float)avgqv;
   return sel;
 }
 
 // The source parcel's state (p, t, td in Pa and K, mixing ratio q): the
 // environment at kmax, or the mixed-layer means at the surface with the
 // dewpoint of the mean mixing ratio.
-template <typename T, int GRID>
+template <bool FAST, typename T, int GRID>
 XC_HD void source_parcel(const ColumnReader<T, GRID> &col, const SourceSel &sel, int source,
                          float &p, float &t, float &td, float &q) {
-  const Env es = col.env(sel.kmax);
+  const Env es = col.template env<FAST>(sel.kmax);
   p = es.p;
   if (source == 3) {
-    q = (float)sel.avgqv;
-    t = (float)sel.avgth * es.pi;
+    q = sel.avgqv;
+    t = sel.avgth * es.pi;
     td = dewpoint_of(es.p, q);
   } else {
     q = es.q;
@@ -544,21 +569,21 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
   r.nsub = 0;
   r.niter = 0;
   const int kmax = sel.kmax;
-  const double avgth = sel.avgth, avgqv = sel.avgqv;
+  const float avgth = sel.avgth, avgqv = sel.avgqv;
 
   // Ascent (:355-559).  Levels below kmax only integrate z.
-  Env prev = col.env(1);
+  constexpr bool FAST = SOLVER != SOLVE_PLAIN;
+  Env prev = col.template env<FAST>(1);
   float z = 0.0f;
   float th2 = 0.f, p2 = 0.f, t2 = 0.f, qv2 = 0.f, b2 = 0.f, ql2 = 0.f, qi2 = 0.f, qt = 0.f;
   float narea = 0.0f;
-  long long nsub_total = 0;
   SolverState ss;
   ss.guess_w = guess_w;
   if (SOLVER == SOLVE_LEARNED) {
     if (guess_w) {
       // the parcel that init_parcel will start at level kmax
       float p0, t0, td0, q0;
-      source_parcel(col, sel, source, p0, t0, td0, q0);
+      source_parcel<SOLVER != SOLVE_PLAIN>(col, sel, source, p0, t0, td0, q0);
       float y;
       if (parcel_lcl_slope(guess_w, p0, t0, td0, q0, y)) ss.lcl_y = y;
     } else if (net_y >= GUESS_Y_MIN && net_y <= GUESS_Y_MAX) {
@@ -568,8 +593,8 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
   Acc<SOLVER != SOLVE_PLAIN> cape_acc, cin_acc;
   auto init_parcel = [&](const Env &e) {
     if (source == 3) {
-      th2 = (float)avgth;
-      qv2 = (float)avgqv;
+      th2 = avgth;
+      qv2 = avgqv;
       const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2);
       p2 = e.p;
       t2 = th2 * e.pi;
@@ -584,7 +609,7 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
     ql2 = 0.0f;
     qi2 = 0.0f;
     qt = qv2;
-    if (SOLVER != SOLVE_PLAIN) ss.lnp = logf(p2);
+    if (SOLVER != SOLVE_PLAIN) ss.lnp = fast_log(p2);
   };
   auto source_diag = [&](const Env &e) {
     if (DIAG) {
@@ -599,7 +624,7 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
   float p_last = 0.0f;
 
   for (int k = 2; k <= ncl; ++k) {
-    const Env cur = col.env_above(k);
+    const Env cur = col.template env_above<FAST>(k);
     const float dz = -CPDG * 0.5f * (cur.thv + prev.thv) * (cur.pi - prev.pi);
     const float z_low = z;
     z = z + dz;
@@ -623,8 +648,7 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
         nloop = 1 + (int)f;
         dp = dp / (float)nloop;
       }
-      nsub_total += nloop;
-      if (nsub_total > MAX_SUBSTEPS) {
+      if (r.nsub + nloop > MAX_SUBSTEPS) {
         r.cape = 0.0f;
         r.cin = 0.0f;
         r.status |= COL_TOOMANYSTEPS;
@@ -716,7 +740,7 @@ template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
 XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
                                   int source, float ml_depth, const float *guess_w = nullptr,
                                   float *dg = nullptr) {
-  const SourceSel sel = select_source(col, ncl, source, ml_depth);
+  const SourceSel sel = select_source<SOLVER != SOLVE_PLAIN>(col, ncl, source, ml_depth);
   if (!sel.ascend) {
     CapeResult r;
     r.mulvl = sel.mulvl;
@@ -743,9 +767,6 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
     if (DIAG)
       for (int d = 0; d < DIAG_N; ++d) dg[d] = DIAG_MISSING;
     const long long stride = a.ld > 0 ? a.ld : a.nk;
-    const T *tin = (const T *)a.t + i * stride;
-    const T *tdin = (const T *)a.td + i * stride;
-    const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * stride;
     const float ts = ldf((const T *)a.ts + i);
     float cape = 0.0f, cin = 0.0f, zo = 0.0f;
     int mulvl = 0, status = 0;
@@ -762,13 +783,10 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
         status = COL_BADSTART;
       } else {
         ColumnReader<T, GRID> col;
-        col.p = pin;
-        col.t = tin;
-        col.td = tdin;
+        col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
         col.ps = ldf((const T *)a.ps + i);
         col.ts = ts;
         col.tds = ldf((const T *)a.tds + i);
-        col.base = start - 3;
         const int ncl = a.nk - start + 2;
         CapeResult r =
             getcape_col<ICE, PSEUDO, SOLVER, DIAG>(col, ncl, a.pinc, a.source, a.ml_depth, guess_w,

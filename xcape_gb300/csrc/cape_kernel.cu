@@ -92,6 +92,32 @@ __device__ void load_warp_net(WarpNetSmem &s, const float *w) {
   }
 }
 
+// The shared-memory image of the guess network on this device, built from
+// the parameters once per xc_guess_set_weights (build_warp_net), so that a
+// block of the learned kernel copies 9.7 KB with 16-byte loads instead of
+// converting and swizzling W2 from FP32 parameters.
+__device__ WarpNetSmem g_warp_net;
+static_assert(sizeof(WarpNetSmem) % 16 == 0, "WarpNetSmem is copied in 16-byte words");
+
+__global__ void build_warp_net_kernel(const float *w) { load_warp_net(g_warp_net, w); }
+
+cudaError_t build_warp_net(const float *w, cudaStream_t s) {
+  build_warp_net_kernel<<<1, 256, 0, s>>>(w);
+  return cudaGetLastError();
+}
+
+// The image into a block's shared memory; blockDim.x == 128.
+__device__ __forceinline__ void copy_warp_net(WarpNetSmem &dst) {
+  constexpr int N16 = sizeof(WarpNetSmem) / 16;
+  const uint4 *src = reinterpret_cast<const uint4 *>(&g_warp_net);
+  uint4 *d = reinterpret_cast<uint4 *>(&dst);
+#pragma unroll
+  for (int k = 0; k < (N16 + 127) / 128; ++k) {
+    const int e = k * 128 + (int)threadIdx.x;
+    if (e < N16) d[e] = src[e];
+  }
+}
+
 // Element (row with inputs f, column k) of the first layer, relu'd.
 __device__ __forceinline__ float l1_unit(const WarpNetSmem &s, const float (&f)[3], int k) {
   const float4 l = s.l1[k];
@@ -108,9 +134,11 @@ __device__ __forceinline__ float l1_unit(const WarpNetSmem &s, const float (&f)[
 __device__ float warp_guess_eval(const WarpNetSmem &s, float f0, float f1, float f2) {
   const int lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
-  uint32_t a[2][4][4];  // [M tile][k step][fragment register]
+  float yp[4];  // rows gid, gid + 8, 16 + gid, 24 + gid
 #pragma unroll
   for (int mt = 0; mt < 2; ++mt) {
+    // the A fragments of rows mt*16 + gid and mt*16 + gid + 8, k = 0..63
+    uint32_t a[4][4];  // [k step][fragment register]
     float lo[3], hi[3];
     const int rlo = mt * 16 + gid, rhi = rlo + 8;
     lo[0] = __shfl_sync(0xffffffffu, f0, rlo);
@@ -122,31 +150,28 @@ __device__ float warp_guess_eval(const WarpNetSmem &s, float f0, float f1, float
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
       const int c = ks * 16 + tig * 2;
-      a[mt][ks][0] = bf16x2(l1_unit(s, lo, c), l1_unit(s, lo, c + 1));
-      a[mt][ks][1] = bf16x2(l1_unit(s, hi, c), l1_unit(s, hi, c + 1));
-      a[mt][ks][2] = bf16x2(l1_unit(s, lo, c + 8), l1_unit(s, lo, c + 9));
-      a[mt][ks][3] = bf16x2(l1_unit(s, hi, c + 8), l1_unit(s, hi, c + 9));
+      a[ks][0] = bf16x2(l1_unit(s, lo, c), l1_unit(s, lo, c + 1));
+      a[ks][1] = bf16x2(l1_unit(s, hi, c), l1_unit(s, hi, c + 1));
+      a[ks][2] = bf16x2(l1_unit(s, lo, c + 8), l1_unit(s, lo, c + 9));
+      a[ks][3] = bf16x2(l1_unit(s, hi, c + 8), l1_unit(s, hi, c + 9));
     }
-  }
-  float yp[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // rows gid, gid + 8, 16 + gid, 24 + gid
-  for (int nt = 0; nt < GUESS_H / 8; ++nt) {
-    float acc[2][4] = {{0.0f, 0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f, 0.0f}};
-    const int n = nt * 8 + gid;
+    float ylo = 0.0f, yhi = 0.0f;
+    for (int nt = 0; nt < GUESS_H / 8; ++nt) {
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      const int n = nt * 8 + gid;
 #pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      const int wd = ks * 8 + tig;
-      const uint32_t b0 = s.w2[swz(n, wd)], b1 = s.w2[swz(n, wd + 4)];
-      mma16816(acc[0], a[0][ks], b0, b1);
-      mma16816(acc[1], a[1][ks], b0, b1);
+      for (int ks = 0; ks < 4; ++ks) {
+        const int wd = ks * 8 + tig;
+        mma16816(acc, a[ks], s.w2[swz(n, wd)], s.w2[swz(n, wd + 4)]);
+      }
+      const int c = nt * 8 + tig * 2;
+      const float z0 = acc[0] + s.b2[c], z1 = acc[1] + s.b2[c + 1];
+      const float z2 = acc[2] + s.b2[c], z3 = acc[3] + s.b2[c + 1];
+      ylo += s.w3[c] * (z0 > 0.0f ? z0 : 0.0f) + s.w3[c + 1] * (z1 > 0.0f ? z1 : 0.0f);
+      yhi += s.w3[c] * (z2 > 0.0f ? z2 : 0.0f) + s.w3[c + 1] * (z3 > 0.0f ? z3 : 0.0f);
     }
-    const int c = nt * 8 + tig * 2;
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-      const float z0 = acc[mt][0] + s.b2[c], z1 = acc[mt][1] + s.b2[c + 1];
-      const float z2 = acc[mt][2] + s.b2[c], z3 = acc[mt][3] + s.b2[c + 1];
-      yp[2 * mt] += s.w3[c] * (z0 > 0.0f ? z0 : 0.0f) + s.w3[c + 1] * (z1 > 0.0f ? z1 : 0.0f);
-      yp[2 * mt + 1] += s.w3[c] * (z2 > 0.0f ? z2 : 0.0f) + s.w3[c + 1] * (z3 > 0.0f ? z3 : 0.0f);
-    }
+    yp[2 * mt] = ylo;
+    yp[2 * mt + 1] = yhi;
   }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -165,7 +190,7 @@ __device__ float warp_guess_eval(const WarpNetSmem &s, float f0, float f1, float
 template <typename T, int GRID, bool ICE, bool PSEUDO>
 __global__ void __launch_bounds__(128, 7) cape_learned_kernel(CapeArgs a) {
   __shared__ WarpNetSmem net;
-  load_warp_net(net, a.guess_w);
+  copy_warp_net(net);
   __syncthreads();
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = t < a.n2;
@@ -177,13 +202,10 @@ __global__ void __launch_bounds__(128, 7) cape_learned_kernel(CapeArgs a) {
   SourceSel sel;
   sel.kmax = 1;
   sel.mulvl = 0;
-  sel.avgth = sel.avgqv = 0.0;
+  sel.avgth = sel.avgqv = 0.0f;
   sel.ascend = false;
   float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
   if (active) {
-    const T *tin = (const T *)a.t + i * a.nk;
-    const T *tdin = (const T *)a.td + i * a.nk;
-    const T *pin = GRID == 2 ? (const T *)a.p : (const T *)a.p + i * a.nk;
     const float ts = ldf((const T *)a.ts + i);
     if (GRID != 1)
       start = a.start ? __ldg(a.start + i)
@@ -192,18 +214,16 @@ __global__ void __launch_bounds__(128, 7) cape_learned_kernel(CapeArgs a) {
       if (start < 1 || start > a.nk) {
         status = COL_BADSTART;
       } else {
-        col.p = pin;
-        col.t = tin;
-        col.td = tdin;
+        col.set((const T *)a.p, (const T *)a.t, (const T *)a.td,
+                i * (a.ld > 0 ? a.ld : a.nk), start);
         col.ps = ldf((const T *)a.ps + i);
         col.ts = ts;
         col.tds = ldf((const T *)a.tds + i);
-        col.base = start - 3;
         ncl = a.nk - start + 2;
-        sel = select_source(col, ncl, a.source, a.ml_depth);
+        sel = select_source<true>(col, ncl, a.source, a.ml_depth);
         if (sel.ascend) {
           float p0, t0, td0, q0;
-          source_parcel(col, sel, a.source, p0, t0, td0, q0);
+          source_parcel<true>(col, sel, a.source, p0, t0, td0, q0);
           lcl_features(p0, t0, td0, q0, f0, f1, f2);
           run = true;
         }

@@ -687,6 +687,9 @@ int xc_guess_set_weights(const float *weights, int on_device, void *stream) {
   e = cudaMemcpyToSymbolAsync(g_guess_w, weights, sizeof(float) * XC_GUESS_NPARAM, 0,
                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                               (cudaStream_t)stream);
+  void *gw = nullptr;
+  if (e == cudaSuccess) e = cudaGetSymbolAddress(&gw, g_guess_w);
+  if (e == cudaSuccess) e = xc::build_warp_net((const float *)gw, (cudaStream_t)stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "loading the guess network");
   std::lock_guard<std::mutex> lk(g_guess_mu);

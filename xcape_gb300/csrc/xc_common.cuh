@@ -95,6 +95,16 @@ XC_HD float fast_exp(float x) {
 #endif
 }
 
+// Approximate natural log: lg2.approx of x times ln 2 (3 ulp at most for x
+// outside [0.5, 2]).  logf on the host.
+XC_HD float fast_log(float x) {
+#if defined(__CUDA_ARCH__)
+  return __logf(x);
+#else
+  return logf(x);
+#endif
+}
+
 // getqvs / getqvi of the accelerated solvers: the same formulas with the
 // approximate exp and divides (the host build computes exactly what getqvs /
 // getqvi do), also returning the saturation vapour pressure es for the

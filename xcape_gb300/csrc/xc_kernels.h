@@ -41,6 +41,9 @@ cudaError_t launch_guess_eval(const float *w, const float *feats, long long n, f
                               cudaStream_t s);
 
 cudaError_t launch_cape(const CapeArgs &a, cudaStream_t s);
+// Rebuilds the learned kernel's shared-memory image of the guess network
+// from the parameters w (device) on this device (cape_kernel.cu).
+cudaError_t build_warp_net(const float *w, cudaStream_t s);
 cudaError_t launch_cape_diag(const CapeArgs &a, cudaStream_t s);  // cape_diag.cu
 
 // Column ordering (cape_kernel.cu): a counting sort of the columns by
