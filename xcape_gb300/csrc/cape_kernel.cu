@@ -106,14 +106,16 @@ cudaError_t build_warp_net(const float *w, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// The image into a block's shared memory; blockDim.x == 128.
+constexpr int LEARNED_THREADS = 128;  // the learned kernel's block size
+
+// The image into a block's shared memory, by the LEARNED_THREADS threads.
 __device__ __forceinline__ void copy_warp_net(WarpNetSmem &dst) {
   constexpr int N16 = sizeof(WarpNetSmem) / 16;
   const uint4 *src = reinterpret_cast<const uint4 *>(&g_warp_net);
   uint4 *d = reinterpret_cast<uint4 *>(&dst);
 #pragma unroll
-  for (int k = 0; k < (N16 + 127) / 128; ++k) {
-    const int e = k * 128 + (int)threadIdx.x;
+  for (int k = 0; k < (N16 + LEARNED_THREADS - 1) / LEARNED_THREADS; ++k) {
+    const int e = k * LEARNED_THREADS + (int)threadIdx.x;
     if (e < N16) d[e] = src[e];
   }
 }
@@ -187,60 +189,91 @@ __device__ float warp_guess_eval(const WarpNetSmem &s, float f0, float f1, float
   return (j == 0 ? v0 : j == 1 ? v1 : j == 2 ? v2 : v3) + s.b3;
 }
 
+// What phases 1 and 2 hand to phase 3, per thread, through shared memory:
+// nothing of the source selection or the network stays live in registers
+// across the network's evaluation or the ascent.
+struct LearnedPrep {
+  int start, kmax, mulvl, status;  // status: COL_* bits, or PREP_RUN when the ascent runs
+  float avgth, avgqv, y, pad;
+};
+constexpr int PREP_RUN = 1 << 30;
+
 template <typename T, int GRID, bool ICE, bool PSEUDO>
-__global__ void __launch_bounds__(128, 7) cape_learned_kernel(CapeArgs a) {
+__global__ void __launch_bounds__(LEARNED_THREADS, 7) cape_learned_kernel(CapeArgs a) {
   __shared__ WarpNetSmem net;
+  __shared__ LearnedPrep prep[LEARNED_THREADS];
   copy_warp_net(net);
   __syncthreads();
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = t < a.n2;
   const long long i = active ? (a.perm ? (long long)__ldg(a.perm + t) : t) : 0;
-  // phase 1: the column's start, gate and source (cape_column_run, getcape_col)
-  ColumnReader<T, GRID> col;
-  int ncl = 0, start = 1, status = 0;
-  bool run = false;
-  SourceSel sel;
-  sel.kmax = 1;
-  sel.mulvl = 0;
-  sel.avgth = sel.avgqv = 0.0f;
-  sel.ascend = false;
-  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
-  if (active) {
-    const float ts = ldf((const T *)a.ts + i);
-    if (GRID != 1)
-      start = a.start ? __ldg(a.start + i)
-                      : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
-    if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
-      if (start < 1 || start > a.nk) {
-        status = COL_BADSTART;
-      } else {
-        col.set((const T *)a.p, (const T *)a.t, (const T *)a.td,
-                i * (a.ld > 0 ? a.ld : a.nk), start);
-        col.ps = ldf((const T *)a.ps + i);
-        col.ts = ts;
-        col.tds = ldf((const T *)a.tds + i);
-        ncl = a.nk - start + 2;
-        sel = select_source<true>(col, ncl, a.source, a.ml_depth);
-        if (sel.ascend) {
-          float p0, t0, td0, q0;
-          source_parcel<true>(col, sel, a.source, p0, t0, td0, q0);
-          lcl_features(p0, t0, td0, q0, f0, f1, f2);
-          run = true;
+  const long long stride = a.ld > 0 ? a.ld : a.nk;
+  {
+    // phase 1: the column's start, gate and source (cape_column_run, getcape_col)
+    int start = 1, status = 0;
+    SourceSel sel;
+    sel.kmax = 1;
+    sel.mulvl = 0;
+    sel.avgth = sel.avgqv = 0.0f;
+    sel.ascend = false;
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
+    if (active) {
+      const float ts = ldf((const T *)a.ts + i);
+      if (GRID != 1)
+        start = a.start ? __ldg(a.start + i)
+                        : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
+      if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
+        if (start < 1 || start > a.nk) {
+          status = COL_BADSTART;
+        } else {
+          ColumnReader<T, GRID> col;
+          col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
+          col.ps = ldf((const T *)a.ps + i);
+          col.ts = ts;
+          col.tds = ldf((const T *)a.tds + i);
+          sel = select_source<true>(col, a.nk - start + 2, a.source, a.ml_depth);
+          if (sel.ascend) {
+            float p0, t0, td0, q0;
+            source_parcel<true>(col, sel, a.source, p0, t0, td0, q0);
+            lcl_features(p0, t0, td0, q0, f0, f1, f2);
+            status = PREP_RUN;
+          }
         }
       }
     }
+    // phase 2: the network for the warp's 32 columns
+    __syncwarp();
+    const float y = warp_guess_eval(net, f0, f1, f2);
+    LearnedPrep &q = prep[threadIdx.x];
+    q.start = start;
+    q.kmax = sel.kmax;
+    q.mulvl = sel.mulvl;
+    q.status = status;
+    q.avgth = sel.avgth;
+    q.avgqv = sel.avgqv;
+    q.y = y;
   }
-  // phase 2: the network for the warp's 32 columns
   __syncwarp();
-  const float y = warp_guess_eval(net, f0, f1, f2);
   // phase 3: the ascent
+  const LearnedPrep q = prep[threadIdx.x];
   float cape = 0.0f, cin = 0.0f, zo = 0.0f;
-  int mulvl = 0, nsub = 0, niter = 0;
+  int mulvl = 0, status = q.status & ~PREP_RUN, nsub = 0, niter = 0;
   if (active && status == 0 && ldf((const T *)a.ts + i) > 0.0f) {
+    SourceSel sel;
+    sel.kmax = q.kmax;
+    sel.mulvl = q.mulvl;
+    sel.avgth = q.avgth;
+    sel.avgqv = q.avgqv;
+    sel.ascend = true;
     CapeResult r;
-    if (run) {
-      r = ascend_col<ICE, PSEUDO, SOLVE_LEARNED, false>(col, ncl, a.pinc, a.source, sel, nullptr,
-                                                        nullptr, y);
+    if (q.status & PREP_RUN) {
+      ColumnReader<T, GRID> col;
+      col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, q.start);
+      col.ps = ldf((const T *)a.ps + i);
+      col.ts = ldf((const T *)a.ts + i);
+      col.tds = ldf((const T *)a.tds + i);
+      r = ascend_col<ICE, PSEUDO, SOLVE_LEARNED, false>(col, a.nk - q.start + 2, a.pinc, a.source,
+                                                        sel, nullptr, nullptr, q.y);
     } else {
       r.mulvl = sel.mulvl;
       r.z_out = -999999.f;
@@ -422,7 +455,9 @@ static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaS
 }
 
 template <typename T, int GRID>
-static void launch_learned(const CapeArgs &a, unsigned blocks, int threads, cudaStream_t s) {
+static void launch_learned(const CapeArgs &a, cudaStream_t s) {
+  const int threads = LEARNED_THREADS;
+  const unsigned blocks = (unsigned)((a.n2 + threads - 1) / threads);
   const bool ice = a.adiabat >= 3;
   const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
   if (ice && pseudo) cape_learned_kernel<T, GRID, true, true><<<blocks, threads, 0, s>>>(a);
@@ -441,7 +476,7 @@ static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
   if (blocks == 0) return cudaSuccess;
   switch (a.guess) {
     case 0: launch_cape_s<T, GRID, SOLVE_PLAIN>(a, blocks, threads, s); break;
-    case 1: launch_learned<T, GRID>(a, blocks, threads, s); break;
+    case 1: launch_learned<T, GRID>(a, s); break;
     case 2: launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s); break;
     case 3: launch_cape_s<T, GRID, SOLVE_SECANT>(a, blocks, threads, s); break;
     default: launch_cape_s<T, GRID, SOLVE_LEARNED_ALL>(a, blocks, threads, s); break;
