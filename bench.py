@@ -43,14 +43,14 @@ SRH_METRIC = "SRH columns/s at 1M×50 lev (calc_srh, depth 1000+3000 m)"
 CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
 # DRAM bytes (read + write) of one most-unstable launch of the lift on this
 # workload, from `ncu --set full` captures of `bench.py --profile`.
-NCU_TRAFFIC = {"learned": 787_232_256, "plain": 725_900_000}
+NCU_TRAFFIC = {"learned": 703_298_304, "plain": 725_548_288}
 # The lift is bound by the SM issue rate, not by HBM: issue-slot activity of
 # the same captures (smsp__issue_active, % of peak over active cycles) and the
 # tensor pipe's share (the learned kernel's guess network).
-NCU_ISSUE = {"learned": {"issue_active": 0.860, "tensor_pipe_active": 0.0052,
-                         "threads_per_warp_instruction": 25.76},
-             "plain": {"issue_active": 0.892, "tensor_pipe_active": 0.0,
-                       "threads_per_warp_instruction": 27.12}}
+NCU_ISSUE = {"learned": {"issue_active": 0.867, "tensor_pipe_active": 0.0070,
+                         "threads_per_warp_instruction": 29.15},
+             "plain": {"issue_active": 0.878, "tensor_pipe_active": 0.0,
+                       "threads_per_warp_instruction": 27.11}}
 ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg
 CPU_SAMPLE_1T = 8192     # columns per single-core CPU-baseline measurement
 REF_SAMPLE = 32768       # columns per --impl reference step
@@ -601,6 +601,7 @@ def run_serve(args):
             b.run([descriptor(b, r) for r in trace[:8]])
             torch.cuda.synchronize()
             lat, batches, busy, cols, nxt = [], [], 0.0, 0, 0
+            slowest = (0.0, 0, 0)  # the longest batch: seconds, requests, columns
             t0 = time.perf_counter()
             while nxt < len(trace):
                 now = time.perf_counter() - t0
@@ -627,7 +628,10 @@ def run_serve(args):
                     off += n
                 stream.synchronize()
                 done = time.perf_counter() - t0
-                busy += time.perf_counter() - tb
+                dt = time.perf_counter() - tb
+                busy += dt
+                if dt > slowest[0]:
+                    slowest = (dt, len(take), sum(r["n2"] for r in take))
                 batches.append(len(take))
                 cols += sum(r["n2"] for r in take)
                 lat += [done - r["arrival"] for r in take]
@@ -639,6 +643,8 @@ def run_serve(args):
                 "p50_ms": float(np.percentile(lat_ms, 50)),
                 "p99_ms": float(np.percentile(lat_ms, 99)),
                 "max_ms": float(lat_ms.max()), "batches": len(batches),
+                "slowest_batch": {"ms": slowest[0] * 1e3, "requests": slowest[1],
+                                  "columns": slowest[2]},
                 "mean_requests_per_batch": float(np.mean(batches)),
                 "graph_launches": len(batches)}
 
