@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--guess", default="learned",
                     choices=["plain", "extrapolated", "learned", "secant", "learned-every"])
-    ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve", "adiabats"])
+    ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve", "adiabats", "cape_srh"])
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the request trace of --workload serve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -527,6 +527,94 @@ def run_srh(args):
     return 0
 
 
+CAPE_SRH_METRIC = "calc_cape + calc_srh columns/s at 1M×50 lev: xc_cape_srh vs two calls"
+
+
+def run_cape_srh(args):
+    """--workload cape_srh: CAPE (most-unstable, pseudo-liquid) and SRH (depth
+    3000 m, output_var='all') of the same 1024x1024 columns x 50 model levels,
+    device-resident: xc_cape_srh (one kernel) against xc_loopcape_ex followed
+    by xc_calc_srh_ex, for the plain and learned solvers and both SRH
+    precisions.  Both paths order the columns for the lift."""
+    import torch
+    from xcape_gb300 import _lib, guess as G
+    from xcape_gb300 import synthetic as S
+    L = _lib.lib()
+    G.ensure_loaded()
+    a = S.srh_c2()
+    n2, nk = 1024 * 1024, 50
+    p, t, td, u, v, ps, ts, tds, us, vs = (torch.from_numpy(np.ascontiguousarray(x)).cuda()
+                                           for x in a)
+    cape, cin, zo = (torch.empty(n2, device="cuda") for _ in range(3))
+    mul = torch.empty(n2, dtype=torch.int32, device="cuda")
+    srm, slm = (torch.empty(n2, dtype=torch.float64, device="cuda") for _ in range(2))
+    rm, lm, mean = (torch.empty(2 * n2, dtype=torch.float32, device="cuda") for _ in range(3))
+    wsb = _lib.workspace_bytes(n2)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    lev = [x.data_ptr() for x in (p, t, td)]
+    sfc = [x.data_ptr() for x in (ps, ts, tds)]
+    outs_c = [x.data_ptr() for x in (cape, cin, mul, zo)]
+    outs_s = [x.data_ptr() for x in (srm, slm, rm, lm, mean)]
+    src, adi, depth = 2, 1, 3000.0
+
+    def separate(g, prec):
+        _lib.check(L.xc_loopcape_ex(1, *lev, *sfc, _lib.XC_F32, PINC, src, ML_DEPTH, adi, None, nk,
+                                    n2, g, *outs_c, None, None, ws.data_ptr(), wsb, st))
+        _lib.check(L.xc_calc_srh_ex(1, *lev, u.data_ptr(), v.data_ptr(), *sfc, us.data_ptr(),
+                                    vs.data_ptr(), _lib.XC_F32, None, depth, 2.0, nk, n2, prec,
+                                    *outs_s, st))
+
+    def fused(g, prec):
+        _lib.check(L.xc_cape_srh(1, *lev, u.data_ptr(), v.data_ptr(), *sfc, us.data_ptr(),
+                                 vs.data_ptr(), _lib.XC_F32, PINC, src, ML_DEPTH, adi, None,
+                                 depth, 2.0, nk, n2, g, prec, *outs_c, None, *outs_s,
+                                 ws.data_ptr(), wsb, st))
+
+    def timed(fn, g, prec):
+        for _ in range(max(3, args.warmup)):
+            fn(g, prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn(g, prec)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    if args.profile:
+        # one launch of each schedule, plain solver and reference SRH stages
+        # (the fused kernel's case), for ncu
+        separate(_lib.XC_GUESS_PLAIN, 0)
+        fused(_lib.XC_GUESS_PLAIN, 0)
+        torch.cuda.synchronize()
+        return 0
+    res = {}
+    with ClockSampler(0) as clk:
+        for gname, g in (("learned", _lib.XC_GUESS_LEARNED), ("plain", _lib.XC_GUESS_PLAIN)):
+            for pname, prec in (("fp32", 1), ("reference", 0)):
+                ms_s = timed(separate, g, prec)
+                ms_f = timed(fused, g, prec)
+                res[f"{gname}/{pname}"] = {
+                    "separate_ms": ms_s, "xc_cape_srh_ms": ms_f, "speedup": ms_s / ms_f,
+                    "schedule": "two kernels" if (gname, pname) == ("learned", "fp32")
+                    else "fused kernel"}
+    head = res["learned/reference"]
+    line = {"metric": CAPE_SRH_METRIC, "value": n2 / (head["xc_cape_srh_ms"] / 1e3),
+            "unit": "columns/s", "n_gpus": 1, "steps": args.steps,
+            "ms_per_step": head["xc_cape_srh_ms"], "dtype": "f32 (SRH stages f64)",
+            "higher_is_better": True, "data": "synthetic", "workload": "cape_srh",
+            "config": {"workload": "calc_cape (most-unstable, pseudo-liquid, pinc 500 Pa) and "
+                                   "calc_srh (depth 3000 m, output_var='all') of 1024x1024 cols "
+                                   "x 50 model levels, device-resident, columns ordered",
+                       "headline": "learned solver, SRH precision 'reference' (calc_srh's "
+                                   "default)"},
+            "per_mode": res, "gpu_launches": 4 * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 SERVE_METRIC = "calc_cape serving loop: p50/p99 latency and columns/s, learned vs plain"
 SERVE_RATE = 200.0        # requests per second (Poisson)
 SERVE_POOL = 1 << 20      # columns of each device-resident input pool
@@ -777,6 +865,8 @@ def main():
         return run_serve(args)
     if args.workload == "adiabats":
         return run_adiabats(args)
+    if args.workload == "cape_srh":
+        return run_cape_srh(args)
     return run_ours(args)
 
 

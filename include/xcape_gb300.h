@@ -228,6 +228,32 @@ int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
                      int precision, double *srh_rm, double *srh_lm, float *rm, float *lm,
                      float *mean6, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* CAPE and SRH of the same columns in one pass                            */
+/* ---------------------------------------------------------------------- */
+
+/* xc_loopcape_ex and xc_calc_srh_ex on the same columns in one kernel: the
+ * FP32 lift (CAPE/CIN) and the SRH chain, whose FP64 stages then run on the
+ * FP64 pipe while other warps lift.  No counterpart in the reference, which
+ * computes the two with separate f2py chains over the same inputs
+ * (src/xcape/core.py:261-332 and :473-542); the results are those of the
+ * two separate calls.  Device pointers.
+ * grid: 1 (sigma, p [n2][nk]) or 2 (pressure, shared p [nk], start_3d
+ * optional).  CAPE options and outputs as xc_loopcape_ex, with guess
+ * XC_GUESS_PLAIN or XC_GUESS_LEARNED; depth, aglh0, precision and the SRH
+ * outputs as xc_calc_srh_ex.  workspace (nullable, as xc_loopcape_ex)
+ * orders the columns for the lift.  With guess XC_GUESS_LEARNED, precision
+ * XC_SRH_FP32 and f32 inputs the call runs the two kernels back to back
+ * instead, which is faster there (the SRH kernel's rows are read coalesced
+ * through shared memory). */
+int xc_cape_srh(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
+                const void *v3d, const void *ps, const void *ts, const void *tds, const void *us,
+                const void *vs, int dtype, float pinc, int source, float ml_depth, int adiabat,
+                const int *start_3d, double depth, double aglh0, int nk, int n2, int guess,
+                int precision, float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                double *srh_rm, double *srh_lm, float *rm, float *lm, float *mean6,
+                void *workspace, size_t workspace_bytes, void *stream);
+
 /* Replaces loop_stdheight_ml: stdheight_2D_model_lev.pyf:6-19,
  * stdheight_2D_model_lev.f90:4-34 (+ stdheight_ml :74-160).  All f64. */
 int xc_loop_stdheight_ml(const double *P, const double *T, const double *Td, const double *Ps,

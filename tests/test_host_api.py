@@ -142,6 +142,33 @@ def test_invalid_arguments_return_status_without_gpu():
     assert rc == _lib.XC_ERR_INVALID
 
 
+def test_cape_srh_arguments_are_checked_before_any_cuda_call(p_t_td_3d, p_t_td_surface):
+    """xc_cape_srh rejects what neither of its halves can run, with no GPU."""
+    L = _lib.lib()
+    null = None
+
+    def call(grid=1, guess=0, precision=0, n2=4, rm=None, source=1):
+        return L.xc_cape_srh(grid, *([null] * 10), 0, 500.0, source, 500.0, 1, null, 3000.0,
+                             2.0, 10, n2, guess, precision, *([null] * 5), null, null, rm,
+                             null, null, null, 0, null)
+    assert call(grid=3) == _lib.XC_ERR_INVALID and b"grid" in L.xc_last_error()
+    assert call(guess=_lib.XC_GUESS_EXTRAPOLATED) == _lib.XC_ERR_INVALID
+    assert b"guess" in L.xc_last_error()
+    assert call(precision=7) == _lib.XC_ERR_INVALID and b"precision" in L.xc_last_error()
+    assert call(rm=ctypes.c_void_p(16)) == _lib.XC_ERR_INVALID
+    assert call(source=5) == _lib.XC_ERR_INVALID and b"source" in L.xc_last_error()
+    assert call(n2=0) == _lib.XC_OK
+    assert call() == _lib.XC_ERR_INVALID and b"NULL" in L.xc_last_error()
+    p, t, td = p_t_td_3d
+    ps, ts, tds = p_t_td_surface
+    with pytest.raises(ValueError, match="guess"):
+        X.calc_cape_srh(p, t, td, t, td, ps, ts, tds, ps, ts, guess="secant")
+    with pytest.raises(ValueError, match="P should be 1d"):
+        X.calc_cape_srh(p, t, td, t, td, ps, ts, tds, ps, ts, vertical_lev="pressure")
+    with pytest.raises(ValueError, match="precision"):
+        X.calc_cape_srh(p, t, td, t, td, ps, ts, tds, ps, ts, precision="fp16")
+
+
 def test_python_raises_library_errors():
     with pytest.raises(_lib.XcapeError, match="status 1"):
         _lib.call("xc_loopcape_ml", None, None, None, None, None, None, 0, 500.0, 4, 500.0, 1,

@@ -57,6 +57,8 @@ SIGNATURES = {
     "xc_calc_srh": [_i] + [_vp] * 10 + [_i, _vp, _d, _d, _i, _i] + [_vp] * 5 + [_vp],
     "xc_calc_srh_ex": [_i] + [_vp] * 10 + [_i, _vp, _d, _d, _i, _i, _i] + [_vp] * 5 + [_vp],
     "xc_calc_srh_host": [_i] + [_vp] * 10 + [_i, _vp, _d, _d, _i, _i, _i] + [_vp] * 5 + [_vp],
+    "xc_cape_srh": [_i] + [_vp] * 10 + [_i, _f, _i, _f, _i, _vp, _d, _d, _i, _i, _i, _i]
+    + [_vp] * 10 + [_vp, ctypes.c_size_t, _vp],
     "xc_loop_stdheight_ml": [_vp] * 7 + [_i, _i, _vp, _vp, _vp],
     "xc_loop_stdheight_pl1d": [_vp] * 7 + [_vp, _i, _i, _vp, _vp, _vp],
     "xc_loop_stdheight_pl": [_vp] * 7 + [_vp, _i, _i, _vp, _vp, _vp],

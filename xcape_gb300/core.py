@@ -17,6 +17,8 @@ tests (test/test_core.py:22-26, 77-82).  ``vertical_lev`` accepts
 ``p`` shared by all columns; levels below the surface are skipped per column
 with the reference's ``pres_lev_pos`` rule, evaluated on the GPU).
 
+``calc_cape_srh`` computes both for the same columns in one pass.
+
 Methods:
 
 * ``'cuda'`` -- the GB300 kernels of ``libxcape_gb300.so``.  numpy inputs go
@@ -432,6 +434,89 @@ def _calc_srh_numpy(*args, depth=3000, vertical_lev="sigma", output_var="srh", m
     if not b.torch:
         res = [np.ascontiguousarray(r) for r in res]
     return tuple(res)
+
+
+# ---------------------------------------------------------------------------
+# CAPE and SRH of the same columns
+
+
+def calc_cape_srh(p, t, td, u, v, ps, ts, tds, us, vs, source="surface", ml_depth=500.0,
+                  adiabat="pseudo-liquid", pinc=500.0, depth=3000, vertical_lev="sigma",
+                  output_var="srh", guess="plain", precision="reference"):
+    """``calc_cape(p, t, td, ps, ts, tds, ...)`` and ``calc_srh(p, t, td, u, v,
+    ps, ts, tds, us, vs, ...)`` on the same columns in one kernel on the GPU:
+    the FP32 lift and the SRH chain's FP64 stages run on different pipes at
+    once, so with ``precision='reference'`` the pair takes about as long as
+    calc_srh alone.  The reference computes the two separately
+    (src/xcape/core.py:261-332, :473-542); the results are those of the two
+    calls.
+
+    Arguments as the two functions (numpy arrays, or CUDA tensors used in
+    place); ``guess`` is ``'plain'`` or ``'learned'``; ``vertical_lev`` is
+    ``'sigma'``/``'model'`` or ``'pressure'``.  Returns ``(cape_result,
+    srh_result)``: the tuples ``calc_cape`` and ``calc_srh`` return.
+    """
+    src = _option(_SOURCE, source, "source")
+    adi = _option(_ADIABAT, adiabat, "adiabat")
+    vl = _option(_VERTICAL, vertical_lev, "vertical_lev")
+    out = _option(_OUTPUT, output_var, "output_var")
+    prec = _option(_SRH_PRECISION, precision, "precision")
+    gs = _option(_GUESS, guess, "guess")
+    if gs not in (_lib.XC_GUESS_PLAIN, _lib.XC_GUESS_LEARNED):
+        raise ValueError("calc_cape_srh: guess must be 'plain' or 'learned'")
+    shape = tuple(t.shape)
+    _check_same([t, td, u, v])
+    _check_same([ps, ts, tds, us, vs])
+    if len(p.shape) == 1 and vl == _lib.GRID_PRESSURE_1D:
+        grid = _lib.GRID_PRESSURE_1D
+        if p.shape[0] != shape[-1]:
+            raise ValueError("1-D p must have one value per level of t")
+    elif tuple(p.shape) == shape and vl == _lib.GRID_SIGMA:
+        grid = _lib.GRID_SIGMA
+    elif tuple(p.shape) == shape and vl == _lib.GRID_PRESSURE_1D:
+        raise ValueError("P should be 1d")
+    else:
+        raise ValueError("Input arrays must have the same shape.")
+    if _prod(tuple(ps.shape)) != _prod(shape[:-1]):
+        raise ValueError("Surface arrays must have one value per column.")
+    if gs == _lib.XC_GUESS_LEARNED:
+        from . import guess as _guess
+        _guess.ensure_loaded()
+    import torch
+    host = not any(_is_torch(a) for a in (p, t, td, u, v, ps, ts, tds, us, vs))
+    if host:
+        p, t, td, u, v, ps, ts, tds, us, vs = (
+            torch.from_numpy(np.ascontiguousarray(a)).cuda()
+            for a in (p, t, td, u, v, ps, ts, tds, us, vs))
+    b = _Batch([t, td, u, v], [ps, ts, tds, us, vs], p, grid)
+    cape, cin, zout = (b.empty(b.n2, "f4") for _ in range(3))
+    mulvl = b.empty(b.n2, "i4")
+    srm, slm = b.empty(b.n2, "f8"), b.empty(b.n2, "f8")
+    if out == 2:
+        rm, lm, mean = (b.empty(2 * b.n2, "f4") for _ in range(3))
+    else:
+        rm = lm = mean = None
+    lv, sf = b.levels, b.surface
+    ws, ws_bytes = b.workspace(_lib.workspace_bytes(b.n2))
+    _lib.call("xc_cape_srh", grid, b.ptr(b.p), b.ptr(lv[0]), b.ptr(lv[1]), b.ptr(lv[2]),
+              b.ptr(lv[3]), b.ptr(sf[0]), b.ptr(sf[1]), b.ptr(sf[2]), b.ptr(sf[3]),
+              b.ptr(sf[4]), b.dtype, float(pinc), src, float(ml_depth), adi, None,
+              float(depth), 2.0, b.nk, b.n2, gs, prec, b.ptr(cape), b.ptr(cin), b.ptr(mulvl),
+              b.ptr(zout), None, b.ptr(srm), b.ptr(slm), b.ptr(rm), b.ptr(lm), b.ptr(mean),
+              ws, ws_bytes, b.stream)
+    shp = _out_shape(shape)
+    cape_res = [cape.reshape(shp), cin.reshape(shp)]
+    if src == 2:
+        cape_res += [mulvl.reshape(shp), zout.reshape(shp)]
+    srh_res = [srm.reshape(shp), slm.reshape(shp)]
+    if out == 2:
+        for a in (rm, lm, mean):
+            a2 = a.reshape(b.n2, 2)
+            srh_res += [a2[:, 0].reshape(shp), a2[:, 1].reshape(shp)]
+    if host:
+        cape_res = [r.cpu().numpy() for r in cape_res]
+        srh_res = [np.ascontiguousarray(r.cpu().numpy()) for r in srh_res]
+    return tuple(cape_res), tuple(srh_res)
 
 
 # ---------------------------------------------------------------------------

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "cape_column.cuh"
+#include "cape_learned.cuh"
 #include "xc_kernels.h"
 
 namespace xc {
@@ -41,63 +42,11 @@ __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
   }
 }
 
-// ---- the learned solver: the guess network on the tensor cores, per warp ----
-//
-// cape_learned_kernel (7 resident blocks of 128 threads per SM, 72
-// registers, 9.7 KB of shared memory: the weights only, the activations stay
-// in registers) runs each column in three phases: (1) every lane selects
-// its parcel's source and forms the network's inputs at the parcel's LCL;
-// (2) the warp, converged (__syncwarp), evaluates the network for its 32
-// columns at once -- the 64x64 hidden layer as 2 x 8 x 4 mma.sync.m16n8k16
-// (BF16 operands, FP32 accumulation, as in training); (3) every lane runs
-// the ascent with that output (ascend_col).  No lane leaves before phase 2:
-// lanes without a column (past n2, ts <= 0, bad start, no ascent) take part
-// with zero inputs and discard the result.
-struct WarpNetSmem {
-  float4 l1[GUESS_H];                               // {W1[k][0..2], b1[k]}
-  float b2[GUESS_H], w3[GUESS_H], b3;
-  alignas(16) uint32_t w2[GUESS_H * GUESS_H / 2];   // W2 as bf16 pairs, swizzled rows
-};
-
-// 32-bit word w (a bf16 pair) of 64-wide row r, XOR-swizzled so that the
-// fragment loads of 8 consecutive rows hit 8 different bank groups.
-__device__ __forceinline__ int swz(int r, int w) { return r * 32 + (w ^ ((r & 7) << 2)); }
-
-__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<uint32_t *>(&v);
-}
-
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
-                                         uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ void load_warp_net(WarpNetSmem &s, const float *w) {
-  for (int k = threadIdx.x; k < GUESS_H; k += blockDim.x) {
-    s.l1[k] = make_float4(w[GUESS_OFF_W1 + 3 * k], w[GUESS_OFF_W1 + 3 * k + 1],
-                          w[GUESS_OFF_W1 + 3 * k + 2], w[GUESS_OFF_B1 + k]);
-    s.b2[k] = w[GUESS_OFF_B2 + k];
-    s.w3[k] = w[GUESS_OFF_W3 + k];
-  }
-  if (threadIdx.x == 0) s.b3 = w[GUESS_OFF_B3];
-  for (int e = threadIdx.x; e < GUESS_H * GUESS_H / 2; e += blockDim.x) {
-    const int n = e / (GUESS_H / 2), wd = e % (GUESS_H / 2);
-    s.w2[swz(n, wd)] = bf16x2(w[GUESS_OFF_W2 + n * GUESS_H + 2 * wd],
-                              w[GUESS_OFF_W2 + n * GUESS_H + 2 * wd + 1]);
-  }
-}
-
 // The shared-memory image of the guess network on this device, built from
 // the parameters once per xc_guess_set_weights (build_warp_net), so that a
 // block of the learned kernel copies 9.7 KB with 16-byte loads instead of
 // converting and swizzling W2 from FP32 parameters.
 __device__ WarpNetSmem g_warp_net;
-static_assert(sizeof(WarpNetSmem) % 16 == 0, "WarpNetSmem is copied in 16-byte words");
 
 __global__ void build_warp_net_kernel(const float *w) { load_warp_net(g_warp_net, w); }
 
@@ -106,198 +55,23 @@ cudaError_t build_warp_net(const float *w, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-constexpr int LEARNED_THREADS = 128;  // the learned kernel's block size
-
-// The image into a block's shared memory, by the LEARNED_THREADS threads.
-__device__ __forceinline__ void copy_warp_net(WarpNetSmem &dst) {
-  constexpr int N16 = sizeof(WarpNetSmem) / 16;
-  const uint4 *src = reinterpret_cast<const uint4 *>(&g_warp_net);
-  uint4 *d = reinterpret_cast<uint4 *>(&dst);
-#pragma unroll
-  for (int k = 0; k < (N16 + LEARNED_THREADS - 1) / LEARNED_THREADS; ++k) {
-    const int e = k * LEARNED_THREADS + (int)threadIdx.x;
-    if (e < N16) d[e] = src[e];
-  }
+cudaError_t warp_net_image(const void **out) {
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_warp_net);
+  *out = p;
+  return e;
 }
 
-// Element (row with inputs f, column k) of the first layer, relu'd.
-__device__ __forceinline__ float l1_unit(const WarpNetSmem &s, const float (&f)[3], int k) {
-  const float4 l = s.l1[k];
-  const float h = l.w + l.x * f[0] + l.y * f[1] + l.z * f[2];
-  return h > 0.0f ? h : 0.0f;
-}
-
-// The network's output for the calling lane's inputs; all 32 lanes of the
-// warp must call it together.  Rows of the hidden-layer product are the
-// warp's lanes; each lane builds the A fragments it holds (rows gid,
-// gid + 8, 16 + gid, 24 + gid of the 32 x 64 activation matrix, fetched as
-// inputs by shuffle) in registers, so no activation tile goes through
-// shared memory.
-__device__ float warp_guess_eval(const WarpNetSmem &s, float f0, float f1, float f2) {
-  const int lane = threadIdx.x & 31;
-  const int gid = lane >> 2, tig = lane & 3;
-  float yp[4];  // rows gid, gid + 8, 16 + gid, 24 + gid
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt) {
-    // the A fragments of rows mt*16 + gid and mt*16 + gid + 8, k = 0..63
-    uint32_t a[4][4];  // [k step][fragment register]
-    float lo[3], hi[3];
-    const int rlo = mt * 16 + gid, rhi = rlo + 8;
-    lo[0] = __shfl_sync(0xffffffffu, f0, rlo);
-    lo[1] = __shfl_sync(0xffffffffu, f1, rlo);
-    lo[2] = __shfl_sync(0xffffffffu, f2, rlo);
-    hi[0] = __shfl_sync(0xffffffffu, f0, rhi);
-    hi[1] = __shfl_sync(0xffffffffu, f1, rhi);
-    hi[2] = __shfl_sync(0xffffffffu, f2, rhi);
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-      const int c = ks * 16 + tig * 2;
-      a[ks][0] = bf16x2(l1_unit(s, lo, c), l1_unit(s, lo, c + 1));
-      a[ks][1] = bf16x2(l1_unit(s, hi, c), l1_unit(s, hi, c + 1));
-      a[ks][2] = bf16x2(l1_unit(s, lo, c + 8), l1_unit(s, lo, c + 9));
-      a[ks][3] = bf16x2(l1_unit(s, hi, c + 8), l1_unit(s, hi, c + 9));
-    }
-    float ylo = 0.0f, yhi = 0.0f;
-    for (int nt = 0; nt < GUESS_H / 8; ++nt) {
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      const int n = nt * 8 + gid;
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-        const int wd = ks * 8 + tig;
-        mma16816(acc, a[ks], s.w2[swz(n, wd)], s.w2[swz(n, wd + 4)]);
-      }
-      const int c = nt * 8 + tig * 2;
-      const float z0 = acc[0] + s.b2[c], z1 = acc[1] + s.b2[c + 1];
-      const float z2 = acc[2] + s.b2[c], z3 = acc[3] + s.b2[c + 1];
-      ylo += s.w3[c] * (z0 > 0.0f ? z0 : 0.0f) + s.w3[c + 1] * (z1 > 0.0f ? z1 : 0.0f);
-      yhi += s.w3[c] * (z2 > 0.0f ? z2 : 0.0f) + s.w3[c + 1] * (z3 > 0.0f ? z3 : 0.0f);
-    }
-    yp[2 * mt] = ylo;
-    yp[2 * mt + 1] = yhi;
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    yp[j] += __shfl_xor_sync(0xffffffffu, yp[j], 1);
-    yp[j] += __shfl_xor_sync(0xffffffffu, yp[j], 2);
-  }
-  // row `lane` is held (whole) by the lanes of quad (lane & 7), in yp[j]
-  const int src = (lane & 7) * 4, j = ((lane >> 4) << 1) | ((lane >> 3) & 1);
-  const float v0 = __shfl_sync(0xffffffffu, yp[0], src);
-  const float v1 = __shfl_sync(0xffffffffu, yp[1], src);
-  const float v2 = __shfl_sync(0xffffffffu, yp[2], src);
-  const float v3 = __shfl_sync(0xffffffffu, yp[3], src);
-  return (j == 0 ? v0 : j == 1 ? v1 : j == 2 ? v2 : v3) + s.b3;
-}
-
-// What phases 1 and 2 hand to phase 3, per thread, through shared memory:
-// nothing of the source selection or the network stays live in registers
-// across the network's evaluation or the ascent.
-struct LearnedPrep {
-  int start, kmax, mulvl, status;  // status: COL_* bits, or PREP_RUN when the ascent runs
-  float avgth, avgqv, y, pad;
-};
-constexpr int PREP_RUN = 1 << 30;
-
+// The learned solver (cape_learned.cuh): 7 resident blocks of 128 threads per SM.
 template <typename T, int GRID, bool ICE, bool PSEUDO>
 __global__ void __launch_bounds__(LEARNED_THREADS, 7) cape_learned_kernel(CapeArgs a) {
   __shared__ WarpNetSmem net;
   __shared__ LearnedPrep prep[LEARNED_THREADS];
-  copy_warp_net(net);
+  copy_warp_net(net, &g_warp_net);
   __syncthreads();
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = t < a.n2;
-  const long long i = active ? (a.perm ? (long long)__ldg(a.perm + t) : t) : 0;
-  const long long stride = a.ld > 0 ? a.ld : a.nk;
-  {
-    // phase 1: the column's start, gate and source (cape_column_run, getcape_col)
-    int start = 1, status = 0;
-    SourceSel sel;
-    sel.kmax = 1;
-    sel.mulvl = 0;
-    sel.avgth = sel.avgqv = 0.0f;
-    sel.ascend = false;
-    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
-    if (active) {
-      const float ts = ldf((const T *)a.ts + i);
-      if (GRID != 1)
-        start = a.start ? __ldg(a.start + i)
-                        : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
-      if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
-        if (start < 1 || start > a.nk) {
-          status = COL_BADSTART;
-        } else {
-          ColumnReader<T, GRID> col;
-          col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
-          col.ps = ldf((const T *)a.ps + i);
-          col.ts = ts;
-          col.tds = ldf((const T *)a.tds + i);
-          sel = select_source<true>(col, a.nk - start + 2, a.source, a.ml_depth);
-          if (sel.ascend) {
-            float p0, t0, td0, q0;
-            source_parcel<true>(col, sel, a.source, p0, t0, td0, q0);
-            lcl_features(p0, t0, td0, q0, f0, f1, f2);
-            status = PREP_RUN;
-          }
-        }
-      }
-    }
-    // phase 2: the network for the warp's 32 columns
-    __syncwarp();
-    const float y = warp_guess_eval(net, f0, f1, f2);
-    LearnedPrep &q = prep[threadIdx.x];
-    q.start = start;
-    q.kmax = sel.kmax;
-    q.mulvl = sel.mulvl;
-    q.status = status;
-    q.avgth = sel.avgth;
-    q.avgqv = sel.avgqv;
-    q.y = y;
-  }
-  __syncwarp();
-  // phase 3: the ascent
-  const LearnedPrep q = prep[threadIdx.x];
-  float cape = 0.0f, cin = 0.0f, zo = 0.0f;
-  int mulvl = 0, status = q.status & ~PREP_RUN, nsub = 0, niter = 0;
-  if (active && status == 0 && ldf((const T *)a.ts + i) > 0.0f) {
-    SourceSel sel;
-    sel.kmax = q.kmax;
-    sel.mulvl = q.mulvl;
-    sel.avgth = q.avgth;
-    sel.avgqv = q.avgqv;
-    sel.ascend = true;
-    CapeResult r;
-    if (q.status & PREP_RUN) {
-      ColumnReader<T, GRID> col;
-      col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, q.start);
-      col.ps = ldf((const T *)a.ps + i);
-      col.ts = ldf((const T *)a.ts + i);
-      col.tds = ldf((const T *)a.tds + i);
-      r = ascend_col<ICE, PSEUDO, SOLVE_LEARNED, false>(col, a.nk - q.start + 2, a.pinc, a.source,
-                                                        sel, nullptr, nullptr, q.y);
-    } else {
-      r.mulvl = sel.mulvl;
-      r.z_out = -999999.f;
-      r.cape = 0.0f;
-      r.cin = 0.0f;
-      r.status = 0;
-      r.nsub = 0;
-      r.niter = 0;
-    }
-    cape = r.cape;
-    cin = r.cin;
-    zo = r.z_out;
-    mulvl = r.mulvl;
-    status = r.status;
-    nsub = r.nsub;
-    niter = r.niter;
-  }
-  if (active) {
-    a.cape[i] = cape;
-    a.cin[i] = cin;
-    a.mulvl[i] = mulvl;
-    a.z_out[i] = zo;
-    if (a.status) a.status[i] = status;
-  }
+  int nsub, niter;
+  learned_column<T, GRID, ICE, PSEUDO>(a, net, prep, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                                       nsub, niter);
   if (a.counters) {
     long long sb = nsub, it = niter;
     for (int o = 16; o > 0; o >>= 1) {

@@ -518,6 +518,109 @@ int xc_calc_srh_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   return XC_OK;
 }
 
+int xc_cape_srh(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
+                const void *v3d, const void *ps, const void *ts, const void *tds, const void *us,
+                const void *vs, int dtype, float pinc, int source, float ml_depth, int adiabat,
+                const int *start_3d, double depth, double aglh0, int nk, int n2, int guess,
+                int precision, float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                double *srh_rm, double *srh_lm, float *rm, float *lm, float *mean6,
+                void *workspace, size_t workspace_bytes, void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  rc = check_cape_opts(pinc, source, ml_depth, adiabat);
+  if (rc) return rc;
+  if (grid != 1 && grid != 2) return fail(XC_ERR_INVALID, "grid must be 1 (sigma) or 2 (pressure, 1-D p)");
+  if (guess != XC_GUESS_PLAIN && guess != XC_GUESS_LEARNED)
+    return fail(XC_ERR_INVALID, "xc_cape_srh: guess must be XC_GUESS_PLAIN or XC_GUESS_LEARNED");
+  if (precision != XC_SRH_REFERENCE && precision != XC_SRH_FP32)
+    return fail(XC_ERR_INVALID, "precision must be XC_SRH_REFERENCE or XC_SRH_FP32");
+  if ((rm == nullptr) != (lm == nullptr) || (rm == nullptr) != (mean6 == nullptr))
+    return fail(XC_ERR_INVALID, "rm, lm and mean6 must be all NULL or all set");
+  const float *guess_w = nullptr;
+  if (guess == XC_GUESS_LEARNED) {
+    rc = guess_weights(&guess_w);
+    if (rc) return rc;
+  }
+  if (n2 == 0) return XC_OK;
+  if (!p || !t3d || !td3d || !u3d || !v3d || !ps || !ts || !tds || !us || !vs || !cape || !cin ||
+      !mulvl || !z_out || !srh_rm || !srh_lm)
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  xc::CapeArgs a;
+  a.grid = grid;
+  a.dtype = dtype;
+  a.p = p;
+  a.t = t3d;
+  a.td = td3d;
+  a.ps = ps;
+  a.ts = ts;
+  a.tds = tds;
+  a.start = grid == 2 ? start_3d : nullptr;
+  a.pinc = pinc;
+  a.source = source;
+  a.ml_depth = ml_depth;
+  a.adiabat = adiabat;
+  a.nk = nk;
+  a.n2 = n2;
+  a.guess = guess;
+  a.cape = cape;
+  a.cin = cin;
+  a.mulvl = mulvl;
+  a.z_out = z_out;
+  a.status = status;
+  a.counters = nullptr;
+  a.perm = nullptr;
+  a.guess_w = guess_w;
+  xc::SrhArgs h;
+  h.grid = grid;
+  h.dtype = dtype;
+  h.p = p;
+  h.t = t3d;
+  h.td = td3d;
+  h.u = u3d;
+  h.v = v3d;
+  h.ps = ps;
+  h.ts = ts;
+  h.tds = tds;
+  h.us = us;
+  h.vs = vs;
+  h.start = a.start;
+  h.depth = depth;
+  h.aglh0 = aglh0;
+  h.nk = nk;
+  h.n2 = n2;
+  h.srh_rm = srh_rm;
+  h.srh_lm = srh_lm;
+  h.rm = rm;
+  h.lm = lm;
+  h.mean6 = mean6;
+  h.precision = precision;
+  cudaError_t e = cudaSuccess;
+  if (workspace) {
+    if (workspace_bytes < xc::order_workspace_bytes(n2))
+      return fail(XC_ERR_INVALID, "workspace of %zu bytes is smaller than the %zu needed",
+                  workspace_bytes, xc::order_workspace_bytes(n2));
+    if (((size_t)workspace & 255) != 0) return fail(XC_ERR_INVALID, "workspace must be 256-byte aligned");
+    e = xc::launch_order(a, workspace, &a.perm, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
+  }
+  if (guess == XC_GUESS_LEARNED && precision == XC_SRH_FP32 && dtype == XC_F32) {
+    // Here the learned lift and the FP32 SRH tile kernel back to back are
+    // faster than the fused kernel: the tile kernel reads its rows
+    // coalesced through shared memory, while the fused kernel's per-thread
+    // walk of the ordered (scattered) columns costs more than the shared
+    // reads save (3.73 against 3.95 ms at 1M columns x 50 levels).  With
+    // the FP64 SRH stages, or the plain solver, the fused kernel wins.
+    e = xc::launch_cape(a, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+    e = xc::launch_srh(h, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "srh kernel launch");
+    return XC_OK;
+  }
+  e = xc::launch_cape_srh(a, h, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cape + srh kernel launch");
+  return XC_OK;
+}
+
 int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
                      const void *u3d, const void *v3d, const void *ps, const void *ts,
                      const void *tds, const void *us, const void *vs, int dtype,

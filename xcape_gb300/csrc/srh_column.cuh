@@ -38,19 +38,39 @@ constexpr double SH_C5349 = (double)53.49f;
 constexpr double SH_C509 = (double)5.09f;
 constexpr float VMSG = -999999.f;
 
+// A product that feeds an addition, rounded on its own as the reference's
+// compiled code rounds it: the device build never fuses it into a
+// multiply-add, whatever the -fmad setting of the translation unit that
+// inlines this file, so every kernel that runs these routines (the SRH
+// kernels, the fused CAPE + SRH kernel) gives the same bits.
+XC_HD float nc_mul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+XC_HD double nc_mul(double a, double b) {
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
 // Virtual temperature of one level (stdheight_2D_model_lev.f90:102-111,
 // 116-131); P in hPa, T/Td in degC.
 XC_HD double stdh_tv(double P, double T, double Td) {
   const double Tin = T + SH_T0;
   const double Tdin = Td + SH_T0;
-  const double E = SH_C6112 * exp((SH_C5349 - (6808.0 / Tdin) - SH_C509 * log(Tdin)));
-  const double w = SH_EPS * (E / (P - E));
-  return Tin * ((w + SH_EPS) / (SH_EPS * (1.0 + w)));
+  const double E = nc_mul(SH_C6112, exp((SH_C5349 - (6808.0 / Tdin) - nc_mul(SH_C509, log(Tdin)))));
+  const double w = nc_mul(SH_EPS, (E / (P - E)));
+  return nc_mul(Tin, ((w + SH_EPS) / (SH_EPS * (1.0 + w))));
 }
 
 // Hypsometric step (:147, :155).
 XC_HD double stdh_step(double Hprev, double Tv, double Tvprev, double P, double Pprev) {
-  return Hprev + ((SH_R * ((Tv + Tvprev) / 2.0) / SH_G)) * (log(P / Pprev));
+  return Hprev + nc_mul((SH_R * ((Tv + Tvprev) / 2.0) / SH_G), (log(P / Pprev)));
 }
 
 // FP32 forms of the two stdheight formulas, for the FP32 SRH path (the
@@ -59,12 +79,12 @@ XC_HD float stdh_tv_f(float P, float T, float Td) {
   const float eps = 0.6219800858985514f;
   const float Tin = T + 273.15f;
   const float Tdin = Td + 273.15f;
-  const float E = 6.112f * expf((53.49f - (6808.0f / Tdin) - 5.09f * logf(Tdin)));
-  const float w = eps * (E / (P - E));
-  return Tin * ((w + eps) / (eps * (1.0f + w)));
+  const float E = nc_mul(6.112f, expf((53.49f - (6808.0f / Tdin) - nc_mul(5.09f, logf(Tdin)))));
+  const float w = nc_mul(eps, (E / (P - E)));
+  return nc_mul(Tin, ((w + eps) / (eps * (1.0f + w))));
 }
 XC_HD float stdh_dh_f(float Tv, float Tvprev, float P, float Pprev) {
-  return ((287.04f * ((Tv + Tvprev) / 2.0f) / -9.80665f)) * logf(P / Pprev);
+  return nc_mul(((287.04f * ((Tv + Tvprev) / 2.0f) / -9.80665f)), logf(P / Pprev));
 }
 
 // Real type of the stdheight / SREH stages: double as in the reference, or
@@ -108,13 +128,13 @@ XC_HD void bunkers_bracket(float zlo, float zhi, float ulo, float uhi, float vlo
   while (i0 > 0 && 500.0f * (float)i0 >= za) --i0;
   while (i0 < 12 && 500.0f * (float)(i0 + 1) < za) ++i0;
   for (int i = i0; i < 12; ++i) {
-    const float h = 500.0f * (float)(i + 1);
+    const float h = nc_mul(500.0f, (float)(i + 1));
     if (!(zb > h)) break;
     if (za <= h) {
       const float w2 = (h - za) / (zb - za);
       const float w1 = (float)(1.0 - (double)w2);  // W1 = 1.D0 - W2
-      u6[i] = w1 * ua + w2 * ub;
-      v6[i] = w1 * va + w2 * vb;
+      u6[i] = nc_mul(w1, ua) + nc_mul(w2, ub);
+      v6[i] = nc_mul(w1, va) + nc_mul(w2, vb);
     }
   }
 }
@@ -138,7 +158,7 @@ XC_HD void bunkers_finish(float u1, float v1, const float *u6, const float *v6, 
   const float vshr_d = ((0.0f + v1) + v6[0]) / 2.0f;
   const float ushr = ushr_u - ushr_d;
   const float vshr = vshr_u - vshr_d;
-  const float nrm = sqrtf(ushr * ushr + vshr * vshr);
+  const float nrm = sqrtf(nc_mul(ushr, ushr) + nc_mul(vshr, vshr));
   rm[0] = m0 + 7.5f * vshr / nrm;
   rm[1] = m1 - 7.5f * ushr / nrm;
   lm[0] = m0 - 7.5f * vshr / nrm;
@@ -231,9 +251,9 @@ XC_HD SrhPass1 srh_pass1(const LV &lv, const SrhSurface &c, int ncl, double dept
       R x1 = H;
       const R x3 = Hprev;
       if (x3 == x1) x1 = x1 - (R)0.01f;
-      r.utop = (double)(ud + ((udprev - ud) * ((rdepth - x1) / (x3 - x1))));
+      r.utop = (double)(ud + nc_mul((udprev - ud), ((rdepth - x1) / (x3 - x1))));
       if (x3 == x1) x1 = x1 - (R)0.01f;
-      r.vtop = (double)(vd + ((vdprev - vd) * ((rdepth - x1) / (x3 - x1))));
+      r.vtop = (double)(vd + nc_mul((vdprev - vd), ((rdepth - x1) / (x3 - x1))));
     }
     Pprev = P;
     Hprev = H;
@@ -290,8 +310,8 @@ XC_HD void srh_column_body(const SrhArgs &a, long long i, const LV &lv, const Sr
       uk = lv.u(c.base + k);
       vk = lv.v(c.base + k);
     }
-    s_rm.add(((uk - cu_rm) * (vk - vprev)) - ((vk - cv_rm) * (uk - uprev)));
-    s_lm.add(((uk - cu_lm) * (vk - vprev)) - ((vk - cv_lm) * (uk - uprev)));
+    s_rm.add(nc_mul((uk - cu_rm), (vk - vprev)) - nc_mul((vk - cv_rm), (uk - uprev)));
+    s_lm.add(nc_mul((uk - cu_lm), (vk - vprev)) - nc_mul((vk - cv_lm), (uk - uprev)));
     uprev = uk;
     vprev = vk;
   }
@@ -386,7 +406,7 @@ XC_HD float dinterp2dz_col(const float *V, const float *Z, float vs, float zs, i
       const float w2 = (loc - za) / (zb - za);
       const float w1 = (float)(1.0 - (double)w2);
       const float va = ka == 1 ? vs : V[ka - 2], vb = kb == 1 ? vs : V[kb - 2];
-      return w1 * va + w2 * vb;
+      return nc_mul(w1, va) + nc_mul(w2, vb);
     }
   }
   return VMSG;
@@ -401,7 +421,7 @@ XC_HD void bunkers_column_run(const float *U, const float *V, const float *Z, co
   const float *Uc = U + i * nk + st - 1, *Vc = V + i * nk + st - 1, *Zc = Z + i * nk + st - 1;
   float u6[12], v6[12];
   for (int k = 0; k < 12; ++k) {
-    const float h = 500.0f * (float)(k + 1);
+    const float h = nc_mul(500.0f, (float)(k + 1));
     u6[k] = dinterp2dz_col(Uc, Zc, Us[i], Zs[i], nz, h);
     v6[k] = dinterp2dz_col(Vc, Zc, Vs[i], Zs[i], nz, h);
   }
@@ -429,9 +449,9 @@ XC_HD void sreh_column_run(const double *u, const double *v, const double *aglh,
       const double uk = uc[k - 2], vk = vc[k - 2];
       const double up = k == 2 ? us[i] : uc[k - 3], vp = k == 2 ? vs[i] : vc[k - 3];
       if (x3 == x1) x1 = x1 - (double)0.01f;
-      ut = uk + ((up - uk) * ((top - x1) / (x3 - x1)));
+      ut = uk + nc_mul((up - uk), ((top - x1) / (x3 - x1)));
       if (x3 == x1) x1 = x1 - (double)0.01f;
-      vt = vk + ((vp - vk) * ((top - x1) / (x3 - x1)));
+      vt = vk + nc_mul((vp - vk), ((top - x1) / (x3 - x1)));
       break;
     }
   }
@@ -439,8 +459,8 @@ XC_HD void sreh_column_run(const double *u, const double *v, const double *aglh,
   double up = us[i], vp = vs[i];
   for (int k = 2; k <= ktop; ++k) {
     const double uk = k == ktop ? ut : uc[k - 2], vk = k == ktop ? vt : vc[k - 2];
-    s1 = s1 + (((uk - cu_rm[i]) * (vk - vp)) - ((vk - cv_rm[i]) * (uk - up)));
-    s2 = s2 + (((uk - cu_lm[i]) * (vk - vp)) - ((vk - cv_lm[i]) * (uk - up)));
+    s1 = s1 + (nc_mul((uk - cu_rm[i]), (vk - vp)) - nc_mul((vk - cv_rm[i]), (uk - up)));
+    s2 = s2 + (nc_mul((uk - cu_lm[i]), (vk - vp)) - nc_mul((vk - cv_lm[i]), (uk - up)));
     up = uk;
     vp = vk;
   }

@@ -44,6 +44,8 @@ cudaError_t launch_cape(const CapeArgs &a, cudaStream_t s);
 // Rebuilds the learned kernel's shared-memory image of the guess network
 // from the parameters w (device) on this device (cape_kernel.cu).
 cudaError_t build_warp_net(const float *w, cudaStream_t s);
+// Device address of that image on this device (for kernels in other files).
+cudaError_t warp_net_image(const void **out);
 cudaError_t launch_cape_diag(const CapeArgs &a, cudaStream_t s);  // cape_diag.cu
 
 // Column ordering (cape_kernel.cu): a counting sort of the columns by
@@ -94,6 +96,8 @@ struct SrhArgs {
 };
 
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
+// CAPE (guess 0 or 1) and SRH of the same columns in one kernel (cape_srh.cu).
+cudaError_t launch_cape_srh(const CapeArgs &a, const SrhArgs &s, cudaStream_t st);
 
 // Stage kernels mirroring the reference's individual Fortran loops.
 cudaError_t launch_stdheight(const double *P, long long p_stride, const double *T,
