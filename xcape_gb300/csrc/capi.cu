@@ -59,11 +59,20 @@ std::vector<Workspace> g_ws;
 // Two non-blocking streams per device for the pipelined host paths (chunk
 // c + 1's copies overlap chunk c's kernels), and an event that chains them
 // to the caller's stream.  Created on first use, kept for the process.
+// Columns per chunk of the pipelined host path: at least this many, at most
+// HOST_CHUNKS chunks; the chunks' device buffers (a ring of slots) take at
+// most HOST_RING_BYTES, and at least two slots.
+constexpr int HOST_CHUNK_MIN = 131072;
+constexpr int HOST_CHUNKS = 8;
+constexpr size_t HOST_RING_BYTES = (size_t)4 << 30;
+
 struct Pipeline {
-  cudaStream_t s[2] = {nullptr, nullptr};
+  cudaStream_t s[2] = {nullptr, nullptr};  // kernels and output copies, alternating
+  cudaStream_t copy = nullptr;             // input copies, in chunk order
   cudaEvent_t start = nullptr;
-  cudaEvent_t done[2] = {nullptr, nullptr};  // a chunk's outputs are in the staging buffer
-  char *pinned = nullptr;                      // pinned output staging, grow-only
+  cudaEvent_t loaded[HOST_CHUNKS] = {};    // slot k holds its chunk's inputs
+  cudaEvent_t done[HOST_CHUNKS] = {};      // slot k's outputs are in its staging
+  char *pinned = nullptr;                  // pinned output staging, grow-only
   size_t pinned_cap = 0;
 };
 std::vector<Pipeline> g_pipe;
@@ -74,10 +83,13 @@ int pipeline_get(Pipeline **out) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if ((int)g_pipe.size() <= dev) g_pipe.resize(dev + 1);
   Pipeline &pl = g_pipe[dev];
-  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k)
     if (!pl.s[k]) e = cudaStreamCreateWithFlags(&pl.s[k], cudaStreamNonBlocking);
-    if (e == cudaSuccess && !pl.done[k])
-      e = cudaEventCreateWithFlags(&pl.done[k], cudaEventDisableTiming);
+  if (e == cudaSuccess && !pl.copy) e = cudaStreamCreateWithFlags(&pl.copy, cudaStreamNonBlocking);
+  for (int k = 0; k < HOST_CHUNKS && e == cudaSuccess; ++k) {
+    if (!pl.done[k]) e = cudaEventCreateWithFlags(&pl.done[k], cudaEventDisableTiming);
+    if (e == cudaSuccess && !pl.loaded[k])
+      e = cudaEventCreateWithFlags(&pl.loaded[k], cudaEventDisableTiming);
   }
   if (e == cudaSuccess && !pl.start) e = cudaEventCreateWithFlags(&pl.start, cudaEventDisableTiming);
   if (e != cudaSuccess) return cuda_fail(e, "creating the host-path streams");
@@ -326,10 +338,6 @@ int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const voi
                         nullptr, nullptr, 0, stream);
 }
 
-// Columns per chunk of the pipelined host path: at least this many, at most
-// HOST_CHUNKS chunks.
-constexpr int HOST_CHUNK_MIN = 131072;
-constexpr int HOST_CHUNKS = 8;
 
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
                         const void *ps, const void *ts, const void *tds, int dtype, float pinc,
@@ -343,13 +351,16 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1, 2 or 3");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
   if (n2 == 0) return XC_OK;
-  // The columns go through in chunks, alternating between two streams that
-  // each own a set of chunk buffers: the copies of one chunk overlap the
-  // kernels of the other.  Outputs come back into pinned staging (a copy
-  // into pageable memory would block this thread) and are moved into the
-  // caller's arrays while the GPU works on the later chunks.  Each column
-  // is still computed by one thread and written to its own index, so the
-  // chunking changes no result.
+  // The columns go through in chunks.  One stream copies the chunks' inputs
+  // in order; each chunk's lift and output copy run on one of two streams
+  // once its inputs are in, so copies overlap lifts and one chunk's last
+  // warps overlap the next chunk's first.  Every chunk has its own device
+  // slot when the ring budget allows (the usual case), and then this thread
+  // queues the whole call without waiting.  Outputs come back into pinned
+  // staging (a copy into pageable memory would block this thread) and are
+  // moved into the caller's arrays at the end, or when a slot is reused.
+  // Each column is still computed by one thread and written to its own
+  // index, so the chunking changes no result.
   int nchunk = (n2 + HOST_CHUNK_MIN - 1) / HOST_CHUNK_MIN;
   if (nchunk > HOST_CHUNKS) nchunk = HOST_CHUNKS;
   const int C = ((n2 + nchunk - 1) / nchunk + 255) / 256 * 256;  // columns per chunk
@@ -360,11 +371,25 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   Pipeline *pl = nullptr;
   rc = pipeline_get(&pl);
   if (rc) return rc;
-  const int nslot = nchunk > 1 ? 2 : 1;
   struct Slot {
     size_t p, t, td, ps, ts, tds, st, cape, cin, mu, z, stat, ord;
-  } sl[2];
+  } sl[HOST_CHUNKS];
   const size_t ord_bytes = xc::order_workspace_bytes(C);
+  size_t slot_bytes = 0;
+  {
+    Carver one;
+    one.take((grid == 2 ? (size_t)nk : c3) * es);
+    one.take(c3 * es);
+    one.take(c3 * es);
+    for (int j = 0; j < 3; ++j) one.take((size_t)C * es);
+    if (has_start) one.take((size_t)C * 4);
+    for (int j = 0; j < (status ? 5 : 4); ++j) one.take((size_t)C * 4);
+    one.take(ord_bytes);
+    slot_bytes = one.off;
+  }
+  int nslot = (int)(HOST_RING_BYTES / slot_bytes);
+  if (nslot < 2) nslot = 2;
+  if (nslot > nchunk) nslot = nchunk;
   Carver cv;
   for (int k = 0; k < nslot; ++k) {
     sl[k].p = cv.take((grid == 2 ? (size_t)nk : c3) * es);
@@ -405,7 +430,8 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     return XC_OK;
   };
   cudaError_t e = cudaEventRecord(pl->start, (cudaStream_t)stream);
-  for (int k = 0; k < nslot && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(pl->s[k], pl->start, 0);
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(pl->s[k], pl->start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->copy, pl->start, 0);
   if (e != cudaSuccess) return cuda_fail(e, "ordering the host path after the caller's stream");
   const char *hp = (const char *)p, *ht = (const char *)t3d, *htd = (const char *)td3d;
   const char *hps = (const char *)ps, *hts = (const char *)ts, *htds = (const char *)tds;
@@ -415,15 +441,18 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     if (c0 >= n2) break;
     const int nc = (int)((n2 - c0) < C ? (n2 - c0) : C);
     const int k = c % nslot;
-    if (c >= nslot) {  // the slot's staging still holds chunk c - nslot
+    if (c >= nslot) {
+      // the slot still holds chunk c - nslot: its outputs leave the staging
+      // first, and its lift (before its output copy) is done with the inputs
       rc = finish(c - nslot);
       if (rc) return rc;
     }
     const Slot &q = sl[k];
-    cudaStream_t s = pl->s[k];
+    cudaStream_t s = pl->s[c & 1];
     const size_t r3 = (size_t)nc * nk * es, off3 = (size_t)c0 * nk * es, off1 = (size_t)c0 * es;
 #define H2D(off, src, bytes)                                                         \
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, s)
+    if (e == cudaSuccess)                                                            \
+      e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, pl->copy)
     if (grid == 2) {
       H2D(q.p, hp, (size_t)nk * es);
     } else {
@@ -436,6 +465,8 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     H2D(q.tds, htds + off1, (size_t)nc * es);
     if (has_start) H2D(q.st, start_3d + c0, (size_t)nc * 4);
 #undef H2D
+    if (e == cudaSuccess) e = cudaEventRecord(pl->loaded[k], pl->copy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, pl->loaded[k], 0);
     if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
     rc = xc_loopcape_ex(grid, b + q.p, b + q.t, b + q.td, b + q.ps, b + q.ts, b + q.tds, dtype,
                         pinc, source, ml_depth, adiabat, has_start ? (const int *)(b + q.st) : nullptr,
