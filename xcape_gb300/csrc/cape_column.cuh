@@ -199,15 +199,136 @@ XC_HD float dqsat_dt(float qsat, float p, float es, float tb, float k) {
   return fast_div(qsat * p * k, (p - es) * tb * tb);
 }
 
+// The map F of a sub-step (:435-463): th2 = F(x) for the guess x, with t2,
+// qv2, ql2, qi2 at x.  The parcel starts the sub-step at (t1, th1, qv1, ql1,
+// qi1) with total water qt; p2, pi2 = (p2/P00)^(Rd/cp) and lp = ln(p2/p1).
+// plain_map is the reference's sequence of operations.
+template <bool ICE>
+XC_HD float plain_map(float x, float p2, float pi2, float lp, float t1, float th1, float qv1,
+                      float ql1, float qi1, float qt, float &t2, float &qv2, float &ql2,
+                      float &qi2) {
+  t2 = x * pi2;
+  float fliq, fice, qsat;
+  if (ICE) {
+    fliq = fmax_f(fmin_f((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
+    fice = 1.0f - fliq;
+    qsat = fliq * getqvs(p2, t2) + fice * getqvi(p2, t2);
+  } else {
+    fliq = 1.0f;
+    fice = 0.0f;
+    qsat = getqvs(p2, t2);
+  }
+  qv2 = fmin_f(qt, qsat);
+  if (ICE) {
+    qi2 = fmax_f(fice * (qt - qv2), 0.0f);
+  } else {
+    qi2 = 0.0f;
+  }
+  ql2 = fmax_f(qt - qv2 - qi2, 0.0f);
+  const float tbar = 0.5f * (t1 + t2);
+  const float qvbar = 0.5f * (qv1 + qv2);
+  const float qlbar = 0.5f * (ql1 + ql2);
+  const float lhv = LV1 - LV2 * tbar;
+  const float rm = RD + RV * qvbar;
+  float expo;
+  if (ICE) {
+    const float qibar = 0.5f * (qi1 + qi2);
+    const float lhs = LS1 - LS2 * tbar;
+    const float cpm = CP + CPV * qvbar + CPL * qlbar + CPI * qibar;
+    expo = lhv * (ql2 - ql1) / (cpm * tbar) + lhs * (qi2 - qi1) / (cpm * tbar) +
+           (rm / cpm - RDDCP) * lp;
+  } else {
+    const float cpm = CP + CPV * qvbar + CPL * qlbar;
+    expo = lhv * (ql2 - ql1) / (cpm * tbar) + (rm / cpm - RDDCP) * lp;
+  }
+  return th1 * expf(expo);
+}
+
+// The same map for the accelerated solvers: the approximate exp and divides
+// of getqvs_fast / getqvi_fast, the exponent over one common denominator
+// (one approximate divide), and the clamps as single min/max operations
+// (equal to the reference's compare-and-select for the non-NaN bounds used
+// here).  With slope set it also returns dex = d expo / d t2 at x,
+// differentiated through the saturation mixing ratio (dqsat_dt), the
+// liquid/ice split and the exponent, for the Newton step of substep.
+template <bool ICE>
+XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th1, float qv1,
+                      float ql1, float qi1, float qt, bool slope, float &t2, float &qv2,
+                      float &ql2, float &qi2, float &dex) {
+  t2 = x * pi2;
+  float fliq, fice, qsat;
+  float dq = 0.0f, dql = 0.0f, dqi = 0.0f;  // d/dt2 of qv2, ql2, qi2 (slope)
+  if (ICE) {
+    fliq = fmaxf(fminf((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
+    fice = 1.0f - fliq;
+    float esl, esi;
+    const float qvs = getqvs_fast(p2, t2, esl), qvi = getqvi_fast(p2, t2, esi);
+    qsat = fliq * qvs + fice * qvi;
+    if (slope && qt > qsat) {
+      // saturated: qv2 = qsat, ql2 = fliq (qt - qsat), qi2 = fice (qt - qsat)
+      const float dfl = (t2 > 233.15f && t2 < 273.15f) ? 1.0f / (273.15f - 233.15f) : 0.0f;
+      dq = dfl * (qvs - qvi) +
+           fliq * dqsat_dt(qvs, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f)) +
+           fice * dqsat_dt(qvi, p2, esi, t2 - 7.66f, 21.8745584f * (273.15f - 7.66f));
+      const float c = dfl * (qt - qsat);
+      dql = c - fliq * dq;
+      dqi = -c - fice * dq;
+    }
+  } else {
+    fliq = 1.0f;
+    fice = 0.0f;
+    float esl;
+    qsat = getqvs_fast(p2, t2, esl);
+    if (slope && qt > qsat) {
+      dq = dqsat_dt(qsat, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f));
+      dql = -dq;
+    }
+  }
+  qv2 = fmin_f(qt, qsat);  // NaN qsat (a NaN column) stays NaN, as in the reference
+  if (ICE) {
+    qi2 = fmaxf(fice * (qt - qv2), 0.0f);
+  } else {
+    qi2 = 0.0f;
+  }
+  ql2 = fmaxf(qt - qv2 - qi2, 0.0f);
+  const float tbar = 0.5f * (t1 + t2);
+  const float qvbar = 0.5f * (qv1 + qv2);
+  const float qlbar = 0.5f * (ql1 + ql2);
+  const float lhv = LV1 - LV2 * tbar;
+  const float rm = RD + RV * qvbar;
+  const float qibar = ICE ? 0.5f * (qi1 + qi2) : 0.0f;
+  const float cpm = ICE ? CP + CPV * qvbar + CPL * qlbar + CPI * qibar
+                        : CP + CPV * qvbar + CPL * qlbar;
+  float num = lhv * (ql2 - ql1) + rm * lp * tbar;
+  if (ICE) num += (LS1 - LS2 * tbar) * (qi2 - qi1);
+  const float den = cpm * tbar;
+  const float r = fast_div(num, den);
+  if (slope) {
+    // d expo / d t2 = (num' - r den') / den, tbar' = 1/2
+    float dnum = lhv * dql - 0.5f * LV2 * (ql2 - ql1) + lp * (0.5f * RV * dq * tbar + 0.5f * rm);
+    float dcpm = CPV * dq + CPL * dql;
+    if (ICE) {
+      dnum += (LS1 - LS2 * tbar) * dqi - 0.5f * LS2 * (qi2 - qi1);
+      dcpm += CPI * dqi;
+    }
+    dex = fast_div(dnum - r * (0.5f * dcpm * tbar + 0.5f * cpm), den);
+  }
+  return th1 * fast_exp(r - RDDCP * lp);
+}
+
+// The step of F(x) - x from x with slope q (secant or Newton), q kept in
+// [-50, 0.5] so that a noisy slope cannot throw x far.
+XC_HD float root_step(float x, float fx, float q) {
+  return x + fast_div(fx - x, 1.0f - fminf(fmaxf(q, -50.0f), 0.5f));
+}
+
 // One sub-step of the moist adiabat (:417-498).  Returns false when the
 // iteration did not converge within 100 steps (:465-474).
 //
 // The accelerated modes (SOLVE_ACCEL, SOLVE_LEARNED) take their first step
 // from the first guess x0 as a Newton step on F(x) - x, with the slope F'(x0)
-// of the map differentiated analytically at the first evaluation: through
-// t2 = x pi2, the saturation mixing ratio (dqsat_dt), the condensate split
-// and the exponent.  Secant steps follow.  The stopping test is the
-// reference's.
+// of the map differentiated analytically at the first evaluation (accel_map
+// with slope).  Secant steps follow.  The stopping test is the reference's.
 template <bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
 XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
                                         float &ql2, float &qi2, float &qt, int &niter,
@@ -235,126 +356,59 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   float thlast = th1;
   float x_prev = 0.0f, f_prev = 0.0f;
   constexpr bool EXTRAP = SOLVER == SOLVE_ACCEL || SOLVER == SOLVE_LEARNED;
-  float dth_net;
-  if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
-             network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net)) {
-    thlast = th1 + dth_net;
-  } else if (EXTRAP) {
+  if (EXTRAP) {
+    // the first evaluation, at the extrapolated guess, also gives the map's
+    // slope: a Newton step from it, then secant steps through the last two
+    // evaluations (Newton again where x repeated)
     thlast = th1 + ss.rate * dp;
-  }
-  // (EXTRAP) d/dt2 of qv2, ql2, qi2 and of the exponent at the first evaluation
-  float dq = 0.0f, dql = 0.0f, dqi = 0.0f, dex = 0.0f;
-  int i = 0;
-  while (true) {
-    i = i + 1;
-    t2 = thlast * pi2;
-    float fliq, fice, qsat;
-    if (ICE) {
-      fliq = fmax_f(fmin_f((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
-      fice = 1.0f - fliq;
-      if (ACCEL_MATH) {
-        float esl, esi;
-        const float qvs = getqvs_fast(p2, t2, esl), qvi = getqvi_fast(p2, t2, esi);
-        qsat = fliq * qvs + fice * qvi;
-        if (EXTRAP && i == 1 && qt > qsat) {
-          // saturated: qv2 = qsat, ql2 = fliq (qt - qsat), qi2 = fice (qt - qsat)
-          const float dfl = (t2 > 233.15f && t2 < 273.15f) ? 1.0f / (273.15f - 233.15f) : 0.0f;
-          dq = dfl * (qvs - qvi) +
-               fliq * dqsat_dt(qvs, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f)) +
-               fice * dqsat_dt(qvi, p2, esi, t2 - 7.66f, 21.8745584f * (273.15f - 7.66f));
-          const float c = dfl * (qt - qsat);
-          dql = c - fliq * dq;
-          dqi = -c - fice * dq;
-        }
-      } else {
-        qsat = fliq * getqvs(p2, t2) + fice * getqvi(p2, t2);
-      }
-    } else {
-      fliq = 1.0f;
-      fice = 0.0f;
-      if (ACCEL_MATH) {
-        float esl;
-        qsat = getqvs_fast(p2, t2, esl);
-        if (EXTRAP && i == 1 && qt > qsat) {
-          dq = dqsat_dt(qsat, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f));
-          dql = -dq;
-        }
-      } else {
-        qsat = getqvs(p2, t2);
-      }
-    }
-    qv2 = fmin_f(qt, qsat);
-    if (ICE) {
-      qi2 = fmax_f(fice * (qt - qv2), 0.0f);
-    } else {
-      qi2 = 0.0f;
-    }
-    ql2 = fmax_f(qt - qv2 - qi2, 0.0f);
-
-    const float tbar = 0.5f * (t1 + t2);
-    const float qvbar = 0.5f * (qv1 + qv2);
-    const float qlbar = 0.5f * (ql1 + ql2);
-    const float lhv = LV1 - LV2 * tbar;
-    const float rm = RD + RV * qvbar;
-    float expo;
-    if (ACCEL_MATH) {
-      // the same exponent over one common denominator (one approximate
-      // divide, a few ulp)
-      const float qibar = ICE ? 0.5f * (qi1 + qi2) : 0.0f;
-      const float cpm = ICE ? CP + CPV * qvbar + CPL * qlbar + CPI * qibar
-                            : CP + CPV * qvbar + CPL * qlbar;
-      float num = lhv * (ql2 - ql1) + rm * lp * tbar;
-      if (ICE) num += (LS1 - LS2 * tbar) * (qi2 - qi1);
-      const float den = cpm * tbar;
-      const float r = fast_div(num, den);
-      expo = r - RDDCP * lp;
-      if (EXTRAP && i == 1) {
-        // d expo / d t2 = (num' - r den') / den, tbar' = 1/2
-        float dnum = lhv * dql - 0.5f * LV2 * (ql2 - ql1) + lp * (0.5f * RV * dq * tbar + 0.5f * rm);
-        float dcpm = CPV * dq + CPL * dql;
-        if (ICE) {
-          dnum += (LS1 - LS2 * tbar) * dqi - 0.5f * LS2 * (qi2 - qi1);
-          dcpm += CPI * dqi;
-        }
-        dex = fast_div(dnum - r * (0.5f * dcpm * tbar + 0.5f * cpm), den);
-      }
-    } else if (ICE) {
-      const float qibar = 0.5f * (qi1 + qi2);
-      const float lhs = LS1 - LS2 * tbar;
-      const float cpm = CP + CPV * qvbar + CPL * qlbar + CPI * qibar;
-      expo = lhv * (ql2 - ql1) / (cpm * tbar) + lhs * (qi2 - qi1) / (cpm * tbar) +
-             (rm / cpm - RDDCP) * lp;
-    } else {
-      const float cpm = CP + CPV * qvbar + CPL * qlbar;
-      expo = lhv * (ql2 - ql1) / (cpm * tbar) + (rm / cpm - RDDCP) * lp;
-    }
-    th2 = th1 * (ACCEL_MATH ? fast_exp(expo) : expf(expo));
-    ++niter;
-    if (i > 100) return false;
-    // difference quotient of F over the last two evaluations, kept in
-    // [-50, 0.5] so that a noisy quotient cannot throw x far
-    const bool have_q = SOLVER != SOLVE_PLAIN && i >= 2 && thlast != x_prev;
-    float s = 0.0f;
-    if (have_q) s = fmin_f(fmax_f(fast_div(th2 - f_prev, thlast - x_prev), -50.0f), 0.5f);
-    if (fabsf(th2 - thlast) > CONVERGE) {
-      const float step = th2 - thlast;
+    float dex = 0.0f;
+    for (int i = 1;; ++i) {
+      th2 = accel_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, i == 1, t2, qv2,
+                           ql2, qi2, dex);
+      ++niter;
+      if (i > 100) return false;
+      if (!(fabsf(th2 - thlast) > CONVERGE)) break;
+      const float q = i >= 2 && thlast != x_prev ? fast_div(th2 - f_prev, thlast - x_prev)
+                                                 : th2 * pi2 * dex;
       x_prev = thlast;
       f_prev = th2;
-      if (have_q) {
-        thlast = thlast + fast_div(step, 1.0f - s);  // secant step on F(x) - x
-      } else if (EXTRAP) {
-        // Newton step with F'(x0) = F(x0) pi2 d expo / d t2, in the same range
-        const float fp = fmin_f(fmax_f(th2 * pi2 * dex, -50.0f), 0.5f);
-        thlast = thlast + fast_div(step, 1.0f - fp);
-      } else {
-        thlast = thlast + 0.3f * step;
-      }
-    } else {
-      break;
+      thlast = root_step(thlast, th2, q);
     }
-  }
-  if (EXTRAP) {
     ss.rate = fast_div(th2 - th1, dp);
+  } else {
+    float dth_net;
+    if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
+        network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net)) {
+      thlast = th1 + dth_net;
+    }
+    int i = 0;
+    while (true) {
+      i = i + 1;
+      float unused;
+      if (ACCEL_MATH) {
+        th2 = accel_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, false, t2, qv2,
+                             ql2, qi2, unused);
+      } else {
+        th2 = plain_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, t2, qv2, ql2, qi2);
+      }
+      ++niter;
+      if (i > 100) return false;
+      if (fabsf(th2 - thlast) > CONVERGE) {
+        if (ACCEL_MATH && i >= 2 && thlast != x_prev) {
+          const float q = fast_div(th2 - f_prev, thlast - x_prev);
+          x_prev = thlast;
+          f_prev = th2;
+          thlast = root_step(thlast, th2, q);  // secant step on F(x) - x
+        } else {
+          const float step = th2 - thlast;
+          x_prev = thlast;
+          f_prev = th2;
+          thlast = thlast + 0.3f * step;
+        }
+      } else {
+        break;
+      }
+    }
   }
   if (SOLVER == SOLVE_LEARNED && ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y) {
     // the parcel has just saturated: the increment extrapolated into the
