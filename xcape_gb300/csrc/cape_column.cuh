@@ -494,7 +494,8 @@ struct SourceSel {
   bool ascend;
 };
 
-// FAST: the accelerated solvers' environment (make_env) in the mixed layer.
+// FAST: the accelerated solvers' theta-e (getthe_fast) for the most
+// unstable level and environment (make_env) in the mixed layer.
 template <bool FAST, typename T, int GRID>
 XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int source,
                               float ml_depth) {
@@ -516,8 +517,9 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
         if (p >= 50000.0f) {
           const float t = 273.15f + tin;
           const float td = 273.15f + tdin;
-          const float q = getqvs(p, td);
-          const float the = getthe(p, t, td, q);
+          float es;
+          const float q = FAST ? getqvs_fast(p, td, es) : getqvs(p, td);
+          const float the = FAST ? getthe_fast(p, t, td, q) : getthe(p, t, td, q);
           if (the > maxthe) {
             sel.mulvl = j;
             maxthe = the;
@@ -717,9 +719,15 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
           return r;
         }
       }
-      // :501-503
-      const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2 + ql2 + qi2);
-      b2 = G * (thv2 - cur.thv) / cur.thv;
+      // :501-503 (FAST: approximate divides, which keep the sign of b2)
+      float thv2;
+      if (FAST) {
+        thv2 = fast_div(th2 * (1.0f + REPS * qv2), 1.0f + qv2 + ql2 + qi2);
+        b2 = fast_div(G * (thv2 - cur.thv), cur.thv);
+      } else {
+        thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2 + ql2 + qi2);
+        b2 = G * (thv2 - cur.thv) / cur.thv;
+      }
       if (DIAG) {
         ascended = true;
         p_last = cur.p;

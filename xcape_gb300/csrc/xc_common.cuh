@@ -105,6 +105,21 @@ XC_HD float fast_log(float x) {
 #endif
 }
 
+// getthe of the accelerated solvers' source selection: the same formula with
+// the approximate log, exp and divides (powf as exp of the log), a relative
+// error near 1e-6 of theta-e.  The host build computes exactly what getthe
+// does except for powf, evaluated as exp(b log a).
+XC_HD float getthe_fast(float p, float t, float td, float q) {
+  float tlcl;
+  if ((td - t) >= -0.1f) {
+    tlcl = t;
+  } else {
+    tlcl = 56.0f + fast_div(1.0f, fast_div(1.0f, td - 56.0f) + 0.00125f * fast_log(fast_div(t, td)));
+  }
+  return t * fast_exp(0.2854f * (1.0f - 0.28f * q) * fast_log(fast_div(100000.0f, p))) *
+         fast_exp((fast_div(3376.0f, tlcl) - 2.54f) * q * (1.0f + 0.81f * q));
+}
+
 // getqvs / getqvi of the accelerated solvers: the same formulas with the
 // approximate exp and divides (the host build computes exactly what getqvs /
 // getqvi do), also returning the saturation vapour pressure es for the
