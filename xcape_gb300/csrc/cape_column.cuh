@@ -159,10 +159,13 @@ struct SolverState {
 // from the temperature and dewpoint, the LCL pressure along the dry
 // adiabat, the features (p_lcl, theta-e, q).  Returns false when the
 // output is out of the network's range.
+// The inputs only steer the first guess, so they use the approximate log,
+// exp and divides.
 XC_HD void lcl_features(float p, float t, float td, float q, float &f0, float &f1, float &f2) {
-  const float tlcl = 56.0f + 1.0f / (1.0f / (td - 56.0f) + logf(t / td) / 800.0f);
-  const float plcl = td < t ? p * powf(tlcl / t, 1.0f / RDDCP) : p;
-  guess_features(plcl, getthe(p, t, td, q), q, f0, f1, f2);
+  const float tlcl =
+      56.0f + fast_div(1.0f, fast_div(1.0f, td - 56.0f) + fast_log(fast_div(t, td)) * (1.0f / 800.0f));
+  const float plcl = td < t ? p * fast_exp((1.0f / RDDCP) * fast_log(fast_div(tlcl, t))) : p;
+  guess_features(plcl, getthe_fast(p, t, td, q), q, f0, f1, f2);
 }
 
 XC_HD bool parcel_lcl_slope(const float *w, float p, float t, float td, float q, float &y) {
@@ -261,6 +264,8 @@ XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th
   if (ICE) {
     fliq = fmaxf(fminf((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
     fice = 1.0f - fliq;
+    // both are evaluated: skipping the one of weight 0 outside the
+    // 233.15-273.15 K ramp was slower (the lanes of a warp straddle it)
     float esl, esi;
     const float qvs = getqvs_fast(p2, t2, esl), qvi = getqvi_fast(p2, t2, esi);
     qsat = fliq * qvs + fice * qvi;
