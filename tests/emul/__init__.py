@@ -46,6 +46,8 @@ def lib():
         L.emu_guess_eval_packed.argtypes = [vp, f, f, f]
         L.emu_guess_eval_packed.restype = f
         L.emu_guess_pairs.argtypes = [ll, ctypes.c_ulonglong, vp, vp, vp]
+        L.emu_accel_map.argtypes = [i] + [f] * 10 + [vp]
+        L.emu_accel_map.restype = f
         L.emu_request_layout.argtypes = [vp]
         L.emu_srh.argtypes = [i] + [vp] * 10 + [i, vp, d, d, i, ll] + [vp] * 5 + [i]
         L.emu_pres_lev_pos.argtypes = [vp, vp, i, i, ll, vp]

@@ -122,6 +122,23 @@ extern "C" float emu_guess_eval_packed(const float *w, float f0, float f1, float
   return guess_eval_packed(packed, f0, f1, f2);
 }
 
+// accel_map at x with the analytic slope: returns F(x) and writes out[0] =
+// F'(x) = F(x) pi2 d expo / d t2, out[1..4] = t2, qv2, ql2, qi2.
+extern "C" float emu_accel_map(int ice, float x, float p2, float pi2, float lp, float t1,
+                               float th1, float qv1, float ql1, float qi1, float qt, float *out) {
+  float t2, qv2, ql2, qi2, dex = 0.0f;
+  const float f = ice ? accel_map<true>(x, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, true, t2, qv2,
+                                        ql2, qi2, dex)
+                      : accel_map<false>(x, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, true, t2,
+                                         qv2, ql2, qi2, dex);
+  out[0] = f * pi2 * dex;
+  out[1] = t2;
+  out[2] = qv2;
+  out[3] = ql2;
+  out[4] = qi2;
+  return f;
+}
+
 extern "C" void emu_guess_pairs(long long n, unsigned long long seed, float *feats,
                                 float *targets, int *iters) {
   for (long long i = 0; i < n; ++i) iters[i] = guess_pair(seed, i, feats + 3 * i, targets + i);

@@ -102,6 +102,59 @@ def test_emulated_extrapolated_solver_vs_fp64(source, adiabat):
     assert fast["counters"][1] < 0.4 * plain["counters"][1]
 
 
+def _qvs_ref(p, t):
+    """getqvs (CAPE_CODE_model_lev.f90:570-581) in float64."""
+    es = 611.2 * np.exp(17.67 * (t - 273.15) / (t - 29.65))
+    return (287.04 / 461.5) * es / (p - es)
+
+
+@pytest.mark.parametrize("reversible", [False, True])
+@pytest.mark.parametrize("ice", [0, 1])
+def test_emulated_map_slope_matches_finite_differences(ice, reversible):
+    """The slope F'(x) that the accelerated solvers' first (Newton) step uses,
+    differentiated analytically through qsat(T), the liquid/ice split and the
+    exponent (accel_map), against a central difference of the map itself:
+    saturated and unsaturated sub-steps from 215 to 305 K, on both sides of
+    the ice ramp, away from the kinks of the map (saturation onset and the
+    ramp's ends)."""
+    L = emul.lib()
+    rng = np.random.default_rng(11 + 2 * ice + int(reversible))
+    o0, op, om = (np.zeros(5, np.float32) for _ in range(3))
+    rddcp = 287.04 / 1005.7
+    h = 0.05
+    checked = sat_checked = 0
+    for _ in range(600):
+        p1 = rng.uniform(20000.0, 100000.0)
+        dp = rng.uniform(100.0, 2000.0)
+        p2 = p1 - dp
+        t1 = rng.uniform(215.0, 305.0)
+        qs1 = min(_qvs_ref(p1, t1), 0.04)
+        sat = rng.random() < 0.7
+        qv1 = qs1 if sat else qs1 * rng.uniform(0.3, 0.9)
+        ql1 = rng.uniform(0.0, 2e-3) if (reversible and sat) else 0.0
+        qt = qv1 + ql1
+        th1 = t1 / (p1 / 1e5) ** rddcp
+        pi2 = (p2 / 1e5) ** rddcp
+        lp = np.log(p2 / p1)
+        x = th1 + rng.uniform(-0.6, 0.1)
+        args = (np.float32(p2), np.float32(pi2), np.float32(lp), np.float32(t1), np.float32(th1),
+                np.float32(qv1), np.float32(ql1), np.float32(0.0), np.float32(qt))
+        f0 = L.emu_accel_map(ice, np.float32(x), *args, o0.ctypes.data)
+        fp = L.emu_accel_map(ice, np.float32(x + h), *args, op.ctypes.data)
+        fm = L.emu_accel_map(ice, np.float32(x - h), *args, om.ctypes.data)
+        cond = [o[3] + o[4] > 0.0 for o in (om, o0, op)]
+        if len(set(cond)) > 1:
+            continue  # the stencil straddles the saturation onset
+        if ice and any(min(om[1], op[1]) - 0.1 <= tb <= max(om[1], op[1]) + 0.1
+                       for tb in (233.15, 273.15)):
+            continue  # the stencil straddles an end of the liquid/ice ramp
+        fd = (np.float64(fp) - np.float64(fm)) / (2 * h)
+        assert abs(o0[0] - fd) <= 3e-3 + 2e-2 * abs(fd), (o0[0], fd, t1, p1, sat)
+        checked += 1
+        sat_checked += cond[1]
+    assert checked > 300 and sat_checked > 150, (checked, sat_checked)
+
+
 def _same(a, b):
     for k in ("cape", "cin", "mulvl", "z_out", "status"):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
