@@ -43,13 +43,13 @@ SRH_METRIC = "SRH columns/s at 1M×50 lev (calc_srh, depth 1000+3000 m)"
 CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
 # DRAM bytes (read + write) of one most-unstable launch of the lift on this
 # workload, from `ncu --set full` captures of `bench.py --profile`.
-NCU_TRAFFIC = {"learned": 703_298_304, "plain": 725_548_288}
+NCU_TRAFFIC = {"learned": 702_052_608, "plain": 725_578_496}
 # The lift is bound by the SM issue rate, not by HBM: issue-slot activity of
 # the same captures (smsp__issue_active, % of peak over active cycles) and the
 # tensor pipe's share (the learned kernel's guess network).
-NCU_ISSUE = {"learned": {"issue_active": 0.867, "tensor_pipe_active": 0.0070,
-                         "threads_per_warp_instruction": 29.15},
-             "plain": {"issue_active": 0.878, "tensor_pipe_active": 0.0,
+NCU_ISSUE = {"learned": {"issue_active": 0.844, "tensor_pipe_active": 0.0079,
+                         "threads_per_warp_instruction": 28.98},
+             "plain": {"issue_active": 0.879, "tensor_pipe_active": 0.0,
                        "threads_per_warp_instruction": 27.11}}
 ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg
 CPU_SAMPLE_1T = 8192     # columns per single-core CPU-baseline measurement
