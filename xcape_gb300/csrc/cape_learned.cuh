@@ -160,61 +160,63 @@ constexpr int PREP_RUN = 1 << 30;
 // (net, copied by copy_warp_net) and the handoff records (prep); every
 // thread of the block calls it, also past n2.  Writes the CAPE outputs and
 // the thread's work counts.
-template <typename T, int GRID, bool ICE, bool PSEUDO>
-__device__ __forceinline__ void learned_column(const CapeArgs &a, const WarpNetSmem &net,
-                                               LearnedPrep *prep, long long t, int &nsub,
-                                               int &niter) {
-  const bool active = t < a.n2;
-  const long long i = active ? (a.perm ? (long long)__ldg(a.perm + t) : t) : 0;
+// Phases 1 and 2 for column i of thread t (all 32 lanes of the warp call
+// it; inactive lanes, past n2, take part with zero inputs): the column's
+// start, gate and source (cape_column_run, getcape_col), then the network
+// for the warp's 32 columns at the parcel's LCL.
+template <typename T, int GRID>
+__device__ __forceinline__ LearnedPrep learned_prepare(const CapeArgs &a, const WarpNetSmem &net,
+                                                       long long i, bool active) {
   const long long stride = a.ld > 0 ? a.ld : a.nk;
-  {
-    // phase 1: the column's start, gate and source (cape_column_run, getcape_col)
-    int start = 1, status = 0;
-    SourceSel sel;
-    sel.kmax = 1;
-    sel.mulvl = 0;
-    sel.avgth = sel.avgqv = 0.0f;
-    sel.ascend = false;
-    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
-    if (active) {
-      const float ts = ldf((const T *)a.ts + i);
-      if (GRID != 1)
-        start = a.start ? __ldg(a.start + i)
-                        : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
-      if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
-        if (start < 1 || start > a.nk) {
-          status = COL_BADSTART;
-        } else {
-          ColumnReader<T, GRID> col;
-          col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
-          col.ps = ldf((const T *)a.ps + i);
-          col.ts = ts;
-          col.tds = ldf((const T *)a.tds + i);
-          sel = select_source<true>(col, a.nk - start + 2, a.source, a.ml_depth);
-          if (sel.ascend) {
-            float p0, t0, td0, q0;
-            source_parcel<true>(col, sel, a.source, p0, t0, td0, q0);
-            lcl_features(p0, t0, td0, q0, f0, f1, f2);
-            status = PREP_RUN;
-          }
+  int start = 1, status = 0;
+  SourceSel sel;
+  sel.kmax = 1;
+  sel.mulvl = 0;
+  sel.avgth = sel.avgqv = 0.0f;
+  sel.ascend = false;
+  float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f;
+  if (active) {
+    const float ts = ldf((const T *)a.ts + i);
+    if (GRID != 1)
+      start = a.start ? __ldg(a.start + i)
+                      : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
+    if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
+      if (start < 1 || start > a.nk) {
+        status = COL_BADSTART;
+      } else {
+        ColumnReader<T, GRID> col;
+        col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
+        col.ps = ldf((const T *)a.ps + i);
+        col.ts = ts;
+        col.tds = ldf((const T *)a.tds + i);
+        sel = select_source<true>(col, a.nk - start + 2, a.source, a.ml_depth);
+        if (sel.ascend) {
+          float p0, t0, td0, q0;
+          source_parcel<true>(col, sel, a.source, p0, t0, td0, q0);
+          lcl_features(p0, t0, td0, q0, f0, f1, f2);
+          status = PREP_RUN;
         }
       }
     }
-    // phase 2: the network for the warp's 32 columns
-    __syncwarp();
-    const float y = warp_guess_eval(net, f0, f1, f2);
-    LearnedPrep &q = prep[threadIdx.x];
-    q.start = start;
-    q.kmax = sel.kmax;
-    q.mulvl = sel.mulvl;
-    q.status = status;
-    q.avgth = sel.avgth;
-    q.avgqv = sel.avgqv;
-    q.y = y;
   }
   __syncwarp();
-  // phase 3: the ascent
-  const LearnedPrep q = prep[threadIdx.x];
+  LearnedPrep q;
+  q.y = warp_guess_eval(net, f0, f1, f2);
+  q.start = start;
+  q.kmax = sel.kmax;
+  q.mulvl = sel.mulvl;
+  q.status = status;
+  q.avgth = sel.avgth;
+  q.avgqv = sel.avgqv;
+  q.pad = 0.0f;
+  return q;
+}
+
+// Phase 3 for column i from its record q: the ascent and the outputs.
+template <typename T, int GRID, bool ICE, bool PSEUDO>
+__device__ __forceinline__ void learned_ascend(const CapeArgs &a, const LearnedPrep &q,
+                                               long long i, bool active, int &nsub, int &niter) {
+  const long long stride = a.ld > 0 ? a.ld : a.nk;
   float cape = 0.0f, cin = 0.0f, zo = 0.0f;
   int mulvl = 0, status = q.status & ~PREP_RUN;
   nsub = 0;
@@ -261,5 +263,22 @@ __device__ __forceinline__ void learned_column(const CapeArgs &a, const WarpNetS
   }
 }
 
+// Column perm[t] (t when unordered) of the learned solver in one kernel, for
+// thread t of a LEARNED_THREADS-thread block whose shared memory holds the
+// network (net, copied by copy_warp_net) and the handoff records (prep);
+// every thread of the block calls it, also past n2.  The record goes
+// through shared memory so that nothing of phases 1-2 stays live in
+// registers across the ascent.
+template <typename T, int GRID, bool ICE, bool PSEUDO>
+__device__ __forceinline__ void learned_column(const CapeArgs &a, const WarpNetSmem &net,
+                                               LearnedPrep *prep, long long t, int &nsub,
+                                               int &niter) {
+  const bool active = t < a.n2;
+  const long long i = active ? (a.perm ? (long long)__ldg(a.perm + t) : t) : 0;
+  prep[threadIdx.x] = learned_prepare<T, GRID>(a, net, i, active);
+  __syncwarp();
+  const LearnedPrep q = prep[threadIdx.x];
+  learned_ascend<T, GRID, ICE, PSEUDO>(a, q, i, active, nsub, niter);
+}
 
 }  // namespace xc
