@@ -181,7 +181,11 @@ int xc_loopcape_ex_noalloc(int grid, const void *p, const void *t3d, const void 
                            float *cin, int *mulvl, float *z_out, int *status,
                            long long *counters, void *stream);
 
-/* Host-pointer form of xc_loopcape_ex (see the family note above). */
+/* Host-pointer form of xc_loopcape_ex (see the family note above).  The
+ * columns go through in up to 8 chunks whose device buffers take at most
+ * 4 GiB (at least two chunks' worth; the environment variable
+ * XC_HOST_RING_BYTES sets another limit, in bytes); chunks beyond that
+ * reuse buffers, which changes no result. */
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
                         const void *ps, const void *ts, const void *tds, int dtype, float pinc,
                         int source, float ml_depth, int adiabat, const int *start_3d, int nk,

@@ -339,12 +339,17 @@ def test_tall_columns(guess):
     assert np.all(d <= np.maximum(1.0, 1e-3 * want["cape"][ok])), d.max()
 
 
+@pytest.mark.parametrize("ring", [None, "1"])
 @pytest.mark.parametrize("guess", ["plain", "learned"])
-def test_host_path_chunks_match_device_path(guess):
+def test_host_path_chunks_match_device_path(guess, ring, monkeypatch):
     """numpy inputs go through the pipelined host entry point (chunks of
-    131,072+ columns alternating between two streams); the results equal
-    those of the device entry point on the same arrays, bit for bit."""
+    131,072+ columns, their inputs copied on one stream, their lifts on two);
+    the results equal those of the device entry point on the same arrays,
+    bit for bit.  With XC_HOST_RING_BYTES=1 the three chunks share two device
+    slots, so the third reuses the first's buffers and staging."""
     import torch
+    if ring is not None:
+        monkeypatch.setenv("XC_HOST_RING_BYTES", ring)
     plev, t, td, ps, ts, tds = S.pressure_c1(shape=(216, 1440))  # 311,040 columns: 3 chunks
     host = X.calc_cape(plev, t, td, ps, ts, tds, source="most-unstable",
                        vertical_lev="pressure", guess=guess)

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -61,10 +62,21 @@ std::vector<Workspace> g_ws;
 // to the caller's stream.  Created on first use, kept for the process.
 // Columns per chunk of the pipelined host path: at least this many, at most
 // HOST_CHUNKS chunks; the chunks' device buffers (a ring of slots) take at
-// most HOST_RING_BYTES, and at least two slots.
+// most host_ring_bytes(), and at least two slots.
 constexpr int HOST_CHUNK_MIN = 131072;
 constexpr int HOST_CHUNKS = 8;
-constexpr size_t HOST_RING_BYTES = (size_t)4 << 30;
+
+// 4 GiB, or the environment's XC_HOST_RING_BYTES (it changes only how
+// many chunks are in flight, never a result).
+size_t host_ring_bytes() {
+  const char *e = getenv("XC_HOST_RING_BYTES");
+  if (e && *e) {
+    char *end = nullptr;
+    const unsigned long long v = strtoull(e, &end, 10);
+    if (end && *end == '\0') return (size_t)v;
+  }
+  return (size_t)4 << 30;
+}
 
 struct Pipeline {
   cudaStream_t s[2] = {nullptr, nullptr};  // kernels and output copies, alternating
@@ -387,7 +399,7 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     one.take(ord_bytes);
     slot_bytes = one.off;
   }
-  int nslot = (int)(HOST_RING_BYTES / slot_bytes);
+  int nslot = (int)(host_ring_bytes() / slot_bytes);
   if (nslot < 2) nslot = 2;
   if (nslot > nchunk) nslot = nchunk;
   Carver cv;
