@@ -211,28 +211,38 @@ struct SrhPass1 {
   float ztop_f;       // f2py-rounded height of the top level (Z(NZ))
 };
 
-// Pass 1 over levels 2..ncl (see the file comment).  F32 selects the FP32
-// height integration (Kahan-compensated) and FP32 helicity inputs.
-template <bool DEC, bool F32, typename LV>
-XC_HD SrhPass1 srh_pass1(const LV &lv, const SrhSurface &c, int ncl, double depth, double aglh0,
-                         float *u6, float *v6) {
+// Pass 1 (see the file comment) as a sweep that takes levels 2..ncl in
+// order, one step per level: the hypsometric height (FP64, or FP32 with
+// Kahan compensation when F32), the 12 Bunkers targets (DEC selects the
+// scan rule) and the SREH top level.  A kernel can feed it levels from
+// global memory (srh_pass1) or from rows staged in shared memory a window at
+// a time (srh_window_kernel); the operations are the same.
+template <bool DEC, bool F32>
+struct SrhSweep {
   typedef typename SrhReal<F32>::type R;
   SrhPass1 r;
-  r.ktop = 0;
-  r.utop = 0.0;
-  r.vtop = 0.0;
-  R Pprev = (R)c.ps;
-  KSum<R> Hsum((R)aglh0);
-  R Hprev = (R)aglh0;
-  R Tvprev = F32 ? (R)stdh_tv_f((float)c.ps, (float)c.ts, (float)c.tds)
+  R Pprev, Hprev, Tvprev, udprev, vdprev, rdepth;
+  KSum<R> Hsum;
+  float zprev, uprev, vprev;
+
+  XC_HD SrhSweep(const SrhSurface &c, double depth, double aglh0) : Hsum((R)aglh0) {
+    r.ktop = 0;
+    r.utop = 0.0;
+    r.vtop = 0.0;
+    r.ztop_f = (float)aglh0;
+    Pprev = (R)c.ps;
+    Hprev = (R)aglh0;
+    Tvprev = F32 ? (R)stdh_tv_f((float)c.ps, (float)c.ts, (float)c.tds)
                  : (R)stdh_tv(c.ps, c.ts, c.tds);
-  const R rdepth = (R)depth;
-  float zprev = (float)aglh0, uprev = (float)c.us, vprev = (float)c.vs;
-  R udprev = (R)c.us, vdprev = (R)c.vs;
-  for (int j = 2; j <= ncl; ++j) {
-    const int m = c.base + j;
-    const R P = lv.p(m);
-    const R Tv = lv.tv(m, P);
+    rdepth = (R)depth;
+    zprev = (float)aglh0;
+    uprev = (float)c.us;
+    vprev = (float)c.vs;
+    udprev = (R)c.us;
+    vdprev = (R)c.vs;
+  }
+  // level j: pressure P, virtual temperature Tv, winds ud, vd
+  XC_HD void step(int j, R P, R Tv, R ud, R vd, float *u6, float *v6) {
     R H;
     if (F32) {
       Hsum.add((R)stdh_dh_f((float)Tv, (float)Tvprev, (float)P, (float)Pprev));
@@ -240,8 +250,6 @@ XC_HD SrhPass1 srh_pass1(const LV &lv, const SrhSurface &c, int ncl, double dept
     } else {
       H = (R)stdh_step((double)Hprev, (double)Tv, (double)Tvprev, (double)P, (double)Pprev);
     }
-    const R ud = lv.u(m);
-    const R vd = lv.v(m);
     const float zf = (float)H, uf = (float)ud, vf = (float)vd;
     bunkers_bracket<DEC>(zprev, zf, uprev, uf, vprev, vf, u6, v6);
     if (r.ktop == 0 && H > rdepth) {
@@ -264,8 +272,58 @@ XC_HD SrhPass1 srh_pass1(const LV &lv, const SrhSurface &c, int ncl, double dept
     udprev = ud;
     vdprev = vd;
   }
-  r.ztop_f = zprev;
-  return r;
+  XC_HD SrhPass1 finish() {
+    r.ztop_f = zprev;
+    return r;
+  }
+};
+
+// Pass 1 over levels 2..ncl read through `lv`.
+template <bool DEC, bool F32, typename LV>
+XC_HD SrhPass1 srh_pass1(const LV &lv, const SrhSurface &c, int ncl, double depth, double aglh0,
+                         float *u6, float *v6) {
+  typedef typename SrhReal<F32>::type R;
+  SrhSweep<DEC, F32> sw(c, depth, aglh0);
+  for (int j = 2; j <= ncl; ++j) {
+    const int m = c.base + j;
+    const R P = lv.p(m);
+    const R Tv = lv.tv(m, P);
+    sw.step(j, P, Tv, lv.u(m), lv.v(m), u6, v6);
+  }
+  return sw.finish();
+}
+
+// Pass 2 (DCALRELHL :100-114) as a sweep over levels 2..ktop in order: the
+// helicity sums for the right- and left-moving storm motions.
+template <bool F32>
+struct SrhSums {
+  typedef typename SrhReal<F32>::type R;
+  R cu_rm, cv_rm, cu_lm, cv_lm, uprev, vprev;
+  KSum<R> s_rm, s_lm;
+  XC_HD SrhSums(const float *rm, const float *lm, const SrhSurface &c)
+      : cu_rm(rm[0]), cv_rm(rm[1]), cu_lm(lm[0]), cv_lm(lm[1]), uprev((R)c.us),
+        vprev((R)c.vs), s_rm((R)0), s_lm((R)0) {}
+  XC_HD void step(R uk, R vk) {
+    s_rm.add(nc_mul((uk - cu_rm), (vk - vprev)) - nc_mul((vk - cv_rm), (uk - uprev)));
+    s_lm.add(nc_mul((uk - cu_lm), (vk - vprev)) - nc_mul((vk - cv_lm), (uk - uprev)));
+    uprev = uk;
+    vprev = vk;
+  }
+};
+
+// The Bunkers vectors of column i (when requested) and its helicities.
+XC_HD void srh_write(const SrhArgs &a, long long i, const float *rm, const float *lm,
+                     const float *mean, double srh_rm, double srh_lm) {
+  if (a.rm) {
+    a.rm[2 * i] = rm[0];
+    a.rm[2 * i + 1] = rm[1];
+    a.lm[2 * i] = lm[0];
+    a.lm[2 * i + 1] = lm[1];
+    a.mean6[2 * i] = mean[0];
+    a.mean6[2 * i + 1] = mean[1];
+  }
+  a.srh_rm[i] = srh_rm;
+  a.srh_lm[i] = srh_lm;
 }
 
 // Passes 1 and 2 of column i (levels through `lv`), and its outputs.
@@ -289,34 +347,12 @@ XC_HD void srh_column_body(const SrhArgs &a, long long i, const LV &lv, const Sr
   }
   float rm[2], lm[2], mean[2];
   bunkers_finish((float)c.us, (float)c.vs, u6, v6, rm, lm, mean);
-  if (a.rm) {
-    a.rm[2 * i] = rm[0];
-    a.rm[2 * i + 1] = rm[1];
-    a.lm[2 * i] = lm[0];
-    a.lm[2 * i + 1] = lm[1];
-    a.mean6[2 * i] = mean[0];
-    a.mean6[2 * i + 1] = mean[1];
-  }
-  // Pass 2: DCALRELHL :100-114.
-  const R cu_rm = rm[0], cv_rm = rm[1], cu_lm = lm[0], cv_lm = lm[1];
-  KSum<R> s_rm((R)0), s_lm((R)0);
-  R uprev = (R)c.us, vprev = (R)c.vs;
+  SrhSums<F32> sums(rm, lm, c);
   for (int k = 2; k <= r.ktop; ++k) {
-    R uk, vk;
-    if (k == r.ktop) {
-      uk = (R)r.utop;
-      vk = (R)r.vtop;
-    } else {
-      uk = lv.u(c.base + k);
-      vk = lv.v(c.base + k);
-    }
-    s_rm.add(nc_mul((uk - cu_rm), (vk - vprev)) - nc_mul((vk - cv_rm), (uk - uprev)));
-    s_lm.add(nc_mul((uk - cu_lm), (vk - vprev)) - nc_mul((vk - cv_lm), (uk - uprev)));
-    uprev = uk;
-    vprev = vk;
+    if (k == r.ktop) sums.step((R)r.utop, (R)r.vtop);
+    else sums.step(lv.u(c.base + k), lv.v(c.base + k));
   }
-  a.srh_rm[i] = -(double)s_rm.s;
-  a.srh_lm[i] = -(double)s_lm.s;
+  srh_write(a, i, rm, lm, mean, -(double)sums.s_rm.s, -(double)sums.s_lm.s);
 }
 
 // Column i of the fused SRH path (core.py:_calc_srh_numpy :473-542).
