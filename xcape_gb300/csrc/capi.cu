@@ -375,7 +375,22 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   // index, so the chunking changes no result.
   int nchunk = (n2 + HOST_CHUNK_MIN - 1) / HOST_CHUNK_MIN;
   if (nchunk > HOST_CHUNKS) nchunk = HOST_CHUNKS;
-  const int C = ((n2 + nchunk - 1) / nchunk + 255) / 256 * 256;  // columns per chunk
+  // Chunk c holds columns [bound[c], bound[c + 1]).  With three or more
+  // chunks the first and the last are half-size: the first lift starts
+  // after a shorter copy, and less work is left after the last copy.
+  long long bound[HOST_CHUNKS + 1];
+  bound[0] = 0;
+  for (int c = 1; c < nchunk; ++c) {
+    const double w = nchunk >= 3 ? (c - 0.5) / (nchunk - 1) : (double)c / nchunk;
+    long long b = ((long long)(w * n2) + 255) / 256 * 256;
+    if (b < bound[c - 1]) b = bound[c - 1];
+    if (b > n2) b = n2;
+    bound[c] = b;
+  }
+  bound[nchunk] = n2;
+  int C = 256;  // columns per slot: the largest chunk
+  for (int c = 0; c < nchunk; ++c)
+    if (bound[c + 1] - bound[c] > C) C = (int)(bound[c + 1] - bound[c]);
   const size_t es = dtype == XC_F32 ? 4 : 8;
   const size_t c3 = (size_t)C * nk;
   const bool has_start = grid != 1 && start_3d;
@@ -429,8 +444,8 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   // moves chunk c's outputs from its slot's staging into the caller's arrays
   auto finish = [&](int c) -> int {
     const int k = c % nslot;
-    const long long c0 = (long long)c * C;
-    const size_t nc = (size_t)((n2 - c0) < C ? (n2 - c0) : C);
+    const long long c0 = bound[c];
+    const size_t nc = (size_t)(bound[c + 1] - bound[c]);
     const cudaError_t we = cudaEventSynchronize(pl->done[k]);
     if (we != cudaSuccess) return cuda_fail(we, "device-to-host copy");
     const char *h = pl->pinned + k * slot_out;
@@ -449,9 +464,8 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   const char *hps = (const char *)ps, *hts = (const char *)ts, *htds = (const char *)tds;
   int issued = 0;
   for (int c = 0; c < nchunk; ++c) {
-    const long long c0 = (long long)c * C;
-    if (c0 >= n2) break;
-    const int nc = (int)((n2 - c0) < C ? (n2 - c0) : C);
+    const long long c0 = bound[c];
+    const int nc = (int)(bound[c + 1] - bound[c]);  // never 0: chunks of 2+ hold 65,536+
     const int k = c % nslot;
     if (c >= nslot) {
       // the slot still holds chunk c - nslot: its outputs leave the staging
