@@ -394,7 +394,7 @@ def run_ours(args):
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(5, min(args.steps, 10))
     for _ in range(e2e_steps):
         e2e_step()
     e2e_dt = max_over_ranks(dist, (time.perf_counter() - t0) / e2e_steps, dev)
