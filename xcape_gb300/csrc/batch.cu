@@ -16,7 +16,9 @@
 // until the space is exhausted (a persistent grid of one wave of blocks),
 // finds the chunk's request by a warp-uniform binary search, and each lane
 // runs one column with the column routine of the single-request kernels
-// (cape_column.cuh), selected at run time by grid kind and adiabat.
+// (cape_column.cuh; for the learned solver cape_learned.cuh, whose guess
+// network the converged warp evaluates for its 32 columns on the tensor
+// cores), selected at run time by grid kind and adiabat.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -26,6 +28,7 @@
 
 #include "../../include/xcape_gb300.h"
 #include "cape_column.cuh"
+#include "cape_learned.cuh"
 #include "xc_kernels.h"
 
 namespace xc {
@@ -50,9 +53,7 @@ size_t table_bytes(int max_requests) {
   return kHeaderBytes + sizeof(BatchReq) * (size_t)max_requests;
 }
 
-template <int SOLVER>
-__device__ void run_request_column(const xc_cape_request &q, long long i, const float *gw,
-                                   int &nsub, int &niter) {
+__device__ __forceinline__ CapeArgs request_args(const xc_cape_request &q) {
   CapeArgs a;
   a.grid = q.grid;
   a.dtype = 0;
@@ -78,7 +79,14 @@ __device__ void run_request_column(const xc_cape_request &q, long long i, const 
   a.status = q.status;
   a.counters = nullptr;
   a.perm = nullptr;
-  a.guess_w = gw;
+  a.guess_w = nullptr;
+  return a;
+}
+
+template <int SOLVER>
+__device__ void run_request_column(const xc_cape_request &q, long long i, int &nsub, int &niter) {
+  const CapeArgs a = request_args(q);
+  const float *gw = nullptr;
   const bool ice = q.adiabat >= 3, pseudo = (q.adiabat == 1 || q.adiabat == 3);
   if (q.grid == 1) {
     if (ice && pseudo) cape_column_run<float, 1, true, true, SOLVER>(a, i, nsub, niter, gw);
@@ -93,18 +101,37 @@ __device__ void run_request_column(const xc_cape_request &q, long long i, const 
   }
 }
 
+// Column i of a request with the learned solver; every lane of the warp
+// calls it (lanes past the request's n2 take part in the network's
+// evaluation and write nothing).
+__device__ void run_request_column_learned(const xc_cape_request &q, long long i,
+                                           const WarpNetSmem &net, LearnedPrep *prep, int &nsub,
+                                           int &niter) {
+  const CapeArgs a = request_args(q);
+  const bool ice = q.adiabat >= 3, pseudo = (q.adiabat == 1 || q.adiabat == 3);
+  if (q.grid == 1) {
+    if (ice && pseudo) learned_column<float, 1, true, true>(a, net, prep, i, nsub, niter);
+    else if (ice) learned_column<float, 1, true, false>(a, net, prep, i, nsub, niter);
+    else if (pseudo) learned_column<float, 1, false, true>(a, net, prep, i, nsub, niter);
+    else learned_column<float, 1, false, false>(a, net, prep, i, nsub, niter);
+  } else {
+    if (ice && pseudo) learned_column<float, 2, true, true>(a, net, prep, i, nsub, niter);
+    else if (ice) learned_column<float, 2, true, false>(a, net, prep, i, nsub, niter);
+    else if (pseudo) learned_column<float, 2, false, true>(a, net, prep, i, nsub, niter);
+    else learned_column<float, 2, false, false>(a, net, prep, i, nsub, niter);
+  }
+}
+
 // counters: [0] the chunk counter, [1] sub-steps, [2] iterations.
 template <int SOLVER>
-__global__ void __launch_bounds__(128) cape_batch_kernel(const unsigned char *table,
-                                                         unsigned long long *counters,
-                                                         const float *guess_w) {
-  extern __shared__ __align__(16) float guess_sm[];
-  const float *gw = nullptr;
+__global__ void __launch_bounds__(LEARNED_THREADS) cape_batch_kernel(const unsigned char *table,
+                                                                     unsigned long long *counters,
+                                                                     const WarpNetSmem *net_img) {
+  __shared__ WarpNetSmem net;                    // SOLVE_LEARNED only
+  __shared__ LearnedPrep prep[LEARNED_THREADS];  // SOLVE_LEARNED only
   if (SOLVER == SOLVE_LEARNED) {
-    for (int k = threadIdx.x; k < GUESS_NPARAM; k += blockDim.x)
-      guess_sm[k] = guess_packed_value(guess_w, k);
+    copy_warp_net(net, net_img);
     __syncthreads();
-    gw = guess_sm;
   }
   const BatchHeader hdr = *reinterpret_cast<const BatchHeader *>(table);
   const BatchReq *reqs = reinterpret_cast<const BatchReq *>(table + kHeaderBytes);
@@ -124,12 +151,14 @@ __global__ void __launch_bounds__(128) cape_batch_kernel(const unsigned char *ta
       else hi = mid - 1;
     }
     const long long i = g + lane - reqs[lo].col0;
-    if (i < reqs[lo].q.n2) {
-      int nsub = 0, niter = 0;
-      run_request_column<SOLVER>(reqs[lo].q, i, gw, nsub, niter);
-      nsub_sum += nsub;
-      niter_sum += niter;
+    int nsub = 0, niter = 0;
+    if (SOLVER == SOLVE_LEARNED) {
+      run_request_column_learned(reqs[lo].q, i, net, prep, nsub, niter);
+    } else if (i < reqs[lo].q.n2) {
+      run_request_column<SOLVER>(reqs[lo].q, i, nsub, niter);
     }
+    nsub_sum += nsub;
+    niter_sum += niter;
   }
   for (int o = 16; o > 0; o >>= 1) {
     nsub_sum += __shfl_down_sync(0xffffffffu, nsub_sum, o);
@@ -143,9 +172,9 @@ __global__ void __launch_bounds__(128) cape_batch_kernel(const unsigned char *ta
 
 template <int SOLVER>
 cudaError_t capture_batch(cudaStream_t cs, unsigned char *dtable, const unsigned char *htable,
-                          size_t bytes, unsigned long long *counters, const float *gw,
+                          size_t bytes, unsigned long long *counters, const WarpNetSmem *gw,
                           cudaGraph_t *graph) {
-  const size_t smem = SOLVER == SOLVE_LEARNED ? sizeof(float) * GUESS_NPARAM : 0;
+  const size_t smem = 0;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -223,10 +252,15 @@ int xc_batch_create(int max_requests, long long max_columns, int guess, xc_batch
   if (guess != XC_GUESS_PLAIN && guess != XC_GUESS_LEARNED && guess != XC_GUESS_EXTRAPOLATED)
     return xc::set_error(XC_ERR_INVALID,
                           "xc_batch_create: guess must be XC_GUESS_PLAIN, _LEARNED or _EXTRAPOLATED");
-  const float *gw = nullptr;
+  const xc::WarpNetSmem *gw = nullptr;  // the learned kernel's image of the guess network
   if (guess == XC_GUESS_LEARNED) {
-    const int rc = xc::guess_weights_ptr(&gw);
+    const float *w = nullptr;
+    const int rc = xc::guess_weights_ptr(&w);  // fails unless a network is loaded
     if (rc) return rc;
+    const void *img = nullptr;
+    const cudaError_t ie = xc::warp_net_image(&img);
+    if (ie != cudaSuccess) return cuda_err(ie, "xc_batch_create: the guess network's image");
+    gw = (const xc::WarpNetSmem *)img;
   }
   xc_batch *b = new (std::nothrow) xc_batch();
   if (!b) return xc::set_error(XC_ERR_NOMEM, "xc_batch_create: host allocation");
