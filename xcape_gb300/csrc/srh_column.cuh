@@ -214,9 +214,9 @@ struct SrhPass1 {
 // Pass 1 (see the file comment) as a sweep that takes levels 2..ncl in
 // order, one step per level: the hypsometric height (FP64, or FP32 with
 // Kahan compensation when F32), the 12 Bunkers targets (DEC selects the
-// scan rule) and the SREH top level.  A kernel can feed it levels from
-// global memory (srh_pass1) or from rows staged in shared memory a window at
-// a time (srh_window_kernel); the operations are the same.
+// scan rule) and the SREH top level.  srh_pass1 feeds it the levels through
+// a reader: global memory (GlobalLevels) or rows that srh_tile_kernel staged
+// in shared memory (SharedLevels); the operations are the same.
 template <bool DEC, bool F32>
 struct SrhSweep {
   typedef typename SrhReal<F32>::type R;
