@@ -137,6 +137,32 @@ def test_learned_mode_against_extrapolated_mode():
     assert lrn["niter_total"] < ext["niter_total"], (lrn["niter_total"], ext["niter_total"])
 
 
+@pytest.mark.parametrize("bad", ["nan", "large"])
+def test_learned_mode_without_a_usable_network_falls_back_to_extrapolation(bad):
+    """NaN weights, or an output bias of 1000 (far outside the output range):
+    the tensor-core evaluation's output is rejected for every column and the
+    learned kernel runs the extrapolated solver's ascent -- same levels,
+    sources and work within the solver tolerance (the two are compiled into
+    different kernels)."""
+    w = np.array(G.read()[0] if os.path.exists(G.DEFAULT_PATH) else _network(), np.float32)
+    if bad == "nan":
+        w[:] = np.nan
+    else:
+        w[G.OFF_B3] = 1000.0
+    try:
+        G.set_weights(w)
+        lrn = _run(_lib.XC_GUESS_LEARNED)
+        ext = _run(_lib.XC_GUESS_EXTRAPOLATED)
+    finally:
+        G.set_weights(_network())
+    for k in ("mulvl", "status"):
+        np.testing.assert_array_equal(lrn[k], ext[k], err_msg=k)
+    for k in ("cape", "cin", "z_out"):
+        np.testing.assert_allclose(lrn[k], ext[k], rtol=2e-4, atol=0.5, err_msg=k)
+    assert lrn["nsub_total"] == ext["nsub_total"]
+    assert abs(lrn["niter_total"] - ext["niter_total"]) <= 1e-3 * ext["niter_total"]
+
+
 @pytest.mark.parametrize("adiabat", ["pseudo-liquid", "reversible-liquid", "pseudo-ice",
                                      "reversible-ice"])
 def test_network_saves_iterations_on_every_adiabat(adiabat):

@@ -80,3 +80,24 @@ def test_emulated_learned_and_secant_modes_vs_fp64(guess):
     assert not np.any((got["status"] & 1) & conv)
     d = np.abs(got["cape"][conv].astype(np.float64) - ref["cape"][conv])
     assert np.all(d <= np.maximum(1.0, 1e-3 * ref["cape"][conv])), d.max()
+
+
+@pytest.mark.parametrize("bad", ["nan", "large"])
+def test_emulated_learned_mode_without_a_usable_network_is_the_extrapolated_mode(bad):
+    """A network whose output is not finite or outside its range (here: NaN
+    weights, or an output bias of 1000) leaves the learned solver with the
+    extrapolated guess everywhere: the host build gives the extrapolated
+    solver's results and work counts exactly."""
+    from test_kernel_emulation import _emu_cape
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(16, 48))
+    w = G.bf16_round(G.init_weights(5, 0.3))
+    if bad == "nan":
+        w[:] = np.nan
+    else:
+        w[G.OFF_B3] = 1000.0
+    for source in (1, 2, 3):
+        lrn = _emu_cape(2, plev, t, td, ps, ts, tds, source, 1, guess=1, guess_w=w)
+        ext = _emu_cape(2, plev, t, td, ps, ts, tds, source, 1, guess=2)
+        for k in ("cape", "cin", "mulvl", "z_out", "status", "counters"):
+            np.testing.assert_array_equal(lrn[k], ext[k], err_msg=f"{k}, source {source}")
+
