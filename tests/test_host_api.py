@@ -169,6 +169,37 @@ def test_cape_srh_arguments_are_checked_before_any_cuda_call(p_t_td_3d, p_t_td_s
         X.calc_cape_srh(p, t, td, t, td, ps, ts, tds, ps, ts, precision="fp16")
 
 
+def test_python_constants_match_the_header():
+    """Every XC_* integer the Python layer mirrors has the header's value."""
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                       "xcape_gb300.h")
+    defines = dict(re.findall(r"^#define (XC_\w+) (-?\d+)", open(hdr).read(), re.M))
+    mirrored = {k: getattr(_lib, k) for k in dir(_lib) if k.startswith("XC_") and
+                isinstance(getattr(_lib, k), int)}
+    assert len(mirrored) >= 10
+    for k, v in mirrored.items():
+        assert k in defines and int(defines[k]) == v, k
+    for k in ("COL_NOCONV", "COL_BADSTART", "COL_TOOMANYSTEPS"):
+        assert int(defines["XC_" + k]) == getattr(_lib, k), k
+
+
+def test_empty_inputs_and_level_limit_without_gpu():
+    """No columns: calc_cape / calc_srh return empty arrays of the right shape
+    (the host entry points return before any CUDA call).  More levels than
+    XC_MAX_LEVELS: the library refuses the call with a status, no work."""
+    p = np.zeros((0, 37), np.float32)
+    sf = np.zeros(0, np.float32)
+    cape, cin, mulev, zmulev = calc_cape(p, p, p, sf, sf, sf, source="most-unstable")
+    assert cape.shape == cin.shape == mulev.shape == zmulev.shape == (0,)
+    srh_rm, srh_lm = calc_srh(p, p, p, p, p, sf, sf, sf, sf, sf)
+    assert srh_rm.shape == srh_lm.shape == (0,)
+    nk = _lib.XC_MAX_LEVELS + 1
+    tall = np.zeros((2, nk), np.float32)
+    with pytest.raises(_lib.XcapeError, match="nk="):
+        calc_cape(tall, tall, tall, np.zeros(2, np.float32), np.ones(2, np.float32),
+                  np.zeros(2, np.float32))
+
+
 def test_python_raises_library_errors():
     with pytest.raises(_lib.XcapeError, match="status 1"):
         _lib.call("xc_loopcape_ml", None, None, None, None, None, None, 0, 500.0, 4, 500.0, 1,

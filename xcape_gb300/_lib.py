@@ -24,6 +24,7 @@ XC_GUESS_EXTRAPOLATED = 2
 XC_GUESS_SECANT = 3
 XC_GUESS_LEARNED_EVERY = 4
 XC_GUESS_NPARAM = 4481
+XC_MAX_LEVELS = 4096
 
 COL_NOCONV = 1
 COL_BADSTART = 2
