@@ -76,6 +76,23 @@ def test_fused_kernel_on_f64_inputs(grid):
         _same_cape(cape_f, cape_s, exact=guess == "plain")
 
 
+@pytest.mark.parametrize("guess", ["plain", "learned"])
+def test_fused_partial_warps(guess):
+    """1,517 columns (a partial last warp and block), pressure levels with
+    ragged starts: the lanes past the last column take part in the guess
+    network's evaluation and write nothing."""
+    args = S.pressure_srh(shape=(37, 41), seed=8)
+    p, t, td, u, v, ps, ts, tds, us, vs = args
+    cape_f, srh_f = X.calc_cape_srh(*args, source="most-unstable", vertical_lev="pressure",
+                                    output_var="all", guess=guess, precision="reference")
+    cape_s = X.calc_cape(p, t, td, ps, ts, tds, source="most-unstable", vertical_lev="pressure",
+                         guess=guess)
+    srh_s = X.calc_srh(*args, vertical_lev="pressure", output_var="all", precision="reference")
+    for g, w in zip(srh_f, srh_s):
+        np.testing.assert_array_equal(g, w)
+    _same_cape(cape_f, cape_s, exact=guess == "plain")
+
+
 @pytest.mark.parametrize("grid", ["model", "pressure"])
 def test_fused_srh_against_the_oracle(grid):
     """SRH at the reference precision against the oracle's calc_srh (the CAPE
