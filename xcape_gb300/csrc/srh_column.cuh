@@ -74,17 +74,20 @@ XC_HD double stdh_step(double Hprev, double Tv, double Tvprev, double P, double 
 }
 
 // FP32 forms of the two stdheight formulas, for the FP32 SRH path (the
-// height is then accumulated with Kahan compensation, see srh_pass1).
+// height is then accumulated with Kahan compensation, see srh_pass1).  Its
+// contract is agreement with FP64 within tolerance, so they use the
+// approximate exp, log and divides (exact on the host).
 XC_HD float stdh_tv_f(float P, float T, float Td) {
   const float eps = 0.6219800858985514f;
   const float Tin = T + 273.15f;
   const float Tdin = Td + 273.15f;
-  const float E = nc_mul(6.112f, expf((53.49f - (6808.0f / Tdin) - nc_mul(5.09f, logf(Tdin)))));
-  const float w = nc_mul(eps, (E / (P - E)));
-  return nc_mul(Tin, ((w + eps) / (eps * (1.0f + w))));
+  const float E =
+      nc_mul(6.112f, fast_exp((53.49f - fast_div(6808.0f, Tdin) - nc_mul(5.09f, fast_log(Tdin)))));
+  const float w = nc_mul(eps, fast_div(E, P - E));
+  return nc_mul(Tin, fast_div(w + eps, eps * (1.0f + w)));
 }
 XC_HD float stdh_dh_f(float Tv, float Tvprev, float P, float Pprev) {
-  return nc_mul(((287.04f * ((Tv + Tvprev) / 2.0f) / -9.80665f)), logf(P / Pprev));
+  return nc_mul(fast_div(287.04f * ((Tv + Tvprev) / 2.0f), -9.80665f), fast_log(fast_div(P, Pprev)));
 }
 
 // Real type of the stdheight / SREH stages: double as in the reference, or
