@@ -14,9 +14,9 @@ namespace xc {
 // (below), which evaluates its guess network per warp on the tensor cores.
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER>
 __global__ void __launch_bounds__(128) cape_kernel(CapeArgs a) {
-  extern __shared__ __align__(16) float guess_sm[];  // packed guess network, SOLVE_LEARNED*
+  extern __shared__ __align__(16) float guess_sm[];  // packed guess network, SOLVE_LEARNED_ALL
   const float *gw = nullptr;
-  if (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) {
+  if (SOLVER == SOLVE_LEARNED_ALL) {
     for (int k = threadIdx.x; k < GUESS_NPARAM; k += blockDim.x)
       guess_sm[k] = guess_packed_value(a.guess_w, k);
     __syncthreads();
@@ -216,8 +216,7 @@ template <typename T, int GRID, int SOLVER>
 static void launch_cape_s(const CapeArgs &a, unsigned blocks, int threads, cudaStream_t s) {
   const bool ice = a.adiabat >= 3;
   const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
-  const size_t sm =
-      (SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_ALL) ? sizeof(float) * GUESS_NPARAM : 0;
+  const size_t sm = SOLVER == SOLVE_LEARNED_ALL ? sizeof(float) * GUESS_NPARAM : 0;
   if (ice && pseudo)
     cape_kernel<T, GRID, true, true, SOLVER><<<blocks, threads, sm, s>>>(a);
   else if (ice)
