@@ -112,33 +112,144 @@ def max_over_ranks(dist, value, device=None):
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 
+# NVML's clock-event reason bits (nvml.h, nvmlClocksEventReason*), under the
+# names nvidia-smi prints for them.
+NVML_REASONS = ((0x4, "sw_power_cap"), (0x8, "hw_slowdown"), (0x20, "sw_thermal_slowdown"),
+                (0x40, "hw_thermal_slowdown"), (0x80, "hw_power_brake_slowdown"))
+
+
+class NvmlReader:
+    """Read-only NVML queries (SM clock, its maximum, clock-event reasons,
+    power) for the GPU behind one CUDA device, through ctypes.
+
+    The GPU is found by the CUDA device's UUID, else its PCI bus id, because
+    CUDA's device numbering (CUDA_VISIBLE_DEVICES) need not be NVML's.  It
+    only reads: no clock, power or mode setting is touched."""
+
+    def __init__(self, device_index, lib=None, props=None):
+        import ctypes
+        self.ct = ctypes
+        if lib is None:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if props is None:
+            import torch
+            props = torch.cuda.get_device_properties(device_index)
+        rc = lib.nvmlInit_v2()
+        if rc:
+            raise OSError(f"nvmlInit_v2 returned {rc}")
+        self.lib = lib
+        self.h = ctypes.c_void_p()
+        found = False
+        uuid = getattr(props, "uuid", None)
+        if uuid is not None:
+            u = str(uuid)
+            u = u if u.startswith(("GPU-", "MIG-")) else "GPU-" + u
+            found = lib.nvmlDeviceGetHandleByUUID(u.encode(), ctypes.byref(self.h)) == 0
+        if not found and hasattr(props, "pci_bus_id"):
+            bus = f"{props.pci_domain_id:08x}:{props.pci_bus_id:02x}:{props.pci_device_id:02x}.0"
+            found = lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) == 0
+        if not found:
+            lib.nvmlShutdown()
+            raise OSError("no NVML device for this CUDA device")
+        self._reasons = (getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+                         or lib.nvmlDeviceGetCurrentClocksThrottleReasons)
+        mx = ctypes.c_uint(0)
+        self.max_mhz = (float(mx.value)
+                        if lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0 else None)
+
+    def sample(self):
+        """(SM MHz, reason bits, watts or None), or None if a query failed."""
+        ct = self.ct
+        mhz, bits, mw = ct.c_uint(0), ct.c_ulonglong(0), ct.c_uint(0)
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(mhz)) != 0:  # NVML_CLOCK_SM
+            return None
+        if self._reasons(self.h, ct.byref(bits)) != 0:
+            return None
+        watts = mw.value / 1e3 if self.lib.nvmlDeviceGetPowerUsage(self.h, ct.byref(mw)) == 0 else None
+        return float(mhz.value), int(bits.value), watts
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class ClockSampler:
+    """SM clocks and clock-event reasons of this process's GPU while the
+    timed region runs (the `with` block holds exactly that region).
+
+    NVML is polled every 2 ms from a thread, and once on entry and once on
+    exit, so a timed region of a few tens of milliseconds still holds many
+    samples.  Without NVML it falls back to an `nvidia-smi -lms 200` loop
+    (started before the region, so at least one sample falls near it)."""
+
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_S = 0.002
 
-    def __init__(self, index):
+    def __init__(self, index, reader=None):
         self.index = index
+        self.reader = reader
+        self.source = None
         self.proc = None
         self.lines = []
+        self.samples = []  # (SM MHz, reason bits, watts) from NVML
+        self._stop = threading.Event()
+        self.thread = None
 
     def __enter__(self):
+        if self.reader is None:
+            try:
+                self.reader = NvmlReader(self.index)
+            except Exception:
+                self.reader = None
+        if self.reader is not None:
+            self.source = "nvml"
+            self._take()
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
+            sel = str(self.index)
+            try:
+                import torch
+                u = str(torch.cuda.get_device_properties(self.index).uuid)
+                sel = u if u.startswith("GPU-") else "GPU-" + u
+            except Exception:
+                pass
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                ["nvidia-smi", "-i", sel, f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            self.source = "nvidia-smi"
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
+
+    def _take(self):
+        s = self.reader.sample()
+        if s is not None:
+            self.samples.append(s)
+
+    def _poll(self):
+        while not self._stop.wait(self.PERIOD_S):
+            self._take()
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *exc):
+        if self.reader is not None:
+            self._stop.set()
+            if self.thread is not None:
+                self.thread.join(timeout=5)
+            self._take()
+            self.reader.close()
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -147,7 +258,15 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
+        sm, mx, power, reasons = [], [], [], set()
+        if self.samples:
+            for mhz, bits, watts in self.samples:
+                sm.append(mhz)
+                if watts is not None:
+                    power.append(watts)
+                reasons.update(name for bit, name in NVML_REASONS if bits & bit)
+            if self.reader.max_mhz is not None:
+                mx.append(self.reader.max_mhz)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
             f = [x.strip() for x in line.split(",")]
@@ -158,14 +277,21 @@ class ClockSampler:
                 mx.append(float(f[2]))
             except ValueError:
                 continue
+            try:
+                power.append(float(f[3]))
+            except ValueError:
+                pass
             for name, val in zip(names, f[5:9]):
                 if val.lower() == "active":
                     reasons.add(name)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
-        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(mx)),
-                "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(mx)) if mx else None,
+               "reasons": sorted(reasons), "samples": len(sm), "source": self.source}
+        if power:
+            out["power_w_median"] = float(np.median(power))
+        return out
 
 
 # ---------------------------------------------------------------------------
