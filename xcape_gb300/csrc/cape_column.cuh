@@ -125,10 +125,11 @@ struct CapeResult {
 //                (guess_mlp.cuh), entered as the extrapolation history when
 //                the parcel saturates.  The network is evaluated once per column,
 //                before the ascent, at the parcel's lifting condensation
-//                level (parcel_lcl_slope), where every thread of a warp
-//                evaluates it together; inside the sub-step loop the
-//                threads that reach saturation at different sub-steps
-//                would evaluate it one after another.
+//                level (lcl_features), where the threads of a warp evaluate
+//                it together (warp_guess_eval, cape_learned.cuh; per thread
+//                through parcel_lcl_slope in the diagnostics kernel); inside
+//                the sub-step loop the threads that reach saturation at
+//                different sub-steps would evaluate it one after another.
 //   SOLVE_LEARNED_ALL: the network's guess on every sub-step that starts
 //                saturated, th1 on the others; secant steps.
 //   SOLVE_SECANT: first guess th1 (the reference's), secant steps -- the
