@@ -52,7 +52,7 @@ def test_sampler_polls_during_the_region_and_names_reasons():
     reader = bench.NvmlReader(0, lib=fake, props=SimpleNamespace(uuid="1234"))
     assert fake.uuid == b"GPU-1234"
     with bench.ClockSampler(0, reader=reader) as clk:
-        time.sleep(0.05)
+        time.sleep(0.1)
     s = clk.summary()
     assert fake.shut
     assert s["source"] == "nvml"
