@@ -41,17 +41,18 @@ ADIABAT = 1
 METRIC = "CAPE/CIN columns/s at 1M×37 lev: learned-guess vs plain CUDA, |ΔCAPE|≤1 J/kg"
 SRH_METRIC = "SRH columns/s at 1M×50 lev (calc_srh, depth 1000+3000 m)"
 CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
-# DRAM bytes (read + write) of one most-unstable launch of the lift on this
-# workload, from `ncu --set full` captures of `bench.py --profile`.
+# Recorded values, not measurements of the run that prints them: DRAM bytes
+# (read + write) of one most-unstable launch of the lift on this workload, and
+# the issue-slot activity (smsp__issue_active over active cycles), tensor-pipe
+# share and active threads per warp instruction, from `ncu --set full`
+# captures of `bench.py --profile` (profiles/cape_kernel_pressure_1M.md).
+NCU_RECORDED = "ncu --set full of bench.py --profile, profiles/cape_kernel_pressure_1M.md"
 NCU_TRAFFIC = {"learned": 702_052_608, "plain": 725_578_496}
-# The lift is bound by the SM issue rate, not by HBM: issue-slot activity of
-# the same captures (smsp__issue_active, % of peak over active cycles) and the
-# tensor pipe's share (the learned kernel's guess network).
 NCU_ISSUE = {"learned": {"issue_active": 0.844, "tensor_pipe_active": 0.0079,
                          "threads_per_warp_instruction": 28.98},
              "plain": {"issue_active": 0.879, "tensor_pipe_active": 0.0,
                        "threads_per_warp_instruction": 27.11}}
-ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg
+ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg (strided)
 CPU_SAMPLE_1T = 8192     # columns per single-core CPU-baseline measurement
 REF_SAMPLE = 32768       # columns per --impl reference step
 
@@ -331,19 +332,26 @@ def cpu_cape(sample, nthreads):
     return sample / (time.perf_counter() - t0)
 
 
-def accuracy_vs_fp64(outs, nthreads):
-    """|dCAPE|, |dCIN| of the timed launches' outputs on the first ACC_SAMPLE
-    columns against the FP64 oracle (the checker), over the columns whose
-    FP64 iteration converges and, for most-unstable parcels, whose source
-    level is the same (theta-e near-ties pick another parcel)."""
+def accuracy_vs_fp64(outs, nthreads, host):
+    """|dCAPE|, |dCIN| of the timed launches' outputs on ACC_SAMPLE columns
+    taken with a constant stride over the whole 721 x 1440 grid (every
+    latitude band of the synthetic field, hence the whole ps range) against
+    the FP64 oracle (the checker), over the columns whose FP64 iteration
+    converges and, for most-unstable parcels, whose source level is the same
+    (theta-e near-ties pick another parcel)."""
     import oracle as O
-    plev, t, td, ps, ts, tds = cape_inputs(0, ACC_SAMPLE)
+    import torch
+    plev, t, td, ps, ts, tds = host
+    n2 = ps.shape[0]
+    idx = np.arange(ACC_SAMPLE, dtype=np.int64) * (n2 // ACC_SAMPLE)
+    t, td, ps, ts, tds = (np.ascontiguousarray(a[idx]) for a in (t, td, ps, ts, tds))
     start = O.pres_lev_pos(plev, ps)
-    res = {"columns": ACC_SAMPLE}
+    res = {"columns": ACC_SAMPLE, "sample": f"every {n2 // ACC_SAMPLE}th column of {n2}"}
     for src, code in SOURCES:
         ref = O.loopcape(plev, t, td, ps, ts, tds, PINC, code, ML_DEPTH, ADIABAT, start=start,
                          p_is_1d=True, nthreads=nthreads, precision="f64", stats=True)
-        cape, cin, _, mulvl = (x[:ACC_SAMPLE].cpu().numpy() for x in outs[src])
+        sel = torch.from_numpy(idx).to(outs[src][0].device)
+        cape, cin, _, mulvl = (x.index_select(0, sel).cpu().numpy() for x in outs[src])
         ok = (ref["status"] & 1) == 0
         if code == 2:
             ok &= mulvl == ref["mulvl"]
@@ -354,6 +362,70 @@ def accuracy_vs_fp64(outs, nthreads):
                     "frac_dcin_le_1_or_0.1pct": float(np.mean(
                         dn <= np.maximum(1.0, 1e-3 * np.abs(ref["cin"][ok]))))}
     return res
+
+
+def column_levels(plev, ps, ts):
+    """Per-column work units of the lift, from the inputs: the levels each
+    column's passes walk (surface included: nk - start + 2, for columns with
+    ts > 0, CAPE_CODE_model_lev.f90:77), and of them the levels at or below
+    500 hPa that the most-unstable search evaluates theta-e on (:261-281).
+    start is the reference's masked-argmin rule (src/xcape/core.py:286-289)."""
+    nk = plev.shape[0]
+    d = ps[None, :].astype(np.float64) - plev[:, None].astype(np.float64)
+    start = np.ma.masked_less(d, 0).argmin(axis=0).astype(np.int64) + 1
+    live = ts > 0
+    ncl = np.where(live, nk - start + 2, 0)
+    ge500 = np.cumsum((plev >= 500.0)[::-1])[::-1]           # levels >= 500 hPa from k on
+    nmu = np.where(live, 1 + ge500[start - 1], 0)             # + the surface
+    return {"columns": int(live.sum()), "levels": int(ncl.sum()), "levels_mu": int(nmu.sum())}
+
+
+# XU (transcendental unit) lane operations of the accelerated solvers per unit
+# of work, counted from the column code (cape_column.cuh, xc_common.cuh): each
+# approximate exp (ex2), log (lg2) and divide (rcp) is one XU operation.
+#   environment of a level (make_env<true>): pi = exp(k ln p) 2, getqvs_fast
+#     3, theta and theta_v 2                                          -> 7
+#   ascent level: the environment + the two buoyancy divides          -> 9
+#   most-unstable level (p >= 500 hPa): getqvs_fast 3 + getthe_fast 9 -> 12
+#   mixed-layer pass level: the environment                           -> 7
+#   sub-step: ln p2, pi2, and the analytic slope's two divides        -> 4
+#   iteration (accel_map, liquid): qsat 3, exponent 1, exp 1          -> 5
+#   step between iterations (secant quotient, root step)             -> 2
+XU_MODEL = {"ascent_level": 9, "mu_level": 12, "ml_level": 7, "substep": 4, "iteration": 5,
+            "step": 2}
+# FP32 lane operations (FFMA, FADD, FMUL, FMNMX, FSETP and the multiplies of
+# the approximate functions) of the same code, per unit.
+FP32_MODEL = {"ascent_level": 30, "mu_level": 35, "ml_level": 25, "substep": 25,
+              "iteration": 45, "step": 12}
+
+
+def model_ops(model, work, lev, source_code):
+    """Operations of `model` for one launch: work = (sub-steps, iterations)
+    from the kernel's counters, lev = column_levels()."""
+    nsub, niter = work
+    ops = model["ascent_level"] * lev["levels"] + model["substep"] * nsub \
+        + model["iteration"] * niter + model["step"] * max(0, niter - nsub)
+    if source_code == 2:
+        ops += model["mu_level"] * lev["levels_mu"]
+    elif source_code == 3:
+        ops += model["ml_level"] * lev["levels"]
+    return float(ops)
+
+
+def pipe_peaks(L, stream_ptr):
+    """FP32 and XU lane-operation rates of this GPU (xc_measure_pipe_peaks),
+    best of three."""
+    import ctypes
+    best = [0.0, 0.0]
+    for _ in range(3):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        rc = L.xc_measure_pipe_peaks(ctypes.byref(a), ctypes.byref(b), stream_ptr)
+        if rc != 0:
+            return None
+        best = [max(best[0], a.value), max(best[1], b.value)]
+    return {"fp32_gops": best[0], "xu_gops": best[1],
+            "how": "xc_measure_pipe_peaks: 8 independent FFMA chains / 8 independent "
+                   "ex2.approx chains per thread, 8 x 256 threads per SM, CUDA events, best of 3"}
 
 
 def run_reference(args):
@@ -537,16 +609,34 @@ def run_ours(args):
     # in, cape/cin/z_out/mulvl out, p1d once.
     bytes_per_launch = n2 * (2 * NLEV * 4 + 3 * 4 + 4 * 4) + NLEV * 4
     top = max(per_src_ms, key=per_src_ms.get)
-    achieved = bytes_per_launch / (per_src_ms[top] / 1e3) / 1e9
+    top_code = dict(SOURCES)[top]
+    top_s = per_src_ms[top] / 1e3
     clocks = clk.summary()
-    # FP32 work: 60 ops per fixed-point iteration, 10 per sub-step, 40 per
-    # level (counted from CAPE_CODE_model_lev.f90:232-248, 417-547, each
-    # exp/log/pow/divide as one op), against the nominal FP32 lane rate.
-    nsub, niter = work[top]
-    flops = 60.0 * niter + 10.0 * nsub + 40.0 * n2 * NLEV
-    sm_mhz = clocks.get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fp32_ach = flops / (per_src_ms[top] / 1e3) / 1e12
+    roof = {"hbm": {"achieved": bytes_per_launch / top_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "peak_kind": peak_kind, "algorithmic_bytes": bytes_per_launch}}
+    peaks = pipe_peaks(L, sptr)
+    lev = column_levels(plev, ps, ts)
+    if peaks and guess != _lib.XC_GUESS_PLAIN:
+        # the compute side: FP32 and XU lane operations of the launch (the
+        # op model above, on the kernel's own sub-step and iteration
+        # counters) against the rates measured on this GPU
+        for key, model, pk in (("fp32", FP32_MODEL, peaks["fp32_gops"]),
+                               ("xu", XU_MODEL, peaks["xu_gops"])):
+            ops = model_ops(model, work[top], lev, top_code)
+            roof[key] = {"achieved": ops / top_s / 1e9, "peak": pk, "unit": "Gop/s",
+                         "peak_kind": "measured (xc_measure_pipe_peaks)", "ops": ops}
+    for v in roof.values():
+        v["frac"] = v["achieved"] / v["peak"]
+    bound = max(roof, key=lambda k: roof[k]["frac"])
+    kernel = (f"cape_learned_kernel ({top})" if args.guess == "learned"
+              else f"cape_kernel ({top})")
+    roofline = {"bound": bound, "achieved": roof[bound]["achieved"], "peak": roof[bound]["peak"],
+                "unit": roof[bound]["unit"], "frac": roof[bound]["frac"],
+                "traffic": NCU_TRAFFIC.get(args.guess), "kernel": kernel,
+                "traffic_source": f"recorded: {NCU_RECORDED}" if args.guess in NCU_TRAFFIC
+                else None,
+                "components": roof,
+                "work": {"substeps": work[top][0], "iterations": work[top][1], **lev}}
     line = {
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max,
@@ -558,21 +648,10 @@ def run_ours(args):
                    "columns": cols_all, "levels": NLEV, "guess": args.guess,
                    "column_order": "start level x surface dewpoint" if order else "natural",
                    "l2": "inputs (307 MB) larger than L2 (129 MB), no flush"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak,
-                     "traffic": NCU_TRAFFIC.get(args.guess),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one "
-                                       "most-unstable launch of this workload"
-                     if args.guess in NCU_TRAFFIC else None,
-                     "kernel": (f"cape_learned_kernel ({top})" if args.guess == "learned"
-                                else f"cape_kernel ({top})"),
-                     "peak_kind": peak_kind,
-                     "note": "compute-bound kernel: see fp32 entry"},
-        "issue_roofline": dict(NCU_ISSUE.get(args.guess, {}),
-                               source="ncu --set full, one most-unstable launch")
+        "roofline": roofline,
+        "pipe_peaks": peaks,
+        "issue_roofline": dict(NCU_ISSUE.get(args.guess, {}), source=f"recorded: {NCU_RECORDED}")
         if args.guess in NCU_ISSUE else None,
-        "fp32": {"achieved_tflops": fp32_ach, "peak_tflops_nominal": fp32_peak,
-                 "frac": fp32_ach / fp32_peak, "iterations": niter, "substeps": nsub},
         "per_source_ms": per_src_ms,
         "vs_plain": ({"plain_value": cols_all / (sum(plain_ms.values()) / 1e3),
                       "plain_per_source_ms": plain_ms,
@@ -596,7 +675,7 @@ def run_ours(args):
                                           "oracle (C restatement of the Fortran), OpenMP",
                                 "single_core": {"value": v1, "cores": 1,
                                                 "sample": f"first {CPU_SAMPLE_1T} columns"}}
-        line["accuracy_vs_fp64"] = accuracy_vs_fp64(outs, nth)
+        line["accuracy_vs_fp64"] = accuracy_vs_fp64(outs, nth, (plev, t, td, ps, ts, tds))
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

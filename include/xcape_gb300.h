@@ -168,12 +168,16 @@ size_t xc_loopcape_workspace_bytes(int n2);
  * start-up.  No counterpart in the reference (its Fortran runs on the host).
  * Same arguments and results as xc_loopcape_ex (device pointers, columns
  * ordered before the lift), but the ordering scratch lives in a static
- * device array inside the library (about 6.1 MiB, held on every GPU that
- * loads the library until the process exits), so the call allocates nothing.
- * n2 above XC_NOALLOC_MAX_COLUMNS is rejected with XC_ERR_INVALID.  The first
- * call on each device looks up the array's device address and should come
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be issued one after the other. */
+ * device array inside the library (about 6.1 MiB), so the call allocates
+ * nothing.  n2 above XC_NOALLOC_MAX_COLUMNS is rejected with XC_ERR_INVALID.
+ * CUDA creates the array on a device when it loads the library's module
+ * that holds it: under lazy module loading (the default) at the first call
+ * on that device, and the device then keeps it until its context is
+ * destroyed.  A call with n2 == 0 does only that set-up, so make one at
+ * start-up on each device, before any stream capture.  Every call looks the
+ * array's address up again, so it stays valid after cudaDeviceReset.  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * issued one after the other. */
 int xc_loopcape_ex_noalloc(int grid, const void *p, const void *t3d, const void *td3d,
                            const void *ps, const void *ts, const void *tds, int dtype,
                            float pinc, int source, float ml_depth, int adiabat,
@@ -355,6 +359,22 @@ const char *xc_last_error(void);
 
 /* Library version string. */
 const char *xc_version(void);
+
+/* Device and pinned-host allocations (cudaMalloc, cudaMallocHost) the library
+ * has made since it was loaded; it does not count CUDA's own allocations
+ * (module loads, graphs, streams).  For checking that a path allocates
+ * nothing, e.g. xc_loopcape_ex_noalloc. */
+long long xc_alloc_count(void);
+
+/* Measures the current device's FP32 and XU (transcendental unit) issue
+ * rates with two short kernels of known instruction mix -- 8 independent
+ * fused multiply-add chains per thread, and 8 independent ex2.approx chains
+ * per thread -- timed with CUDA events on `stream` after a warm-up launch.
+ * Outputs are lane operations per second, in units of 1e9 (one FFMA or one
+ * ex2.approx of one thread is one operation).  They are the denominators of
+ * the CAPE lift's compute roofline.  No counterpart in the reference.
+ * Synchronises `stream`; takes a few milliseconds. */
+int xc_measure_pipe_peaks(double *fp32_gops, double *xu_gops, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Ragged batches in one persistent, graph-captured kernel.  No counterpart  */

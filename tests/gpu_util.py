@@ -137,3 +137,45 @@ def compare_cape(got, want, want64=None, max_status_flip=0.02, max_cin_ties=0.00
     summary["cin_ties"] = int(bad.sum())
     summary["max_abs_cin_nontie"] = float(np.max(np.abs(g - w)[~tie])) if (~tie).any() else 0.0
     return summary
+
+
+def oracle_cols(grid, p, t, td, ps, ts, tds, source, adiabat, pinc, ml_depth, start=None,
+                precision="f32"):
+    """The oracle (loopcape_ml / _pl1d / _pl restated in C) on the same
+    columns, with its per-column statistics (status, bmin)."""
+    import oracle as O
+    n2 = int(np.prod(np.shape(t)[:-1]))
+    nk = np.shape(t)[-1]
+    t2, td2 = np.reshape(t, (n2, nk)), np.reshape(td, (n2, nk))
+    sf = [np.ravel(a) for a in (ps, ts, tds)]
+    src, adi = SOURCES.get(source, source), ADIABATS.get(adiabat, adiabat)
+    kw = dict(stats=True, precision=precision)
+    if grid == 1:
+        return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, **kw)
+    if grid == 2:
+        st = O.pres_lev_pos(p, sf[0]) if start is None else start
+        return O.loopcape(np.ravel(p), t2, td2, *sf, pinc, src, ml_depth, adi, start=st,
+                          p_is_1d=True, **kw)
+    return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, start=start,
+                      **kw)
+
+
+def check_vs_fp64(got, ref, what="", min_same_parcel=0.99):
+    """The accelerated solvers' contract against the FP64 oracle: no column
+    gives up where FP64 converges; CAPE within max(1 J/kg, 0.1 %) wherever
+    both lift the same parcel (a most-unstable theta-e near-tie can pick
+    another level); CIN within the same bound outside buoyancy near-ties.
+    Returns the largest |dCAPE|."""
+    conv64 = (ref["status"] & _lib.COL_NOCONV) == 0
+    gave_up = (got["status"] & _lib.COL_NOCONV) != 0
+    assert not np.any(gave_up & conv64), f"{what}: {np.sum(gave_up & conv64)} columns gave up"
+    ok = conv64 & (got["mulvl"] == ref["mulvl"])
+    other = int(np.sum(conv64 & ~ok))
+    assert other <= max(1, (1.0 - min_same_parcel) * ok.size), (
+        f"{what}: {other} of {ok.size} columns lift another parcel")
+    d = np.abs(got["cape"][ok].astype(np.float64) - ref["cape"][ok])
+    assert np.all(d <= _tol(ref["cape"][ok])), f"{what}: |dCAPE| up to {d.max()}"
+    okc = ok & (ref["bmin"] >= BUOYANCY_TIE)
+    dc = np.abs(got["cin"][okc].astype(np.float64) - ref["cin"][okc])
+    assert np.all(dc <= _tol(ref["cin"][okc])), f"{what}: |dCIN| up to {dc.max()}"
+    return float(d.max()) if d.size else 0.0

@@ -166,3 +166,37 @@ def test_batch_rejects_invalid_batches_without_launching(pools):
         b.run(reqs)
         torch.cuda.synchronize()
         assert bool((reqs[0].cape >= 0).all())
+
+
+@pytest.mark.parametrize("guess", ["plain", "extrapolated", "learned"])
+def test_batch_requests_match_oracle(pools, guess):
+    """Every request of a mixed batch (sigma and pressure levels, views of
+    wider arrays, every source and adiabat, ragged column counts) against
+    the oracle on the same columns: the plain solver within the parity
+    criteria of the single-request tests against the FP32 oracle (the
+    reference's arithmetic), the accelerated solvers within their contract
+    against the FP64 oracle."""
+    torch = torch_cuda()
+    from gpu_util import check_vs_fp64, compare_cape, oracle_cols
+    from xcape_gb300.batch import CapeBatch
+    with CapeBatch(max_requests=16, max_columns=1 << 16, guess=guess) as b:
+        reqs, refs = _build(b, pools, _spec())
+        b.run(reqs)
+        torch.cuda.synchronize()
+        checked = 0
+        for r, (grid, a, source, adiabat) in zip(reqs, refs):
+            if a[1].shape[0] == 0:
+                continue
+            g = 1 if grid == "sigma" else 2
+            args = [np.ascontiguousarray(x) for x in a]
+            got = {k: getattr(r, k).cpu().numpy() for k in ("cape", "cin", "mulvl", "z_out",
+                                                              "status")}
+            want64 = oracle_cols(g, *args, source, adiabat, 500.0, 500.0, precision="f64")
+            what = f"{guess} {grid} {source} {adiabat} n2={a[1].shape[0]} nk={a[1].shape[1]}"
+            if guess == "plain":
+                want = oracle_cols(g, *args, source, adiabat, 500.0, 500.0)
+                compare_cape(got, want, want64, what=what)
+            else:
+                check_vs_fp64(got, want64, what=what, min_same_parcel=0.98)
+            checked += a[1].shape[0]
+        assert checked == sum(s[2] for s in _spec())

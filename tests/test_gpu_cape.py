@@ -15,8 +15,8 @@ import xcape_gb300 as X
 from xcape_gb300 import _lib
 from xcape_gb300 import synthetic as S
 
-from gpu_util import (ADIABATS, SOURCES, cape_device, compare_cape, thetae_f64, to_dev,
-                      torch_cuda)
+from gpu_util import (ADIABATS, SOURCES, cape_device, compare_cape, oracle_cols, thetae_f64,
+                      to_dev, torch_cuda)
 
 pytestmark = pytest.mark.gpu
 
@@ -75,22 +75,7 @@ def test_cape_pressure_golden(era5, source, keys, use_torch):
         _close(got, e[key])
 
 
-def _oracle_cols(grid, p, t, td, ps, ts, tds, source, adiabat, pinc, ml_depth, start=None,
-                 precision="f32"):
-    n2 = int(np.prod(np.shape(t)[:-1]))
-    nk = np.shape(t)[-1]
-    t2, td2 = np.reshape(t, (n2, nk)), np.reshape(td, (n2, nk))
-    sf = [np.ravel(a) for a in (ps, ts, tds)]
-    src, adi = SOURCES[source], ADIABATS[adiabat]
-    kw = dict(stats=True, precision=precision)
-    if grid == 1:
-        return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, **kw)
-    if grid == 2:
-        st = O.pres_lev_pos(p, sf[0]) if start is None else start
-        return O.loopcape(np.ravel(p), t2, td2, *sf, pinc, src, ml_depth, adi, start=st,
-                          p_is_1d=True, **kw)
-    return O.loopcape(np.reshape(p, (n2, nk)), t2, td2, *sf, pinc, src, ml_depth, adi, start=start,
-                      **kw)
+_oracle_cols = oracle_cols
 
 
 def _check_mulvl(got, want, p, t, td, ps, ts, tds, grid, start=None):

@@ -183,6 +183,41 @@ def test_srh_pressure_stage_entry_points(era5):
     np.testing.assert_allclose(SRM.cpu().numpy(), srm_w, rtol=1e-12, atol=1e-9)
 
 
+@pytest.mark.parametrize("hin_m", [2.0, 0.0])
+def test_stdheight_pressure_3d_entry_point(hin_m):
+    """loop_stdheight_pl (stdheight_2D_pressure_lev.f90:5-47, :133-219): a
+    pressure per column and level plus a per-column start level, against the
+    oracle's restatement of the same routine.  The columns' pressures are the
+    shared levels perturbed per column, ps is ragged so that the start level
+    varies, and a few columns start at the first or the last level."""
+    torch = torch_cuda()
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(24, 40), seed=9)
+    n2, nk = ps.size, plev.size
+    rng = np.random.default_rng(19)
+    P = np.broadcast_to(plev.astype(np.float64), (n2, nk)).copy()
+    P *= 1.0 + rng.normal(0.0, 2e-3, P.shape)
+    T = np.ascontiguousarray(t.reshape(n2, nk), np.float64)
+    TD = np.ascontiguousarray(td.reshape(n2, nk), np.float64)
+    ps64, ts64, tds64 = (np.ascontiguousarray(np.ravel(a), np.float64) for a in (ps, ts, tds))
+    start = np.array([O.pres_lev_pos(P[i], ps64[i:i + 1])[0] for i in range(n2)], np.int32)
+    start[:3] = [1, nk, nk - 1]
+    hin = np.full(n2, hin_m)
+    H_w, Hs_w = O.loop_stdheight(P, T, TD, ps64, ts64, tds64, hin, start=start)
+    d = to_dev(P, T, TD, ps64, ts64, tds64, hin)
+    S_ = to_dev(start)[0]
+    H = torch.empty((n2, nk), dtype=torch.float64, device="cuda")
+    Hs = torch.empty(n2, dtype=torch.float64, device="cuda")
+    _lib.call("xc_loop_stdheight_pl", *[x.data_ptr() for x in d], S_.data_ptr(), nk, n2,
+              H.data_ptr(), Hs.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = H.cpu().numpy()
+    # below-ground levels carry the reference's -999999 sentinel on both sides
+    np.testing.assert_array_equal(got == -999999.0, H_w == -999999.0)
+    np.testing.assert_allclose(got, H_w, rtol=1e-12, atol=1e-9)
+    np.testing.assert_array_equal(Hs.cpu().numpy(), Hs_w)
+    assert len(set(start.tolist())) > 3  # the start level really varies
+
+
 def test_srh_full_size_workload():
     """1024x1024 columns x 50 levels: determinism and a sample vs the oracle."""
     torch = torch_cuda()

@@ -91,7 +91,7 @@ def test_fortran_method_needs_reference(p_t_td_3d, p_t_td_surface):
 
 def _declared_entry_points():
     text = open(os.path.join(ROOT, "include", "xcape_gb300.h")).read()
-    return sorted(set(re.findall(r"^(?:int|size_t|const char \*)\s*(xc_\w+)\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|size_t|long long|const char \*)\s*(xc_\w+)\(", text, re.M)))
 
 
 def test_library_exports_every_declared_symbol():
@@ -231,3 +231,28 @@ def test_batch_request_descriptor_layout_matches_the_header():
     R = _lib.CapeRequest
     assert list(out) == [ctypes.sizeof(R), R.n2.offset, R.ld.offset, R.p.offset, R.pinc.offset,
                          R.adiabat.offset, R.cape.offset, R.status.offset]
+
+
+def test_plugin_stub_binds_the_library_without_a_gpu(monkeypatch):
+    """The reference-side binding (xcape_gb300/plugin/cape_cuda.py, the file
+    a maintainer copies into xcape) loads the library and declares the
+    argument types of the two host entry points it calls; an argument the
+    library rejects before any CUDA work comes back as RuntimeError."""
+    import importlib.util
+    from xcape_gb300 import _build
+    monkeypatch.setenv("XCAPE_GB300_LIB", _build.build())
+    spec = importlib.util.spec_from_file_location(
+        "cape_cuda_stub", os.path.join(ROOT, "xcape_gb300", "plugin", "cape_cuda.py"))
+    stub = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(stub)
+    L = stub._lib()
+    assert len(L.xc_loopcape_ex_host.argtypes) == len(_lib.SIGNATURES["xc_loopcape_ex_host"])
+    assert len(L.xc_calc_srh_host.argtypes) == len(_lib.SIGNATURES["xc_calc_srh_host"])
+    t2 = np.zeros((20, 4), np.float32)   # (nlev, ngrid), as the seam hands it over
+    s1 = np.zeros(4, np.float32)
+    with pytest.raises(RuntimeError, match="adiabat"):
+        stub.cape(t2, t2, t2, s1, s1, s1, 0, 1, source=1, ml_depth=500.0, adiabat=7, pinc=500.0,
+                  type_grid=1)
+    with pytest.raises(ValueError, match="1-D pressure"):
+        stub.cape(t2, t2, t2, s1, s1, s1, 0, 1, source=1, ml_depth=500.0, adiabat=1, pinc=500.0,
+                  type_grid=2)

@@ -25,6 +25,7 @@ XC_GUESS_SECANT = 3
 XC_GUESS_LEARNED_EVERY = 4
 XC_GUESS_NPARAM = 4481
 XC_MAX_LEVELS = 4096
+XC_NOALLOC_MAX_COLUMNS = 1048576
 
 COL_NOCONV = 1
 COL_BADSTART = 2
@@ -74,6 +75,7 @@ SIGNATURES = {
     "xc_guess_adam": [_vp, _vp, _vp, _vp, _f, _i, _vp],
     "xc_guess_eval": [_vp, _vp, ctypes.c_longlong, _vp, _vp],
     "xc_release_workspace": [],
+    "xc_measure_pipe_peaks": [_vp, _vp, _vp],
     "xc_batch_create": [_i, ctypes.c_longlong, _i, ctypes.POINTER(_vp)],
     "xc_batch_run": [_vp, _vp, _i, _vp],
     "xc_batch_work": [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
@@ -125,6 +127,8 @@ def lib():
             L.xc_last_error.argtypes = []
             L.xc_version.restype = ctypes.c_char_p
             L.xc_version.argtypes = []
+            L.xc_alloc_count.restype = ctypes.c_longlong
+            L.xc_alloc_count.argtypes = []
             _lib = L
     return _lib
 
@@ -145,7 +149,7 @@ def version():
 def exported_symbols():
     """Names of the entry points declared in include/xcape_gb300.h."""
     return sorted(list(SIGNATURES) + ["xc_last_error", "xc_version",
-                                      "xc_loopcape_workspace_bytes"])
+                                      "xc_loopcape_workspace_bytes", "xc_alloc_count"])
 
 
 def workspace_bytes(n2):

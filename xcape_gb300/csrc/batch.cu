@@ -272,9 +272,9 @@ int xc_batch_create(int max_requests, long long max_columns, int guess, xc_batch
   cudaStream_t cs = nullptr;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   for (int s = 0; s < xc::kSlots && e == cudaSuccess; ++s) {
-    e = cudaMallocHost((void **)&b->htable[s], b->bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&b->dtable[s], b->bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&b->counters[s], 3 * sizeof(unsigned long long));
+    e = xc::host_malloc((void **)&b->htable[s], b->bytes);
+    if (e == cudaSuccess) e = xc::dev_malloc((void **)&b->dtable[s], b->bytes);
+    if (e == cudaSuccess) e = xc::dev_malloc((void **)&b->counters[s], 3 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done[s], cudaEventDisableTiming);
     if (e != cudaSuccess) break;
     memset(b->htable[s], 0, b->bytes);

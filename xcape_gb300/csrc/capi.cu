@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -18,6 +19,8 @@
 namespace {
 
 thread_local char g_err[512] = "";
+// successful device and pinned-host allocations since the library was loaded
+std::atomic<long long> g_allocs{0};
 
 int fail(int code, const char *fmt, ...) {
   va_list ap;
@@ -114,7 +117,7 @@ int pipeline_pinned(Pipeline *pl, size_t bytes) {
   if (pl->pinned) cudaFreeHost(pl->pinned);
   pl->pinned = nullptr;
   pl->pinned_cap = 0;
-  const cudaError_t e = cudaMallocHost((void **)&pl->pinned, bytes);
+  const cudaError_t e = xc::host_malloc((void **)&pl->pinned, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(XC_ERR_NOMEM, "cudaMallocHost(%zu) for the host-path staging: %s", bytes,
@@ -136,7 +139,7 @@ int ws_get(size_t bytes, void **out) {
       w.ptr = nullptr;
       w.cap = 0;
     }
-    e = cudaMalloc(&w.ptr, bytes);
+    e = xc::dev_malloc(&w.ptr, bytes);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(XC_ERR_NOMEM, "cudaMalloc(%zu) for the host-path workspace: %s", bytes,
@@ -189,6 +192,8 @@ extern "C" {
 const char *xc_last_error(void) { return g_err; }
 
 const char *xc_version(void) { return "xcape_gb300 0.1.0 (sm_103a)"; }
+
+long long xc_alloc_count(void) { return g_allocs.load(std::memory_order_relaxed); }
 
 int xc_release_workspace(void) {
   std::lock_guard<std::mutex> lk(g_ws_mu);
@@ -897,6 +902,16 @@ namespace xc {
 int set_error(int code, const char *msg) {
   snprintf(g_err, sizeof(g_err), "%s", msg);
   return code;
+}
+cudaError_t dev_malloc(void **p, size_t bytes) {
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) g_allocs.fetch_add(1, std::memory_order_relaxed);
+  return e;
+}
+cudaError_t host_malloc(void **p, size_t bytes) {
+  const cudaError_t e = cudaMallocHost(p, bytes);
+  if (e == cudaSuccess) g_allocs.fetch_add(1, std::memory_order_relaxed);
+  return e;
 }
 // For the batch executor (batch.cu): the loaded guess network, and the
 // option checks of the single-request entry points.

@@ -10,12 +10,18 @@
 // inputs and outputs and nothing is allocated per call.
 //
 // * The array holds the ordering scratch for at most XC_NOALLOC_MAX_COLUMNS
-//   columns (about 6.1 MiB).  Every GPU that loads this library holds it
-//   until the process exits.
-// * Host code cannot use the array's name as a device address.  The first
-//   call on each device looks the address up with cudaGetSymbolAddress (with
-//   that device current) and keeps it; that first call should therefore come
-//   before any stream capture.
+//   columns (about 6.1 MiB).  It is created on a device when CUDA loads this
+//   file's module there: at the first look-up of its address under lazy
+//   module loading (CUDA_MODULE_LOADING=LAZY, the default), or when the
+//   library's modules are loaded otherwise.  From then on the device holds
+//   it until the context is destroyed (process exit or cudaDeviceReset).
+//   A call with n2 == 0 performs only that look-up, so a caller can make the
+//   one allocation CUDA does for the array at start-up, before any stream
+//   capture.
+// * Host code cannot use the array's name as a device address.  Every call
+//   looks the address up with cudaGetSymbolAddress on the current device
+//   (cheap once the module is loaded), so a context that was reset and
+//   re-created, which may place the array elsewhere, gets the new address.
 // * All calls share the one array, and it keeps the last call's contents.
 //   The bucket counters that must start at zero are cleared at every call.
 //   Calls that overlap on the GPU (on different streams, or from several host
@@ -24,8 +30,6 @@
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
-
-#include <mutex>
 
 #include "../../include/xcape_gb300.h"
 #include "xc_kernels.h"
@@ -39,10 +43,6 @@ constexpr size_t kNoallocScratchBytes =
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_addr_mu;
-void *g_addr[kMaxDevices] = {};
-
 // Formats the message into xc_last_error() and returns code.
 int noalloc_fail(int code, const char *fmt, ...) {
   char msg[256];
@@ -53,25 +53,17 @@ int noalloc_fail(int code, const char *fmt, ...) {
   return xc::set_error(code, msg);
 }
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device).
+// Device address of g_noalloc_scratch on the current device, looked up on
+// every call (loading this module on the device at the first one).
 int scratch_address(void **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess)
-    return noalloc_fail(XC_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices)
-    return noalloc_fail(XC_ERR_INVALID, "device %d is beyond the %d this entry point tracks", dev,
-                        kMaxDevices);
-  std::lock_guard<std::mutex> lk(g_addr_mu);
-  if (g_addr[dev] == nullptr) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess)
-      return noalloc_fail(XC_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_addr[dev] = p;
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return noalloc_fail(XC_ERR_CUDA, "cudaGetSymbolAddress of the static scratch: %s",
+                        cudaGetErrorString(e));
   }
-  *out = g_addr[dev];
+  *out = p;
   return XC_OK;
 }
 
@@ -91,12 +83,14 @@ extern "C" int xc_loopcape_ex_noalloc(int grid, const void *p, const void *t3d, 
   if (n2 > 0 && xc::order_workspace_bytes(n2) > kNoallocScratchBytes)
     return noalloc_fail(XC_ERR_INVALID, "ordering scratch for %d columns exceeds the static array",
                         n2);
+  if (n2 < 0) return noalloc_fail(XC_ERR_INVALID, "n2=%d is negative", n2);
+  // Also for n2 == 0: an empty call performs the set-up (the module load
+  // that creates the array on this device) and nothing else.
   void *scratch = nullptr;
-  if (n2 > 0) {
-    const int rc = scratch_address(&scratch);
-    if (rc != XC_OK) return rc;
-  }
+  const int rc = scratch_address(&scratch);
+  if (rc != XC_OK) return rc;
+  if (n2 == 0) return XC_OK;
   return xc_loopcape_ex(grid, p, t3d, td3d, ps, ts, tds, dtype, pinc, source, ml_depth, adiabat,
                         start_3d, nk, n2, guess, cape, cin, mulvl, z_out, status, counters,
-                        scratch, scratch ? kNoallocScratchBytes : 0, stream);
+                        scratch, kNoallocScratchBytes, stream);
 }

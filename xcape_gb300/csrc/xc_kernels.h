@@ -63,6 +63,11 @@ cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStre
 // Records msg as the calling thread's xc_last_error() text (capi.cu).
 int set_error(int code, const char *msg);
 
+// Every device or pinned-host allocation the library makes goes through
+// these two (capi.cu), which count the successful ones for xc_alloc_count().
+cudaError_t dev_malloc(void **p, size_t bytes);
+cudaError_t host_malloc(void **p, size_t bytes);
+
 // Raises `func`'s dynamic shared-memory limit to `bytes` on the current
 // device, once per device (the attribute is per device; setting it again is
 // harmless, so concurrent first calls need no lock).  done: a per-call-site
