@@ -60,6 +60,7 @@ extern "C" {
 #define XC_COL_BADSTART 2 /* start_3d outside 1..nk: outputs zero              */
 #define XC_COL_TOOMANYSTEPS 4 /* the ascent would take more than 2^22 sub-steps, or
                                  a pressure step is not finite: cape = cin = 0   */
+#define XC_COL_FP64 8     /* recomputed in double precision by the FP64 retry      */
 
 /* Moist-adiabat solver of xc_loopcape_ex (`guess` argument).
  * XC_GUESS_PLAIN is the reference's iteration: first guess thlast = th1,
@@ -76,6 +77,17 @@ extern "C" {
 #define XC_GUESS_SECANT 3       /* first guess th1 (the reference's), secant steps */
 #define XC_GUESS_LEARNED_EVERY 4 /* the network's guess on every sub-step that starts
                                     saturated, th1 on the others; secant steps */
+
+/* Flag OR'ed into `guess` (xc_loopcape_ex, xc_loopcape_ex_host,
+ * xc_loopcape_multi_host, xc_loopcape_ex_noalloc): after the FP32 lift, the
+ * columns it flagged XC_COL_NOCONV -- the reference's give-up after 100
+ * iterations, CAPE = CIN = 0 (CAPE_CODE_model_lev.f90:464-474), which FP32
+ * rounding can cause where the iteration converges in FP64 -- are lifted
+ * again in double precision with the reference's iteration, in a second
+ * kernel, and their outputs replaced.  Their status gains XC_COL_FP64 and
+ * keeps XC_COL_NOCONV only if the FP64 iteration gave up too.  The device
+ * entry points need the status array for it. */
+#define XC_RETRY_FP64 256
 
 /* Parameters of the guess network (3 -> 64 -> 64 -> 1, ReLU), flat:
  * W1[64][3] b1[64] W2[64][64] b2[64] w3[64] b3. */
@@ -195,6 +207,19 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
                         int source, float ml_depth, int adiabat, const int *start_3d, int nk,
                         int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
                         int *status, void *stream);
+
+/* xc_loopcape_ex_host for nsrc (1..3) sources of the same columns: the
+ * inputs cross to the device once and every source is lifted from them.
+ * No counterpart in the reference, where each source is its own calc_cape
+ * call (src/xcape/core.py:130-235), each handing the same p, t, td to the
+ * Fortran again.  sources [nsrc] holds XC_SOURCE_* codes; the outputs are
+ * [nsrc][n2] (source j's results of column i at j * n2 + i) and equal those
+ * of nsrc xc_loopcape_ex_host calls. */
+int xc_loopcape_multi_host(int grid, const void *p, const void *t3d, const void *td3d,
+                           const void *ps, const void *ts, const void *tds, int dtype, float pinc,
+                           int nsrc, const int *sources, float ml_depth, int adiabat,
+                           const int *start_3d, int nk, int n2, int guess, float *cape,
+                           float *cin, int *mulvl, float *z_out, int *status, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* Storm-relative helicity                                                 */

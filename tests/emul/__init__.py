@@ -41,6 +41,7 @@ def lib():
         vp, i, f, d, ll = (ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double,
                            ctypes.c_longlong)
         L.emu_cape.argtypes = [i] + [vp] * 6 + [i, f, i, f, i, vp, i, ll] + [vp] * 6 + [i, vp, vp]
+        L.emu_cape64.argtypes = [i] + [vp] * 6 + [i, f, i, f, i, vp, i, ll] + [vp] * 5
         L.emu_guess_eval.argtypes = [vp, f, f, f]
         L.emu_guess_eval.restype = f
         L.emu_guess_eval_packed.argtypes = [vp, f, f, f]

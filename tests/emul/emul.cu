@@ -47,6 +47,42 @@ static void cape_loop(const CapeArgs &a, long long *counters) {
   }
 }
 
+// The double-precision plain solver (the FP64 retry's column routine) on
+// every column.
+template <typename T, int GRID>
+static void cape64_loop(const CapeArgs &a) {
+  const bool ice = a.adiabat >= 3, pseudo = (a.adiabat == 1 || a.adiabat == 3);
+  for (long long i = 0; i < a.n2; ++i) {
+    int nsub = 0, niter = 0;
+    if (ice && pseudo) cape_column_run<T, GRID, true, true, SOLVE_PLAIN, false, double>(a, i, nsub, niter);
+    else if (ice) cape_column_run<T, GRID, true, false, SOLVE_PLAIN, false, double>(a, i, nsub, niter);
+    else if (pseudo) cape_column_run<T, GRID, false, true, SOLVE_PLAIN, false, double>(a, i, nsub, niter);
+    else cape_column_run<T, GRID, false, false, SOLVE_PLAIN, false, double>(a, i, nsub, niter);
+  }
+}
+
+extern "C" int emu_cape64(int grid, const void *p, const void *t, const void *td, const void *ps,
+                          const void *ts, const void *tds, int dtype, float pinc, int source,
+                          float ml_depth, int adiabat, const int *start, int nk, long long n2,
+                          float *cape, float *cin, int *mulvl, float *z_out, int *status) {
+  CapeArgs a;
+  a.grid = grid; a.dtype = dtype; a.p = p; a.t = t; a.td = td; a.ps = ps; a.ts = ts; a.tds = tds;
+  a.start = grid == 1 ? nullptr : start; a.pinc = pinc; a.source = source; a.ml_depth = ml_depth;
+  a.adiabat = adiabat; a.nk = nk; a.n2 = n2; a.guess = 0; a.perm = nullptr; a.cape = cape;
+  a.cin = cin; a.mulvl = mulvl; a.z_out = z_out; a.status = status; a.counters = nullptr;
+  a.guess_w = nullptr;
+  if (dtype == 0) {
+    if (grid == 1) cape64_loop<float, 1>(a);
+    else if (grid == 2) cape64_loop<float, 2>(a);
+    else cape64_loop<float, 3>(a);
+  } else {
+    if (grid == 1) cape64_loop<double, 1>(a);
+    else if (grid == 2) cape64_loop<double, 2>(a);
+    else cape64_loop<double, 3>(a);
+  }
+  return 0;
+}
+
 extern "C" int emu_cape(int grid, const void *p, const void *t, const void *td, const void *ps,
                         const void *ts, const void *tds, int dtype, float pinc, int source,
                         float ml_depth, int adiabat, const int *start, int nk, long long n2,

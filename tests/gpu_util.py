@@ -113,7 +113,8 @@ def compare_cape(got, want, want64=None, max_status_flip=0.02, max_cin_ties=0.00
     noconv_g = (got["status"] & _lib.COL_NOCONV) != 0
     noconv_w = (want["status"] & _lib.COL_NOCONV) != 0
     flip = noconv_g != noconv_w
-    assert flip.mean() <= max_status_flip, f"{what}: {flip.sum()} of {n} convergence flips"
+    assert flip.sum() <= max(1, max_status_flip * n), (
+        f"{what}: {flip.sum()} of {n} convergence flips")
     summary = {"n": n, "flips": int(flip.sum())}
     if want64 is not None:
         # the GPU converged where FP32 Fortran arithmetic cycled: FP64 agrees

@@ -343,3 +343,118 @@ def test_host_path_chunks_match_device_path(guess, ring, monkeypatch):
     torch.cuda.synchronize()
     for h, d in zip(host, ref):
         np.testing.assert_array_equal(h, d.cpu().numpy())
+
+
+@pytest.mark.parametrize("ring", [None, "1"])
+@pytest.mark.parametrize("guess", ["plain", "learned"])
+def test_calc_cape_sources_one_upload(guess, ring, monkeypatch):
+    """calc_cape_sources (xc_loopcape_multi_host): the three sources of the
+    same columns from one upload of the inputs.  Each source's results equal
+    a calc_cape call of its own bit for bit (the same kernels on the same
+    columns, one ordering shared by the sources), over three chunks, also
+    when the chunks share two device slots (XC_HOST_RING_BYTES=1); the plain
+    solver's results meet the parity criteria against the oracle."""
+    if ring is not None:
+        monkeypatch.setenv("XC_HOST_RING_BYTES", ring)
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(216, 1440), seed=4)  # 311,040 columns
+    names = ["mixed-layer", "surface", "most-unstable"]
+    got = X.calc_cape_sources(plev, t, td, ps, ts, tds, sources=names, vertical_lev="pressure",
+                              guess=guess)
+    assert list(got) == names
+    for name in names:
+        single = X.calc_cape(plev, t, td, ps, ts, tds, source=name, vertical_lev="pressure",
+                             guess=guess)
+        assert len(got[name]) == len(single) == (4 if name == "most-unstable" else 2)
+        for a, b in zip(got[name], single):
+            assert a.shape == (216, 1440)
+            np.testing.assert_array_equal(a, b)
+    if guess == "plain":
+        n = 8192  # a strided sample of the grid against the oracle
+        idx = np.arange(n) * (ps.size // n)
+        sub = [np.reshape(a, (ps.size, -1))[idx] for a in (t, td)] + \
+              [np.ravel(a)[idx] for a in (ps, ts, tds)]
+        for name in names:
+            want = oracle_cols(2, plev, *sub, name, "pseudo-liquid", 500.0, 500.0)
+            g = {"cape": got[name][0].ravel()[idx], "cin": got[name][1].ravel()[idx]}
+            # the host path returns no status: a zero pair where the oracle's
+            # is not the reference's give-up is a convergence flip
+            zero = (g["cape"] == 0) & (g["cin"] == 0)
+            real_zero = ((want["status"] & 1) == 0) & (want["cape"] == 0) & (want["cin"] == 0)
+            g["status"] = np.where(zero & ~real_zero, 1, 0)
+            compare_cape(g, want, what=f"calc_cape_sources {name}")
+
+
+def test_calc_cape_sources_arguments():
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(4, 8))
+    with pytest.raises(ValueError, match="at most once"):
+        X.calc_cape_sources(plev, t, td, ps, ts, tds, sources=["surface", "surface"],
+                            vertical_lev="pressure")
+    with pytest.raises(ValueError, match="source"):
+        X.calc_cape_sources(plev, t, td, ps, ts, tds, sources=["lifted"], vertical_lev="pressure")
+
+
+@pytest.mark.parametrize("source", ["surface", "most-unstable", "mixed-layer"])
+@pytest.mark.parametrize("adiabat", ["pseudo-liquid", "reversible-ice"])
+def test_fp64_retry_of_given_up_columns(source, adiabat):
+    """XC_RETRY_FP64 with the plain solver (the reference's iteration) on the
+    noisy pressure-level workload, where FP32 rounding makes the iteration
+    give up on a few percent of the columns.  Exactly those columns are
+    lifted again in double precision (XC_COL_FP64), and then match the FP64
+    oracle within max(1 J/kg, 0.1 %); every other column is bit for bit what
+    the lift without the retry gives.  With and without the ordering
+    workspace (the retry then scans every column's status instead of a
+    compacted list)."""
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(96, 128), seed=6)
+    base = cape_device(2, plev, t, td, ps, ts, tds, source, adiabat, guess=0)
+    gave_up = (base["status"] & _lib.COL_NOCONV) != 0
+    assert gave_up.sum() >= 20  # the workload exercises the retry
+    ref = oracle_cols(2, plev, t, td, ps, ts, tds, source, adiabat, 500.0, 500.0,
+                      precision="f64")
+    for order in (True, False):
+        got = cape_device(2, plev, t, td, ps, ts, tds, source, adiabat,
+                          guess=_lib.XC_GUESS_PLAIN | _lib.XC_RETRY_FP64, order=order)
+        retried = (got["status"] & _lib.COL_FP64) != 0
+        np.testing.assert_array_equal(retried, gave_up)
+        for k in ("cape", "cin", "z_out", "mulvl", "status"):
+            np.testing.assert_array_equal(got[k][~retried], base[k][~retried])
+        conv64 = (ref["status"] & _lib.COL_NOCONV) == 0
+        np.testing.assert_array_equal((got["status"][retried] & _lib.COL_NOCONV) != 0,
+                                      ~conv64[retried])
+        ok = retried & conv64
+        assert ok.sum() == retried.sum()  # FP64 converges on all of them here
+        for k in ("cape", "cin"):
+            w = ref[k][ok]
+            d = np.abs(got[k][ok].astype(np.float64) - w)
+            assert np.all(d <= np.maximum(1.0, 1e-3 * np.abs(w))), (k, d.max())
+        np.testing.assert_array_equal(got["mulvl"][ok], ref["mulvl"][ok])
+
+
+def test_fp64_retry_through_the_public_api():
+    """calc_cape(..., fp64_retry=True) on numpy (the host pipeline, three
+    chunks) and on CUDA tensors gives the same results, and no column is
+    left at the reference's give-up zeros where FP64 converges."""
+    import torch
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(216, 1440), seed=8)
+    host = X.calc_cape(plev, t, td, ps, ts, tds, source="most-unstable", vertical_lev="pressure",
+                       fp64_retry=True)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (plev, t, td, ps, ts, tds)]
+    devr = X.calc_cape(*dev, source="most-unstable", vertical_lev="pressure", fp64_retry=True)
+    torch.cuda.synchronize()
+    for h, d in zip(host, devr):
+        np.testing.assert_array_equal(h, d.cpu().numpy())
+    plain = X.calc_cape(plev, t, td, ps, ts, tds, source="most-unstable", vertical_lev="pressure")
+    changed = host[0] != plain[0]
+    assert changed.sum() > 100
+    assert np.all(plain[0][changed] == 0)  # only the give-ups changed
+    n = 4096
+    idx = np.flatnonzero(changed.ravel())[:n]
+    sub = [np.reshape(a, (ps.size, -1))[idx] for a in (t, td)] + \
+          [np.ravel(a)[idx] for a in (ps, ts, tds)]
+    ref = oracle_cols(2, plev, *sub, "most-unstable", "pseudo-liquid", 500.0, 500.0,
+                      precision="f64")
+    d = np.abs(host[0].ravel()[idx].astype(np.float64) - ref["cape"])
+    assert np.all(d <= np.maximum(1.0, 1e-3 * np.abs(ref["cape"])))
+    srcs = X.calc_cape_sources(plev, t, td, ps, ts, tds, sources=["most-unstable"],
+                               vertical_lev="pressure", fp64_retry=True)
+    for a, b in zip(srcs["most-unstable"], host):
+        np.testing.assert_array_equal(a, b)

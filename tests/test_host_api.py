@@ -179,7 +179,7 @@ def test_python_constants_match_the_header():
     assert len(mirrored) >= 10
     for k, v in mirrored.items():
         assert k in defines and int(defines[k]) == v, k
-    for k in ("COL_NOCONV", "COL_BADSTART", "COL_TOOMANYSTEPS"):
+    for k in ("COL_NOCONV", "COL_BADSTART", "COL_TOOMANYSTEPS", "COL_FP64"):
         assert int(defines["XC_" + k]) == getattr(_lib, k), k
 
 

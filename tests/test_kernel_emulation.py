@@ -334,3 +334,46 @@ def test_emulated_nonfinite_inputs_bit_exact(source):
     assert np.all(got["cape"][flagged] == 0) and np.all(got["cin"][flagged] == 0)
     for k in ("cape", "cin", "mulvl", "z_out"):
         np.testing.assert_array_equal(got[k][~flagged], want[k][~flagged], err_msg=k)
+
+
+def _emu_cape64(grid, p, t, td, ps, ts, tds, source, adiabat, pinc=500.0, ml_depth=500.0,
+                start=None):
+    L = emul.lib()
+    f64 = any(np.asarray(a).dtype == np.float64 for a in (p, t, td, ps, ts, tds))
+    dt = np.float64 if f64 else np.float32
+    t = np.ascontiguousarray(t, dt)
+    nk = t.shape[-1]
+    n2 = t.size // nk
+    arrs = [np.ascontiguousarray(a, dt) for a in (p, t, td, ps, ts, tds)]
+    st = None if start is None else np.ascontiguousarray(start, np.int32)
+    out = dict(cape=np.empty(n2, np.float32), cin=np.empty(n2, np.float32),
+               mulvl=np.empty(n2, np.int32), z_out=np.empty(n2, np.float32),
+               status=np.empty(n2, np.int32))
+    L.emu_cape64(grid, *[a.ctypes.data for a in arrs], int(f64), pinc, source, ml_depth, adiabat,
+                 None if st is None else st.ctypes.data, nk, n2, out["cape"].ctypes.data,
+                 out["cin"].ctypes.data, out["mulvl"].ctypes.data, out["z_out"].ctypes.data,
+                 out["status"].ctypes.data)
+    return out
+
+
+@pytest.mark.parametrize("adiabat", ADIABATS)
+@pytest.mark.parametrize("source", SOURCES)
+def test_emulated_fp64_plain_solver_vs_fp64_oracle(source, adiabat):
+    """The double-precision instance of the column routine (the FP64
+    retry's) against the oracle's FP64 build: the same algorithm in double,
+    differing only in the named physical constants, which the routine takes
+    from the FP32 program widened to double (relative differences near
+    1e-8).  Every column's give-up flag must agree, the parcel level too,
+    and CAPE/CIN within 1e-3 J/kg (or 1e-5 relative)."""
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(24, 64), seed=13)
+    got = _emu_cape64(2, plev, t, td, ps, ts, tds, source, adiabat)
+    want = _oracle(2, plev, t, td, ps, ts, tds, source, adiabat, precision="f64")
+    np.testing.assert_array_equal(got["status"] & 1, want["status"] & 1)
+    np.testing.assert_array_equal(got["mulvl"], want["mulvl"])
+    for k in ("cape", "cin", "z_out"):
+        w = want[k].astype(np.float64)
+        d = np.abs(got[k].astype(np.float64) - w)
+        assert np.all(d <= np.maximum(1e-3, 1e-5 * np.abs(w))), (k, d.max())
+    # in double precision the plain iteration converges where FP32 cycled
+    f32 = _oracle(2, plev, t, td, ps, ts, tds, source, adiabat)
+    assert (got["status"] & 1).sum() <= (f32["status"] & 1).sum()

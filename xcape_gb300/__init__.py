@@ -5,9 +5,10 @@
 default.  The compute path is ``libxcape_gb300.so`` (C ABI declared in
 ``include/xcape_gb300.h``); there is no CPU fallback.
 """
-from .core import calc_cape, calc_cape_diagnostics, calc_cape_srh, calc_srh  # noqa: F401
+from .core import (calc_cape, calc_cape_diagnostics, calc_cape_sources, calc_cape_srh,  # noqa: F401
+                   calc_srh)
 from ._lib import XcapeError, version  # noqa: F401
 
-__all__ = ["calc_cape", "calc_cape_diagnostics", "calc_cape_srh", "calc_srh", "XcapeError",
-           "version"]
+__all__ = ["calc_cape", "calc_cape_diagnostics", "calc_cape_sources", "calc_cape_srh", "calc_srh",
+           "XcapeError", "version"]
 __version__ = "0.1.0"

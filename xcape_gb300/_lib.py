@@ -26,10 +26,12 @@ XC_GUESS_LEARNED_EVERY = 4
 XC_GUESS_NPARAM = 4481
 XC_MAX_LEVELS = 4096
 XC_NOALLOC_MAX_COLUMNS = 1048576
+XC_RETRY_FP64 = 256
 
 COL_NOCONV = 1
 COL_BADSTART = 2
 COL_TOOMANYSTEPS = 4
+COL_FP64 = 8
 
 GRID_SIGMA = 1
 GRID_PRESSURE_1D = 2
@@ -54,6 +56,8 @@ SIGNATURES = {
     + [_vp],
     "xc_loopcape_ex_host": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i] + [_vp] * 5
     + [_vp],
+    "xc_loopcape_multi_host": [_i] + [_vp] * 6 + [_i, _f, _i, _vp, _f, _i, _vp, _i, _i, _i]
+    + [_vp] * 5 + [_vp],
     "xc_loopcape_ex_noalloc": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i]
     + [_vp] * 6 + [_vp],
     "xc_calc_srh": [_i] + [_vp] * 10 + [_i, _vp, _d, _d, _i, _i] + [_vp] * 5 + [_vp],

@@ -171,7 +171,10 @@ def calc_cape(*args, **kwargs):
     Keywords: ``source``, ``ml_depth`` (m), ``adiabat``, ``pinc`` (Pa),
     ``method`` (``'cuda'``, ``'dummy'``, ``'fortran'``), ``vertical_lev``, and
     ``guess``: the moist-adiabat solver. ``'plain'`` is the reference's
-    iteration.  The others keep its stopping test and take secant steps:
+    iteration.  ``fp64_retry=True`` lifts again, in double precision with the
+    reference's iteration, the columns whose FP32 iteration gave up after 100
+    steps (the reference then returns CAPE = CIN = 0; FP32 rounding causes
+    that on a few percent of warm, noisy columns where FP64 converges).  The others keep its stopping test and take secant steps:
     ``'extrapolated'`` (first guess from the previous sub-step's increment),
     ``'learned'`` (as extrapolated, with the trained guess network's guess on
     the first saturated sub-step), ``'secant'`` (the reference's first
@@ -220,13 +223,9 @@ def _calc_cape_gufunc(*args, **kwargs):
                            vectorize=False, **kwargs)
 
 
-def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-liquid",
-                     pinc=500.0, method="cuda", vertical_lev="sigma", guess="plain"):
-    p, t, td, ps, ts, tds = args
-    src = _option(_SOURCE, source, "source")
-    adi = _option(_ADIABAT, adiabat, "adiabat")
-    vl = _option(_VERTICAL, vertical_lev, "vertical_lev")
-    gs = _option(_GUESS, guess, "guess")
+def _cape_grid(p, t, td, ps, ts, tds, vl):
+    """The grid kind and the 3-D shape of one calc_cape call, with the
+    reference's shape checks (core.py:278-300)."""
     original_shape = tuple(t.shape)
     _check_same([t, td])
     _check_same([ps, ts, tds])
@@ -242,6 +241,18 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
         raise ValueError("Input arrays must have the same shape.")
     if _prod(tuple(ps.shape)) != _prod(original_shape[:-1]):
         raise ValueError("Surface arrays must have one value per column.")
+    return grid, original_shape
+
+
+def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-liquid",
+                     pinc=500.0, method="cuda", vertical_lev="sigma", guess="plain",
+                     fp64_retry=False):
+    p, t, td, ps, ts, tds = args
+    src = _option(_SOURCE, source, "source")
+    adi = _option(_ADIABAT, adiabat, "adiabat")
+    vl = _option(_VERTICAL, vertical_lev, "vertical_lev")
+    gs = _option(_GUESS, guess, "guess")
+    grid, original_shape = _cape_grid(p, t, td, ps, ts, tds, vl)
 
     if method == "dummy":
         p2 = np.reshape(np.atleast_2d(np.asarray(p)), (-1, np.asarray(p).shape[-1])).T
@@ -262,10 +273,15 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
     b = _Batch([t, td], [ps, ts, tds], p, grid)
     cape, cin, zout = (b.empty(b.n2, "f4") for _ in range(3))
     mulvl = b.empty(b.n2, "i4")
+    status = None
+    if fp64_retry:
+        gs |= _lib.XC_RETRY_FP64
+        if b.torch:
+            status = b.empty(b.n2, "i4")  # the device path carries the flags in it
     args_ = (grid, b.ptr(b.p), b.ptr(b.levels[0]), b.ptr(b.levels[1]), b.ptr(b.surface[0]),
              b.ptr(b.surface[1]), b.ptr(b.surface[2]), b.dtype, float(pinc), src,
              float(ml_depth), adi, None, b.nk, b.n2, gs, b.ptr(cape), b.ptr(cin), b.ptr(mulvl),
-             b.ptr(zout), None)
+             b.ptr(zout), b.ptr(status))
     if b.torch:
         ws, ws_bytes = b.workspace(_lib.workspace_bytes(b.n2))
         _lib.call("xc_loopcape_ex", *args_, None, ws, ws_bytes, b.stream)
@@ -276,6 +292,68 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
     if src == 2:
         res += [mulvl.reshape(shp), zout.reshape(shp)]
     return tuple(res)
+
+
+def calc_cape_sources(p, t, td, ps, ts, tds, sources=("most-unstable", "mixed-layer"),
+                      ml_depth=500.0, adiabat="pseudo-liquid", pinc=500.0, vertical_lev="sigma",
+                      guess="plain", fp64_retry=False):
+    """``calc_cape`` for several parcel sources of the same columns in one
+    call: ``{source: calc_cape(p, t, td, ps, ts, tds, source=source, ...)}``
+    for each entry of ``sources`` (each of ``'surface'``, ``'most-unstable'``,
+    ``'mixed-layer'`` at most once), with the same values.
+
+    The reference computes each source with its own ``calc_cape`` call
+    (src/xcape/core.py:130-235), so numpy inputs would cross to the device
+    once per source; here they cross once (``xc_loopcape_multi_host``), and
+    the columns are ordered once for all the sources.  CUDA tensors are used
+    in place, one launch per source.  ``guess`` and ``fp64_retry`` as in
+    ``calc_cape``.
+    """
+    names = list(sources)
+    if not names or len(set(names)) != len(names):
+        raise ValueError("sources must name each source at most once")
+    codes = [_option(_SOURCE, src, "source") for src in names]
+    adi = _option(_ADIABAT, adiabat, "adiabat")
+    vl = _option(_VERTICAL, vertical_lev, "vertical_lev")
+    gs = _option(_GUESS, guess, "guess")
+    grid, original_shape = _cape_grid(p, t, td, ps, ts, tds, vl)
+    if gs in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY):
+        from . import guess as _guess
+        _guess.ensure_loaded()
+    b = _Batch([t, td], [ps, ts, tds], p, grid)
+    ns = len(codes)
+    cape, cin, zout = (b.empty(ns * b.n2, "f4") for _ in range(3))
+    mulvl = b.empty(ns * b.n2, "i4")
+    status = None
+    if fp64_retry:
+        gs |= _lib.XC_RETRY_FP64
+        if b.torch:
+            status = b.empty(ns * b.n2, "i4")
+    common = (grid, b.ptr(b.p), b.ptr(b.levels[0]), b.ptr(b.levels[1]), b.ptr(b.surface[0]),
+              b.ptr(b.surface[1]), b.ptr(b.surface[2]), b.dtype, float(pinc))
+    if b.torch:
+        ws, ws_bytes = b.workspace(_lib.workspace_bytes(b.n2))
+        for j, code in enumerate(codes):
+            sl = slice(j * b.n2, (j + 1) * b.n2)
+            _lib.call("xc_loopcape_ex", *common, code, float(ml_depth), adi, None, b.nk, b.n2, gs,
+                      b.ptr(cape[sl]), b.ptr(cin[sl]), b.ptr(mulvl[sl]), b.ptr(zout[sl]),
+                      None if status is None else b.ptr(status[sl]), None, ws, ws_bytes,
+                      b.stream)
+    else:
+        import ctypes
+        arr = (ctypes.c_int * ns)(*codes)
+        _lib.call("xc_loopcape_multi_host", *common, ns, ctypes.cast(arr, ctypes.c_void_p),
+                  float(ml_depth), adi, None, b.nk, b.n2, gs, b.ptr(cape), b.ptr(cin),
+                  b.ptr(mulvl), b.ptr(zout), None, None)
+    shp = _out_shape(original_shape)
+    out = {}
+    for j, (name, code) in enumerate(zip(names, codes)):
+        sl = slice(j * b.n2, (j + 1) * b.n2)
+        res = [cape[sl].reshape(shp), cin[sl].reshape(shp)]
+        if code == 2:
+            res += [mulvl[sl].reshape(shp), zout[sl].reshape(shp)]
+        out[name] = tuple(res)
+    return out
 
 
 DIAG_FIELDS = ("plfc", "zlfc", "pel", "zel", "zsource", "thetae_source")

@@ -14,37 +14,54 @@
 //   * in the liquid-only adiabats the ice term lhs*(qi2-qi1)/(cpm*tbar) is
 //     identically zero (qi1 = qi2 = 0) and is not evaluated, nor is getqvi
 //     whose product with fice = 0 it would be.
+//
+// The routines are templated on their real type R.  R = float is the
+// kernels' arithmetic above.  R = double runs the same plain solver in
+// double precision for the FP64 retry of columns whose FP32 iteration gave
+// up (cape_retry64_kernel): literals are then the double values of the
+// decimal constants, the named physical constants the FP32 program's,
+// widened.
 #pragma once
 #include "guess_mlp.cuh"
 #include "xc_common.cuh"
 #include "xc_kernels.h"
 
+// A decimal literal in the routine's precision: the single-precision
+// literal (x)f for float, the double literal x for double.
+#define XC_LIT(R, x) (sizeof(R) == sizeof(float) ? (R)(x##f) : (R)(x))
+
 namespace xc {
 
-// Environment of one level (:232-240).
-struct Env {
-  float p, t, td, pi, q, th, thv;
-};
+XC_HD float xabs(float x) { return fabsf(x); }
+XC_HD double xabs(double x) { return fabs(x); }
 
-// FAST (the accelerated solvers): pi from exp(RDDCP ln(p/P00)), q from
-// getqvs_fast and the two quotients from approximate divides.
-template <bool FAST = false>
-XC_HD Env make_env(float pin, float tin, float tdin) {
-  Env e;
-  e.p = 100.0f * pin;
-  e.t = 273.15f + tin;
-  e.td = 273.15f + tdin;
-  if (FAST) {
+// Environment of one level (:232-240).
+template <typename R = float>
+struct EnvT {
+  R p, t, td, pi, q, th, thv;
+};
+using Env = EnvT<float>;
+
+// FAST (the accelerated solvers, float only): pi from exp(RDDCP ln(p/P00)),
+// q from getqvs_fast and the two quotients from approximate divides.
+template <bool FAST = false, typename R = float>
+XC_HD EnvT<R> make_env(R pin, R tin, R tdin) {
+  EnvT<R> e;
+  e.p = XC_LIT(R, 100.0) * pin;
+  e.t = XC_LIT(R, 273.15) + tin;
+  e.td = XC_LIT(R, 273.15) + tdin;
+  if constexpr (FAST) {
+    static_assert(sizeof(R) == sizeof(float), "the accelerated environment is FP32");
     float es;
     e.pi = fast_exp(RDDCP * fast_log(e.p * RP00));
     e.q = getqvs_fast(e.p, e.td, es);
     e.th = fast_div(e.t, e.pi);
     e.thv = fast_div(e.th * (1.0f + REPS * e.q), 1.0f + e.q);
   } else {
-    e.pi = powf(e.p * RP00, RDDCP);
+    e.pi = xpow(e.p * (R)RP00, (R)RDDCP);
     e.q = getqvs(e.p, e.td);
     e.th = e.t / e.pi;
-    e.thv = e.th * (1.0f + REPS * e.q) / (1.0f + e.q);
+    e.thv = e.th * (XC_LIT(R, 1.0) + (R)REPS * e.q) / (XC_LIT(R, 1.0) + e.q);
   }
   return e;
 }
@@ -54,12 +71,12 @@ XC_HD Env make_env(float pin, float tin, float tdin) {
 // The array pointers are those of all columns (the kernel's arguments) and
 // one 64-bit offset locates the column, so that a column costs the ascent
 // one register pair instead of three pointers.
-template <typename T, int GRID>
+template <typename T, int GRID, typename R = float>
 struct ColumnReader {
   const T *p;   // GRID 1/3: p of all columns; GRID 2: the shared p1d
   const T *t;   // t of all columns
   const T *td;  // td of all columns
-  float ps, ts, tds;
+  R ps, ts, tds;
   long long cbase;  // column offset + start - 3: t, td (and GRID 1/3 p) of level j at cbase + j
   int base;         // start - 3: the GRID 2 p of level j at base + j
 
@@ -72,28 +89,28 @@ struct ColumnReader {
   }
   XC_HD const T *p_at(int j) const { return GRID == 2 ? p + (base + j) : p + (cbase + j); }
 
-  XC_HD void level(int j, float &pin, float &tin, float &tdin) const {
+  XC_HD void level(int j, R &pin, R &tin, R &tdin) const {
     if (j == 1) {
       pin = ps;
       tin = ts;
       tdin = tds;
     } else {
-      pin = ldf(p_at(j));
-      tin = ldf(t + (cbase + j));
-      tdin = ldf(td + (cbase + j));
+      pin = (R)ld(p_at(j));
+      tin = (R)ld(t + (cbase + j));
+      tdin = (R)ld(td + (cbase + j));
     }
   }
   template <bool FAST = false>
-  XC_HD Env env(int j) const {
-    float a, b, c;
+  XC_HD EnvT<R> env(int j) const {
+    R a, b, c;
     level(j, a, b, c);
-    return make_env<FAST>(a, b, c);
+    return make_env<FAST, R>(a, b, c);
   }
   // level j >= 2 (above the surface): loops over those levels then need no
   // surface values, which frees their registers
   template <bool FAST = false>
-  XC_HD Env env_above(int j) const {
-    return make_env<FAST>(ldf(p_at(j)), ldf(t + (cbase + j)), ldf(td + (cbase + j)));
+  XC_HD EnvT<R> env_above(int j) const {
+    return make_env<FAST, R>((R)ld(p_at(j)), (R)ld(t + (cbase + j)), (R)ld(td + (cbase + j)));
   }
 };
 
@@ -207,45 +224,46 @@ XC_HD float dqsat_dt(float qsat, float p, float es, float tb, float k) {
 // qv2, ql2, qi2 at x.  The parcel starts the sub-step at (t1, th1, qv1, ql1,
 // qi1) with total water qt; p2, pi2 = (p2/P00)^(Rd/cp) and lp = ln(p2/p1).
 // plain_map is the reference's sequence of operations.
-template <bool ICE>
-XC_HD float plain_map(float x, float p2, float pi2, float lp, float t1, float th1, float qv1,
-                      float ql1, float qi1, float qt, float &t2, float &qv2, float &ql2,
-                      float &qi2) {
+template <bool ICE, typename R>
+XC_HD R plain_map(R x, R p2, R pi2, R lp, R t1, R th1, R qv1, R ql1, R qi1, R qt, R &t2, R &qv2,
+                  R &ql2, R &qi2) {
+  const R zero = XC_LIT(R, 0.0), one = XC_LIT(R, 1.0), half = XC_LIT(R, 0.5);
   t2 = x * pi2;
-  float fliq, fice, qsat;
+  R fliq, fice, qsat;
   if (ICE) {
-    fliq = fmax_f(fmin_f((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
-    fice = 1.0f - fliq;
+    fliq = fmax_f(fmin_f((t2 - XC_LIT(R, 233.15)) / (XC_LIT(R, 273.15) - XC_LIT(R, 233.15)), one),
+                  zero);
+    fice = one - fliq;
     qsat = fliq * getqvs(p2, t2) + fice * getqvi(p2, t2);
   } else {
-    fliq = 1.0f;
-    fice = 0.0f;
+    fliq = one;
+    fice = zero;
     qsat = getqvs(p2, t2);
   }
   qv2 = fmin_f(qt, qsat);
   if (ICE) {
-    qi2 = fmax_f(fice * (qt - qv2), 0.0f);
+    qi2 = fmax_f(fice * (qt - qv2), zero);
   } else {
-    qi2 = 0.0f;
+    qi2 = zero;
   }
-  ql2 = fmax_f(qt - qv2 - qi2, 0.0f);
-  const float tbar = 0.5f * (t1 + t2);
-  const float qvbar = 0.5f * (qv1 + qv2);
-  const float qlbar = 0.5f * (ql1 + ql2);
-  const float lhv = LV1 - LV2 * tbar;
-  const float rm = RD + RV * qvbar;
-  float expo;
+  ql2 = fmax_f(qt - qv2 - qi2, zero);
+  const R tbar = half * (t1 + t2);
+  const R qvbar = half * (qv1 + qv2);
+  const R qlbar = half * (ql1 + ql2);
+  const R lhv = (R)LV1 - (R)LV2 * tbar;
+  const R rm = (R)RD + (R)RV * qvbar;
+  R expo;
   if (ICE) {
-    const float qibar = 0.5f * (qi1 + qi2);
-    const float lhs = LS1 - LS2 * tbar;
-    const float cpm = CP + CPV * qvbar + CPL * qlbar + CPI * qibar;
+    const R qibar = half * (qi1 + qi2);
+    const R lhs = (R)LS1 - (R)LS2 * tbar;
+    const R cpm = (R)CP + (R)CPV * qvbar + (R)CPL * qlbar + (R)CPI * qibar;
     expo = lhv * (ql2 - ql1) / (cpm * tbar) + lhs * (qi2 - qi1) / (cpm * tbar) +
-           (rm / cpm - RDDCP) * lp;
+           (rm / cpm - (R)RDDCP) * lp;
   } else {
-    const float cpm = CP + CPV * qvbar + CPL * qlbar;
-    expo = lhv * (ql2 - ql1) / (cpm * tbar) + (rm / cpm - RDDCP) * lp;
+    const R cpm = (R)CP + (R)CPV * qvbar + (R)CPL * qlbar;
+    expo = lhv * (ql2 - ql1) / (cpm * tbar) + (rm / cpm - (R)RDDCP) * lp;
   }
-  return th1 * expf(expo);
+  return th1 * xexp(expo);
 }
 
 // The same map for the accelerated solvers: the approximate exp and divides
@@ -335,11 +353,12 @@ XC_HD float root_step(float x, float fx, float q) {
 // from the first guess x0 as a Newton step on F(x) - x, with the slope F'(x0)
 // of the map differentiated analytically at the first evaluation (accel_map
 // with slope).  Secant steps follow.  The stopping test is the reference's.
-template <bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN>
-XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
-                                        float &ql2, float &qi2, float &qt, int &niter,
-                                        SolverState &ss) {
-  const float p1 = p2, t1 = t2, th1 = th2, qv1 = qv2, ql1 = ql2, qi1 = qi2;
+template <bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN, typename R = float>
+XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, int &niter,
+                   SolverState &ss) {
+  static_assert(SOLVER == SOLVE_PLAIN || sizeof(R) == sizeof(float),
+                "only the plain solver runs in double precision");
+  const R p1 = p2, t1 = t2, th1 = th2, qv1 = qv2, ql1 = ql2, qi1 = qi2;
   p2 = p2 - dp;
   // The accelerated modes take pi2 and ln(p2/p1) from one logarithm of p2
   // (ln p1 is the previous sub-step's), with the approximate log and exp, in
@@ -349,20 +368,20 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
   // 0.02, and pi2 = exp(R_d/c_p (ln p2 - ln P00)) as a relative error of
   // about 1e-6 in t2, which the next sub-step's map does not carry forward.
   constexpr bool ACCEL_MATH = SOLVER != SOLVE_PLAIN;
-  float pi2, lp;
-  if (ACCEL_MATH) {
+  R pi2, lp;
+  if constexpr (ACCEL_MATH) {
     const float lnp2 = fast_log(p2);
     lp = lnp2 - ss.lnp;
     pi2 = fast_exp(RDDCP * (lnp2 - LN_P00));
     ss.lnp = lnp2;
   } else {
-    pi2 = powf(p2 * RP00, RDDCP);
-    lp = logf(p2 / p1);
+    pi2 = xpow(p2 * (R)RP00, (R)RDDCP);
+    lp = xlog(p2 / p1);
   }
-  float thlast = th1;
-  float x_prev = 0.0f, f_prev = 0.0f;
+  R thlast = th1;
+  R x_prev = XC_LIT(R, 0.0), f_prev = XC_LIT(R, 0.0);
   constexpr bool EXTRAP = SOLVER == SOLVE_ACCEL || SOLVER == SOLVE_LEARNED;
-  if (EXTRAP) {
+  if constexpr (EXTRAP) {
     // the first evaluation, at the extrapolated guess, also gives the map's
     // slope: a Newton step from it, then secant steps through the last two
     // evaluations (Newton again where x repeated)
@@ -382,16 +401,16 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
     }
     ss.rate = fast_div(th2 - th1, dp);
   } else {
-    float dth_net;
-    if (SOLVER == SOLVE_LEARNED_ALL && ss.saturated &&
-        network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net)) {
-      thlast = th1 + dth_net;
+    if constexpr (SOLVER == SOLVE_LEARNED_ALL) {
+      float dth_net;
+      if (ss.saturated && network_increment(ss.guess_w, p1, p2, t1, qv1, qt, lp, dth_net))
+        thlast = th1 + dth_net;
     }
     int i = 0;
     while (true) {
       i = i + 1;
-      float unused;
-      if (ACCEL_MATH) {
+      if constexpr (ACCEL_MATH) {
+        float unused;
         th2 = accel_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, false, t2, qv2,
                              ql2, qi2, unused);
       } else {
@@ -399,34 +418,40 @@ XC_HD bool substep(float dp, float &p2, float &t2, float &th2, float &qv2,
       }
       ++niter;
       if (i > 100) return false;
-      if (fabsf(th2 - thlast) > CONVERGE) {
-        if (ACCEL_MATH && i >= 2 && thlast != x_prev) {
-          const float q = fast_div(th2 - f_prev, thlast - x_prev);
-          x_prev = thlast;
-          f_prev = th2;
-          thlast = root_step(thlast, th2, q);  // secant step on F(x) - x
+      if (xabs(th2 - thlast) > XC_LIT(R, 0.0002)) {
+        bool secant = false;
+        if constexpr (ACCEL_MATH) secant = i >= 2 && thlast != x_prev;
+        if (secant) {
+          if constexpr (ACCEL_MATH) {
+            const float q = fast_div(th2 - f_prev, thlast - x_prev);
+            x_prev = thlast;
+            f_prev = th2;
+            thlast = root_step(thlast, th2, q);  // secant step on F(x) - x
+          }
         } else {
-          const float step = th2 - thlast;
+          const R step = th2 - thlast;
           x_prev = thlast;
           f_prev = th2;
-          thlast = thlast + 0.3f * step;
+          thlast = thlast + XC_LIT(R, 0.3) * step;
         }
       } else {
         break;
       }
     }
   }
-  if (SOLVER == SOLVE_LEARNED && ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y) {
-    // the parcel has just saturated: the increment extrapolated into the
-    // next sub-step is the network's, not this sub-step's partial one
-    ss.rate = -GUESS_SLOPE_SCALE * ss.lcl_y * fast_div(lp, dp);
-    ss.lcl_y = NAN;
+  if constexpr (SOLVER == SOLVE_LEARNED) {
+    if (ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y) {
+      // the parcel has just saturated: the increment extrapolated into the
+      // next sub-step is the network's, not this sub-step's partial one
+      ss.rate = -GUESS_SLOPE_SCALE * ss.lcl_y * fast_div(lp, dp);
+      ss.lcl_y = NAN;
+    }
   }
-  if (SOLVER == SOLVE_LEARNED_ALL) ss.saturated = ql2 + qi2 > 0.0f;
+  if constexpr (SOLVER == SOLVE_LEARNED_ALL) ss.saturated = ql2 + qi2 > 0.0f;
   if (PSEUDO) {  // :487-491
     qt = qv2;
-    ql2 = 0.0f;
-    qi2 = 0.0f;
+    ql2 = XC_LIT(R, 0.0);
+    qi2 = XC_LIT(R, 0.0);
   }
   return true;
 }
@@ -461,13 +486,13 @@ XC_HD int guess_pair(uint64_t seed, long long i, float *f, float *y) {
 
 // Running sum with Kahan compensation (SOLVE_ACCEL) or plain FP32 addition in
 // the reference's order (SOLVE_PLAIN).
-template <bool COMPENSATED>
+template <bool COMPENSATED, typename R = float>
 struct Acc {
-  float s = 0.0f, c = 0.0f;
-  XC_HD void add(float x) {
+  R s = XC_LIT(R, 0.0), c = XC_LIT(R, 0.0);
+  XC_HD void add(R x) {
     if (COMPENSATED) {
-      const float y = x - c;
-      const float t = s + y;
+      const R y = x - c;
+      const R t = s + y;
       c = (t - s) - y;
       s = t;
     } else {
@@ -493,19 +518,22 @@ constexpr int DIAG_N = 6;
 // The lifted parcel's source (:252-352): its level kmax, the mixed-layer
 // means (FP64 accumulation, :183), the most-unstable level (mulvl,
 // -999999 otherwise) and whether the ascent runs at all.
-struct SourceSel {
+template <typename R = float>
+struct SourceSelT {
   int kmax;
   int mulvl;
-  float avgth, avgqv;  // the FP64 means, rounded once (every use is in FP32)
+  R avgth, avgqv;  // the FP64 means, rounded once to R (every use is in R)
   bool ascend;
 };
+using SourceSel = SourceSelT<float>;
 
 // FAST: the accelerated solvers' theta-e (getthe_fast) for the most
 // unstable level and environment (make_env) in the mixed layer.
-template <bool FAST, typename T, int GRID>
-XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int source,
-                              float ml_depth) {
-  SourceSel sel;
+template <bool FAST, typename T, int GRID, typename R = float>
+XC_HD SourceSelT<R> select_source(const ColumnReader<T, GRID, R> &col, int ncl, int source,
+                                  R ml_depth) {
+  static_assert(!FAST || sizeof(R) == sizeof(float), "the accelerated source selection is FP32");
+  SourceSelT<R> sel;
   sel.mulvl = -999999;  // :252-253
   sel.ascend = true;
   int kmax = 1;
@@ -513,19 +541,25 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
 
   if (source == 2) {
     // :261-281 -- argmax of theta-e over levels with p >= 500 hPa, strict >.
-    const float p1 = 100.0f * col.ps;
-    if (!(p1 < 50000.0f)) {
-      float maxthe = 0.0f;
+    const R p1 = XC_LIT(R, 100.0) * col.ps;
+    if (!(p1 < XC_LIT(R, 50000.0))) {
+      R maxthe = XC_LIT(R, 0.0);
       for (int j = 1; j <= ncl; ++j) {
-        float pin, tin, tdin;
+        R pin, tin, tdin;
         col.level(j, pin, tin, tdin);
-        const float p = 100.0f * pin;
-        if (p >= 50000.0f) {
-          const float t = 273.15f + tin;
-          const float td = 273.15f + tdin;
-          float es;
-          const float q = FAST ? getqvs_fast(p, td, es) : getqvs(p, td);
-          const float the = FAST ? getthe_fast(p, t, td, q) : getthe(p, t, td, q);
+        const R p = XC_LIT(R, 100.0) * pin;
+        if (p >= XC_LIT(R, 50000.0)) {
+          const R t = XC_LIT(R, 273.15) + tin;
+          const R td = XC_LIT(R, 273.15) + tdin;
+          R q, the;
+          if constexpr (FAST) {
+            float es;
+            q = getqvs_fast(p, td, es);
+            the = getthe_fast(p, t, td, q);
+          } else {
+            q = getqvs(p, td);
+            the = getthe(p, t, td, q);
+          }
           if (the > maxthe) {
             sel.mulvl = j;
             maxthe = the;
@@ -538,26 +572,27 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
     // :284-339 -- mixed layer.  One upward pass evaluates the do-while
     // accumulation (:313-322) and the two guards (:287, :295), which need
     // z(2) and z(nk).
-    Env prev = col.template env<FAST>(1);
-    const Env e1 = prev;
-    float zprev = 0.0f, z2 = 0.0f;
+    const R half = XC_LIT(R, 0.5);
+    EnvT<R> prev = col.template env<FAST>(1);
+    const EnvT<R> e1 = prev;
+    R zprev = XC_LIT(R, 0.0), z2 = XC_LIT(R, 0.0);
     bool active = true;
     double acc_th = 0.0, acc_qv = 0.0;
-    Env last = prev;
+    EnvT<R> last = prev;
     for (int j = 2; j <= ncl; ++j) {
-      const Env e = col.template env_above<FAST>(j);
-      const float dz = -CPDG * 0.5f * (e.thv + prev.thv) * (e.pi - prev.pi);
-      const float z = zprev + dz;
+      const EnvT<R> e = col.template env_above<FAST>(j);
+      const R dz = -(R)CPDG * half * (e.thv + prev.thv) * (e.pi - prev.pi);
+      const R z = zprev + dz;
       if (j == 2) z2 = z;
       if (active) {
         if (z <= ml_depth) {
-          acc_th = acc_th + (double)(0.5f * (z - zprev) * (e.th + prev.th));
-          acc_qv = acc_qv + (double)(0.5f * (z - zprev) * (e.q + prev.q));
+          acc_th = acc_th + (double)(half * (z - zprev) * (e.th + prev.th));
+          acc_qv = acc_qv + (double)(half * (z - zprev) * (e.q + prev.q));
         } else {
-          const float th2 = prev.th + (e.th - prev.th) * (ml_depth - zprev) / (z - zprev);
-          const float qv2 = prev.q + (e.q - prev.q) * (ml_depth - zprev) / (z - zprev);
-          acc_th = acc_th + (double)(0.5f * (ml_depth - zprev) * (th2 + prev.th));
-          acc_qv = acc_qv + (double)(0.5f * (ml_depth - zprev) * (qv2 + prev.q));
+          const R th2 = prev.th + (e.th - prev.th) * (ml_depth - zprev) / (z - zprev);
+          const R qv2 = prev.q + (e.q - prev.q) * (ml_depth - zprev) / (z - zprev);
+          acc_th = acc_th + (double)(half * (ml_depth - zprev) * (th2 + prev.th));
+          acc_qv = acc_qv + (double)(half * (ml_depth - zprev) * (qv2 + prev.q));
           active = false;
         }
       }
@@ -568,10 +603,10 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
     if (active) {
       // The loop ran past the top (z(nk) == ml_depth): the interpolation
       // term is multiplied by ml_depth - z(nk) == 0, th2 = th(nk).
-      acc_th = acc_th + (double)(0.5f * (ml_depth - zprev) * (last.th + last.th));
-      acc_qv = acc_qv + (double)(0.5f * (ml_depth - zprev) * (last.q + last.q));
+      acc_th = acc_th + (double)(half * (ml_depth - zprev) * (last.th + last.th));
+      acc_qv = acc_qv + (double)(half * (ml_depth - zprev) * (last.q + last.q));
     }
-    if ((z2 - 0.0f) > ml_depth) {
+    if ((z2 - XC_LIT(R, 0.0)) > ml_depth) {
       avgth = e1.th;
       avgqv = e1.q;
       kmax = 1;
@@ -587,8 +622,8 @@ XC_HD SourceSel select_source(const ColumnReader<T, GRID> &col, int ncl, int sou
     }
   }
   sel.kmax = kmax;
-  sel.avgth = (float)avgth;
-  sel.avgqv = (float)avgqv;
+  sel.avgth = (R)avgth;
+  sel.avgqv = (R)avgqv;
   return sel;
 }
 
@@ -615,10 +650,12 @@ XC_HD void source_parcel(const ColumnReader<T, GRID> &col, const SourceSel &sel,
 // guess network's output at the parcel's LCL from `net_y` when guess_w is
 // null (the CAPE kernel evaluates it for a whole warp on the tensor cores),
 // and evaluates it here otherwise; a non-finite net_y means none.
-template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
-XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pinc, int source,
-                            const SourceSel &sel, const float *guess_w, float *dg,
+template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID, typename R = float>
+XC_HD CapeResult ascend_col(const ColumnReader<T, GRID, R> &col, int ncl, float pinc, int source,
+                            const SourceSelT<R> &sel, const float *guess_w, float *dg,
                             float net_y) {
+  static_assert((SOLVER == SOLVE_PLAIN && !DIAG) || sizeof(R) == sizeof(float),
+                "the double-precision ascent is the plain solver's, without diagnostics");
   CapeResult r;
   float d_plfc = DIAG_MISSING, d_zlfc = DIAG_MISSING, d_pel = DIAG_MISSING,
         d_zel = DIAG_MISSING, d_zsrc = DIAG_MISSING, d_the = DIAG_MISSING;
@@ -631,17 +668,18 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
   r.nsub = 0;
   r.niter = 0;
   const int kmax = sel.kmax;
-  const float avgth = sel.avgth, avgqv = sel.avgqv;
+  const R avgth = sel.avgth, avgqv = sel.avgqv;
+  const R zero = XC_LIT(R, 0.0), one = XC_LIT(R, 1.0), half = XC_LIT(R, 0.5);
 
   // Ascent (:355-559).  Levels below kmax only integrate z.
   constexpr bool FAST = SOLVER != SOLVE_PLAIN;
-  Env prev = col.template env<FAST>(1);
-  float z = 0.0f;
-  float th2 = 0.f, p2 = 0.f, t2 = 0.f, qv2 = 0.f, b2 = 0.f, ql2 = 0.f, qi2 = 0.f, qt = 0.f;
-  float narea = 0.0f;
+  EnvT<R> prev = col.template env<FAST>(1);
+  R z = zero;
+  R th2 = zero, p2 = zero, t2 = zero, qv2 = zero, b2 = zero, ql2 = zero, qi2 = zero, qt = zero;
+  R narea = zero;
   SolverState ss;
   ss.guess_w = guess_w;
-  if (SOLVER == SOLVE_LEARNED) {
+  if constexpr (SOLVER == SOLVE_LEARNED) {
     if (guess_w) {
       // the parcel that init_parcel will start at level kmax
       float p0, t0, td0, q0;
@@ -652,29 +690,29 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
       ss.lcl_y = net_y;
     }
   }
-  Acc<SOLVER != SOLVE_PLAIN> cape_acc, cin_acc;
-  auto init_parcel = [&](const Env &e) {
+  Acc<SOLVER != SOLVE_PLAIN, R> cape_acc, cin_acc;
+  auto init_parcel = [&](const EnvT<R> &e) {
     if (source == 3) {
       th2 = avgth;
       qv2 = avgqv;
-      const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2);
+      const R thv2 = th2 * (one + (R)REPS * qv2) / (one + qv2);
       p2 = e.p;
       t2 = th2 * e.pi;
-      b2 = G * (thv2 - e.thv) / e.thv;
+      b2 = (R)G * (thv2 - e.thv) / e.thv;
     } else {
       th2 = e.th;
       p2 = e.p;
       t2 = e.t;
       qv2 = e.q;
-      b2 = 0.0f;
+      b2 = zero;
     }
-    ql2 = 0.0f;
-    qi2 = 0.0f;
+    ql2 = zero;
+    qi2 = zero;
     qt = qv2;
-    if (SOLVER != SOLVE_PLAIN) ss.lnp = fast_log(p2);
+    if constexpr (SOLVER != SOLVE_PLAIN) ss.lnp = fast_log(p2);
   };
-  auto source_diag = [&](const Env &e) {
-    if (DIAG) {
+  auto source_diag = [&](const EnvT<R> &e) {
+    if constexpr (DIAG) {
       d_zsrc = z;
       d_the = source == 3 ? getthe(p2, t2, dewpoint_of(p2, qv2), qv2) : getthe(e.p, e.t, e.td, e.q);
     }
@@ -683,32 +721,33 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
     init_parcel(prev);
     source_diag(prev);
   }
-  float p_last = 0.0f;
+  R p_last = zero;
+  const R pinc_r = (R)pinc;
 
   for (int k = 2; k <= ncl; ++k) {
-    const Env cur = col.template env_above<FAST>(k);
-    const float dz = -CPDG * 0.5f * (cur.thv + prev.thv) * (cur.pi - prev.pi);
-    const float z_low = z;
+    const EnvT<R> cur = col.template env_above<FAST>(k);
+    const R dz = -(R)CPDG * half * (cur.thv + prev.thv) * (cur.pi - prev.pi);
+    const R z_low = z;
     z = z + dz;
     if (k == kmax) {
       init_parcel(cur);
       source_diag(cur);
     } else if (k > kmax) {
-      const float b1 = b2;
-      float dp = prev.p - cur.p;
+      const R b1 = b2;
+      R dp = prev.p - cur.p;
       int nloop;
-      if (dp < pinc) {
+      if (dp < pinc_r) {
         nloop = 1;
       } else {
-        const float f = dp / pinc;
-        if (!(f < (float)MAX_SUBSTEPS)) {
+        const R f = dp / pinc_r;
+        if (!(f < (R)MAX_SUBSTEPS)) {
           r.cape = 0.0f;
           r.cin = 0.0f;
           r.status |= COL_TOOMANYSTEPS;
           return r;
         }
         nloop = 1 + (int)f;
-        dp = dp / (float)nloop;
+        dp = dp / (R)nloop;
       }
       if (r.nsub + nloop > MAX_SUBSTEPS) {
         r.cape = 0.0f;
@@ -726,15 +765,15 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
         }
       }
       // :501-503 (FAST: approximate divides, which keep the sign of b2)
-      float thv2;
-      if (FAST) {
+      R thv2;
+      if constexpr (FAST) {
         thv2 = fast_div(th2 * (1.0f + REPS * qv2), 1.0f + qv2 + ql2 + qi2);
         b2 = fast_div(G * (thv2 - cur.thv), cur.thv);
       } else {
-        thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2 + ql2 + qi2);
-        b2 = G * (thv2 - cur.thv) / cur.thv;
+        thv2 = th2 * (one + (R)REPS * qv2) / (one + qv2 + ql2 + qi2);
+        b2 = (R)G * (thv2 - cur.thv) / cur.thv;
       }
-      if (DIAG) {
+      if constexpr (DIAG) {
         ascended = true;
         p_last = cur.p;
         if ((b2 >= 0.0f) && (b1 < 0.0f)) {
@@ -762,34 +801,35 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
         }
       }
       // :509-547
-      float parea;
-      if ((b2 >= 0.0f) && (b1 < 0.0f)) {
-        const float frac = b2 / (b2 - b1);
-        parea = 0.5f * b2 * dz * frac;
-        narea = narea - 0.5f * b1 * dz * (1.0f - frac);
+      R parea;
+      if ((b2 >= zero) && (b1 < zero)) {
+        const R frac = b2 / (b2 - b1);
+        parea = half * b2 * dz * frac;
+        narea = narea - half * b1 * dz * (one - frac);
         cin_acc.add(narea);
-        narea = 0.0f;
-      } else if ((b2 < 0.0f) && (b1 > 0.0f)) {
-        const float frac = b1 / (b1 - b2);
-        parea = 0.5f * b1 * dz * frac;
-        narea = -0.5f * b2 * dz * (1.0f - frac);
-      } else if (b2 < 0.0f) {
-        parea = 0.0f;
-        narea = narea - 0.5f * dz * (b1 + b2);
+        narea = zero;
+      } else if ((b2 < zero) && (b1 > zero)) {
+        const R frac = b1 / (b1 - b2);
+        parea = half * b1 * dz * frac;
+        narea = -half * b2 * dz * (one - frac);
+      } else if (b2 < zero) {
+        parea = zero;
+        narea = narea - half * dz * (b1 + b2);
       } else {
-        parea = 0.5f * dz * (b1 + b2);
-        narea = 0.0f;
+        parea = half * dz * (b1 + b2);
+        narea = zero;
       }
-      cape_acc.add(fmax_f(0.0f, parea));
-      r.z_out = z;
+      cape_acc.add(fmax_f(zero, parea));
+      r.z_out = (float)z;
       // :554-557
-      if ((cur.p <= 10000.0f) && (b2 < 0.0f)) break;
+      if ((cur.p <= XC_LIT(R, 10000.0)) && (b2 < zero)) break;
     }
     prev = cur;
   }
-  r.cape = cape_acc.s;
-  r.cin = cin_acc.s;
-  if (DIAG && ascended) {
+  r.cape = (float)cape_acc.s;
+  r.cin = (float)cin_acc.s;
+  if constexpr (DIAG) {
+   if (ascended) {
     if (have_lfc && b2 >= 0.0f) {
       d_pel = p_last / 100.0f;
       d_zel = r.z_out;
@@ -800,15 +840,16 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID> &col, int ncl, float pin
     dg[3] = have_lfc ? d_zel : DIAG_MISSING;
     dg[4] = d_zsrc;
     dg[5] = d_the;
+   }
   }
   return r;
 }
 
-template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID>
-XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pinc,
+template <bool ICE, bool PSEUDO, int SOLVER, bool DIAG, typename T, int GRID, typename R = float>
+XC_HD CapeResult getcape_col(const ColumnReader<T, GRID, R> &col, int ncl, float pinc,
                                   int source, float ml_depth, const float *guess_w = nullptr,
                                   float *dg = nullptr) {
-  const SourceSel sel = select_source<SOLVER != SOLVE_PLAIN>(col, ncl, source, ml_depth);
+  const SourceSelT<R> sel = select_source<SOLVER != SOLVE_PLAIN>(col, ncl, source, (R)ml_depth);
   if (!sel.ascend) {
     CapeResult r;
     r.mulvl = sel.mulvl;
@@ -828,14 +869,14 @@ XC_HD CapeResult getcape_col(const ColumnReader<T, GRID> &col, int ncl, float pi
 // (CAPE_CODE_model_lev.f90:76-89, CAPE_CODE_pressure_lev.f90:66-82, 151-167):
 // the ts > 0 gate, the start level, getcape, and the outputs of column i.
 template <typename T, int GRID, bool ICE, bool PSEUDO, int SOLVER = SOLVE_PLAIN,
-          bool DIAG = false>
+          bool DIAG = false, typename R = float>
 XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter,
                            const float *guess_w = nullptr) {
     float dg[DIAG_N];
     if (DIAG)
       for (int d = 0; d < DIAG_N; ++d) dg[d] = DIAG_MISSING;
     const long long stride = a.ld > 0 ? a.ld : a.nk;
-    const float ts = ldf((const T *)a.ts + i);
+    const R ts = (R)ld((const T *)a.ts + i);
     float cape = 0.0f, cin = 0.0f, zo = 0.0f;
     int mulvl = 0, status = 0;
     int start = 1;
@@ -846,15 +887,15 @@ XC_HD void cape_column_run(const CapeArgs &a, long long i, int &nsub, int &niter
         start = pres_lev_pos_col<T>((const T *)a.p, ld((const T *)a.ps + i), a.nk);
       }
     }
-    if (ts > 0.0f) {  // CAPE_CODE_model_lev.f90:77
+    if (ts > XC_LIT(R, 0.0)) {  // CAPE_CODE_model_lev.f90:77
       if (start < 1 || start > a.nk) {
         status = COL_BADSTART;
       } else {
-        ColumnReader<T, GRID> col;
+        ColumnReader<T, GRID, R> col;
         col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
-        col.ps = ldf((const T *)a.ps + i);
+        col.ps = (R)ld((const T *)a.ps + i);
         col.ts = ts;
-        col.tds = ldf((const T *)a.tds + i);
+        col.tds = (R)ld((const T *)a.tds + i);
         const int ncl = a.nk - start + 2;
         CapeResult r =
             getcape_col<ICE, PSEUDO, SOLVER, DIAG>(col, ncl, a.pinc, a.source, a.ml_depth, guess_w,

@@ -186,12 +186,19 @@ static void launch_bucket(const CapeArgs &a, unsigned short *bucket, unsigned *h
   order_bucket_kernel<T, GRID><<<blocks, 256, 0, s>>>(a, bucket, hist);
 }
 
+void order_workspace_parts(void *ws, long long n2, unsigned **hist, int **perm) {
+  char *b = (char *)ws;
+  *hist = (unsigned *)b;
+  *perm = (int *)(b + round256(sizeof(unsigned) * ORDER_BUCKETS) +
+                  round256(sizeof(unsigned short) * n2));
+}
+
 cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStream_t s) {
   char *b = (char *)ws;
-  unsigned *hist = (unsigned *)b;
+  unsigned *hist = nullptr;
+  int *pm = nullptr;
+  order_workspace_parts(ws, a.n2, &hist, &pm);
   unsigned short *bucket = (unsigned short *)(b + round256(sizeof(unsigned) * ORDER_BUCKETS));
-  int *pm = (int *)(b + round256(sizeof(unsigned) * ORDER_BUCKETS) +
-                    round256(sizeof(unsigned short) * a.n2));
   *perm = pm;
   if (a.n2 <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * ORDER_BUCKETS, s);

@@ -225,8 +225,11 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   if (rc) return rc;
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
+  const bool retry = (guess & XC_RETRY_FP64) != 0;
+  guess &= ~XC_RETRY_FP64;
   if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_EVERY)
     return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
+  if (retry && !status) return fail(XC_ERR_INVALID, "XC_RETRY_FP64 needs the status array");
   const float *guess_w = nullptr;
   if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY) {
     rc = guess_weights(&guess_w);
@@ -271,6 +274,10 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   }
   e = xc::launch_cape(a, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+  if (retry) {
+    e = xc::launch_retry64(a, workspace, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "FP64 retry launch");
+  }
   return XC_OK;
 }
 
@@ -356,28 +363,50 @@ int xc_loopcape_pl(const void *p3d, const void *t3d, const void *td3d, const voi
 }
 
 
-int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
-                        const void *ps, const void *ts, const void *tds, int dtype, float pinc,
-                        int source, float ml_depth, int adiabat, const int *start_3d, int nk,
-                        int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
-                        int *status, void *stream) {
+}  // extern "C"
+
+namespace {
+
+// The host-pointer CAPE path for nsrc sources of the same columns.  The
+// columns go through in chunks.  One stream copies the chunks' inputs in
+// order, once for all the sources; each chunk's ordering, its nsrc lifts and
+// its output copies run on one of two streams once its inputs are in, so
+// copies overlap lifts and one chunk's last warps overlap the next chunk's
+// first.  Every chunk has its own device slot when the ring budget allows
+// (the usual case), and then the calling thread queues the whole call
+// without waiting.  Outputs come back into pinned staging (a copy into
+// pageable memory would block this thread) and are moved into the caller's
+// arrays at the end, or when a slot is reused.  The column ordering depends
+// only on the start level and the surface dewpoint, not on the source, so
+// one ordering per chunk serves every source.  Each column is still computed
+// by one thread and written to its own index, so neither the chunking nor
+// the number of sources changes a result.  Outputs are [nsrc][n2].
+int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+              const void *ts, const void *tds, int dtype, float pinc, int nsrc,
+              const int *sources, float ml_depth, int adiabat, const int *start_3d, int nk,
+              int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out, int *status,
+              void *stream) {
   int rc = check_common(dtype, nk, n2);
   if (rc) return rc;
-  rc = check_cape_opts(pinc, source, ml_depth, adiabat);
-  if (rc) return rc;
+  if (nsrc < 1 || nsrc > 3 || !sources) return fail(XC_ERR_INVALID, "nsrc must be 1..3 with a source list");
+  for (int j = 0; j < nsrc; ++j) {
+    rc = check_cape_opts(pinc, sources[j], ml_depth, adiabat);
+    if (rc) return rc;
+  }
   if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1, 2 or 3");
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
+  const bool retry = (guess & XC_RETRY_FP64) != 0;
+  guess &= ~XC_RETRY_FP64;
+  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_EVERY)
+    return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
+  const float *guess_w = nullptr;
+  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY) {
+    rc = guess_weights(&guess_w);
+    if (rc) return rc;
+  }
   if (n2 == 0) return XC_OK;
-  // The columns go through in chunks.  One stream copies the chunks' inputs
-  // in order; each chunk's lift and output copy run on one of two streams
-  // once its inputs are in, so copies overlap lifts and one chunk's last
-  // warps overlap the next chunk's first.  Every chunk has its own device
-  // slot when the ring budget allows (the usual case), and then this thread
-  // queues the whole call without waiting.  Outputs come back into pinned
-  // staging (a copy into pageable memory would block this thread) and are
-  // moved into the caller's arrays at the end, or when a slot is reused.
-  // Each column is still computed by one thread and written to its own
-  // index, so the chunking changes no result.
+  if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
+    return fail(XC_ERR_INVALID, "NULL array argument");
   int nchunk = (n2 + HOST_CHUNK_MIN - 1) / HOST_CHUNK_MIN;
   if (nchunk > HOST_CHUNKS) nchunk = HOST_CHUNKS;
   // Chunk c holds columns [bound[c], bound[c + 1]).  With three or more
@@ -399,53 +428,48 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
   const size_t es = dtype == XC_F32 ? 4 : 8;
   const size_t c3 = (size_t)C * nk;
   const bool has_start = grid != 1 && start_3d;
+  // cape, cin, mulvl, z_out (, status: the caller's, or the retry's flags) per source
+  const int nout = (status || retry) ? 5 : 4;
   std::lock_guard<std::mutex> lk(g_ws_mu);
   Pipeline *pl = nullptr;
   rc = pipeline_get(&pl);
   if (rc) return rc;
   struct Slot {
-    size_t p, t, td, ps, ts, tds, st, cape, cin, mu, z, stat, ord;
+    size_t p, t, td, ps, ts, tds, st, out, ord;
   } sl[HOST_CHUNKS];
   const size_t ord_bytes = xc::order_workspace_bytes(C);
+  const size_t out_bytes = (size_t)nsrc * nout * C * 4;  // [nsrc][nout][C]
+  auto carve = [&](Carver &cv, Slot &q) {
+    q.p = cv.take((grid == 2 ? (size_t)nk : c3) * es);
+    q.t = cv.take(c3 * es);
+    q.td = cv.take(c3 * es);
+    q.ps = cv.take((size_t)C * es);
+    q.ts = cv.take((size_t)C * es);
+    q.tds = cv.take((size_t)C * es);
+    q.st = has_start ? cv.take((size_t)C * 4) : 0;
+    q.out = cv.take(out_bytes);
+    q.ord = cv.take(ord_bytes);
+  };
   size_t slot_bytes = 0;
   {
     Carver one;
-    one.take((grid == 2 ? (size_t)nk : c3) * es);
-    one.take(c3 * es);
-    one.take(c3 * es);
-    for (int j = 0; j < 3; ++j) one.take((size_t)C * es);
-    if (has_start) one.take((size_t)C * 4);
-    for (int j = 0; j < (status ? 5 : 4); ++j) one.take((size_t)C * 4);
-    one.take(ord_bytes);
+    Slot q;
+    carve(one, q);
     slot_bytes = one.off;
   }
   int nslot = (int)(host_ring_bytes() / slot_bytes);
   if (nslot < 2) nslot = 2;
   if (nslot > nchunk) nslot = nchunk;
   Carver cv;
-  for (int k = 0; k < nslot; ++k) {
-    sl[k].p = cv.take((grid == 2 ? (size_t)nk : c3) * es);
-    sl[k].t = cv.take(c3 * es);
-    sl[k].td = cv.take(c3 * es);
-    sl[k].ps = cv.take((size_t)C * es);
-    sl[k].ts = cv.take((size_t)C * es);
-    sl[k].tds = cv.take((size_t)C * es);
-    sl[k].st = has_start ? cv.take((size_t)C * 4) : 0;
-    sl[k].cape = cv.take((size_t)C * 4);
-    sl[k].cin = cv.take((size_t)C * 4);
-    sl[k].mu = cv.take((size_t)C * 4);
-    sl[k].z = cv.take((size_t)C * 4);
-    sl[k].stat = status ? cv.take((size_t)C * 4) : 0;
-    sl[k].ord = cv.take(ord_bytes);
-  }
+  for (int k = 0; k < nslot; ++k) carve(cv, sl[k]);
   void *base = nullptr;
   rc = ws_get(cv.off, &base);
   if (rc) return rc;
   char *b = (char *)base;
-  const int nout = status ? 5 : 4;
-  const size_t slot_out = (size_t)nout * C * 4;
-  rc = pipeline_pinned(pl, slot_out * nslot);
+  rc = pipeline_pinned(pl, out_bytes * nslot);
   if (rc) return rc;
+  // output array j of source s in a slot (device or its pinned staging)
+  auto out_off = [&](int s_, int j) { return ((size_t)s_ * nout + j) * C * 4; };
   // moves chunk c's outputs from its slot's staging into the caller's arrays
   auto finish = [&](int c) -> int {
     const int k = c % nslot;
@@ -453,12 +477,15 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     const size_t nc = (size_t)(bound[c + 1] - bound[c]);
     const cudaError_t we = cudaEventSynchronize(pl->done[k]);
     if (we != cudaSuccess) return cuda_fail(we, "device-to-host copy");
-    const char *h = pl->pinned + k * slot_out;
-    memcpy(cape + c0, h, nc * 4);
-    memcpy(cin + c0, h + (size_t)C * 4, nc * 4);
-    memcpy(mulvl + c0, h + (size_t)2 * C * 4, nc * 4);
-    memcpy(z_out + c0, h + (size_t)3 * C * 4, nc * 4);
-    if (status) memcpy(status + c0, h + (size_t)4 * C * 4, nc * 4);
+    const char *h = pl->pinned + k * out_bytes;
+    for (int s_ = 0; s_ < nsrc; ++s_) {
+      const size_t o = (size_t)s_ * n2 + c0;
+      memcpy(cape + o, h + out_off(s_, 0), nc * 4);
+      memcpy(cin + o, h + out_off(s_, 1), nc * 4);
+      memcpy(mulvl + o, h + out_off(s_, 2), nc * 4);
+      memcpy(z_out + o, h + out_off(s_, 3), nc * 4);
+      if (status) memcpy(status + o, h + out_off(s_, 4), nc * 4);
+    }
     return XC_OK;
   };
   cudaError_t e = cudaEventRecord(pl->start, (cudaStream_t)stream);
@@ -474,7 +501,7 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     const int k = c % nslot;
     if (c >= nslot) {
       // the slot still holds chunk c - nslot: its outputs leave the staging
-      // first, and its lift (before its output copy) is done with the inputs
+      // first, and its lifts (before its output copies) are done with the inputs
       rc = finish(c - nslot);
       if (rc) return rc;
     }
@@ -499,23 +526,55 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     if (e == cudaSuccess) e = cudaEventRecord(pl->loaded[k], pl->copy);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, pl->loaded[k], 0);
     if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
-    rc = xc_loopcape_ex(grid, b + q.p, b + q.t, b + q.td, b + q.ps, b + q.ts, b + q.tds, dtype,
-                        pinc, source, ml_depth, adiabat, has_start ? (const int *)(b + q.st) : nullptr,
-                        nk, nc, guess, (float *)(b + q.cape), (float *)(b + q.cin),
-                        (int *)(b + q.mu), (float *)(b + q.z),
-                        status ? (int *)(b + q.stat) : nullptr, nullptr, b + q.ord, ord_bytes, s);
-    if (rc) return rc;
-    char *h = pl->pinned + k * slot_out;
-#define D2H(j, off)                                                                  \
-    if (e == cudaSuccess)                                                            \
-      e = cudaMemcpyAsync(h + (size_t)(j) * C * 4, b + (off), (size_t)nc * 4,        \
-                          cudaMemcpyDeviceToHost, s)
-    D2H(0, q.cape);
-    D2H(1, q.cin);
-    D2H(2, q.mu);
-    D2H(3, q.z);
-    if (status) D2H(4, q.stat);
-#undef D2H
+    xc::CapeArgs a;
+    a.grid = grid;
+    a.dtype = dtype;
+    a.p = b + q.p;
+    a.t = b + q.t;
+    a.td = b + q.td;
+    a.ps = b + q.ps;
+    a.ts = b + q.ts;
+    a.tds = b + q.tds;
+    a.start = has_start ? (const int *)(b + q.st) : nullptr;
+    a.pinc = pinc;
+    a.ml_depth = ml_depth;
+    a.adiabat = adiabat;
+    a.nk = nk;
+    a.n2 = nc;
+    a.guess = guess;
+    a.counters = nullptr;
+    a.perm = nullptr;
+    a.guess_w = guess_w;
+    e = xc::launch_order(a, b + q.ord, &a.perm, s);
+    if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
+    auto point = [&](int s_) {
+      char *o = b + q.out;
+      a.source = sources[s_];
+      a.cape = (float *)(o + out_off(s_, 0));
+      a.cin = (float *)(o + out_off(s_, 1));
+      a.mulvl = (int *)(o + out_off(s_, 2));
+      a.z_out = (float *)(o + out_off(s_, 3));
+      a.status = nout == 5 ? (int *)(o + out_off(s_, 4)) : nullptr;
+    };
+    for (int s_ = 0; s_ < nsrc; ++s_) {
+      point(s_);
+      e = xc::launch_cape(a, s);
+      if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+    }
+    // the FP64 retries come after every source's lift: each reuses the
+    // ordering workspace, which the lifts read
+    for (int s_ = 0; retry && s_ < nsrc; ++s_) {
+      point(s_);
+      e = xc::launch_retry64(a, b + q.ord, s);
+      if (e != cudaSuccess) return cuda_fail(e, "FP64 retry launch");
+    }
+    // copies of the slot's outputs: [nsrc][nout][C], of which the first nc
+    // entries of each array are this chunk's (the status only if asked for)
+    char *h = pl->pinned + k * out_bytes;
+    for (int j = 0; j < nsrc * nout && e == cudaSuccess; ++j)
+      if (j % nout < 4 || status)
+        e = cudaMemcpyAsync(h + (size_t)j * C * 4, b + q.out + (size_t)j * C * 4,
+                            (size_t)nc * 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaEventRecord(pl->done[k], s);
     if (e != cudaSuccess) return cuda_fail(e, "device-to-host copy");
     issued = c + 1;
@@ -525,6 +584,28 @@ int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td
     if (rc) return rc;
   }
   return XC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
+                        const void *ps, const void *ts, const void *tds, int dtype, float pinc,
+                        int source, float ml_depth, int adiabat, const int *start_3d, int nk,
+                        int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
+                        int *status, void *stream) {
+  return host_lift(grid, p, t3d, td3d, ps, ts, tds, dtype, pinc, 1, &source, ml_depth, adiabat,
+                   start_3d, nk, n2, guess, cape, cin, mulvl, z_out, status, stream);
+}
+
+int xc_loopcape_multi_host(int grid, const void *p, const void *t3d, const void *td3d,
+                           const void *ps, const void *ts, const void *tds, int dtype, float pinc,
+                           int nsrc, const int *sources, float ml_depth, int adiabat,
+                           const int *start_3d, int nk, int n2, int guess, float *cape,
+                           float *cin, int *mulvl, float *z_out, int *status, void *stream) {
+  return host_lift(grid, p, t3d, td3d, ps, ts, tds, dtype, pinc, nsrc, sources, ml_depth, adiabat,
+                   start_3d, nk, n2, guess, cape, cin, mulvl, z_out, status, stream);
 }
 
 int xc_calc_srh(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #if defined(__CUDACC__)
@@ -137,8 +138,42 @@ XC_HD float getqvi_fast(float p, float t, float &es_out) {
 
 // Fortran MIN/MAX as gfortran lowers them for the reference build: the
 // second operand is returned when the comparison fails (NaN included).
-XC_HD float fmin_f(float a, float b) { return a < b ? a : b; }
-XC_HD float fmax_f(float a, float b) { return a > b ? a : b; }
+template <typename R>
+XC_HD R fmin_f(R a, R b) { return a < b ? a : b; }
+template <typename R>
+XC_HD R fmax_f(R a, R b) { return a > b ? a : b; }
+
+// ---- double precision (the FP64 retry of the CAPE lift) -------------------
+// getqvs / getqvi / getthe in double precision with double literals: the
+// same formulas (CAPE_CODE_model_lev.f90:570-620) evaluated as the FP64
+// oracle evaluates them.
+XC_HD double getqvs(double p, double t) {
+  const double es = 611.2 * exp(17.67 * (t - 273.15) / (t - 29.65));
+  return (287.04 / 461.5) * es / (p - es);
+}
+XC_HD double getqvi(double p, double t) {
+  const double es = 611.2 * exp(21.8745584 * (t - 273.15) / (t - 7.66));
+  return (287.04 / 461.5) * es / (p - es);
+}
+XC_HD double getthe(double p, double t, double td, double q) {
+  double tlcl;
+  if ((td - t) >= -0.1) {
+    tlcl = t;
+  } else {
+    tlcl = 56.0 + 1.0 / (1.0 / (td - 56.0) + 0.00125 * log(t / td));
+  }
+  return t * pow(100000.0 / p, 0.2854 * (1.0 - 0.28 * q)) *
+         exp(((3376.0 / tlcl) - 2.54) * q * (1.0 + 0.81 * q));
+}
+
+// exp, log and pow of the column routines in their precision: CUDA's (or
+// libm's) single-precision functions for float, double ones for double.
+XC_HD float xexp(float x) { return expf(x); }
+XC_HD double xexp(double x) { return exp(x); }
+XC_HD float xlog(float x) { return logf(x); }
+XC_HD double xlog(double x) { return log(x); }
+XC_HD float xpow(float a, float b) { return powf(a, b); }
+XC_HD double xpow(double a, double b) { return pow(a, b); }
 
 // ---- input loads ------------------------------------------------------------
 template <typename T>

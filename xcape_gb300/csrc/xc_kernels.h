@@ -59,6 +59,13 @@ size_t order_workspace_bytes(long long n2);
 // Carves `ws` (order_workspace_bytes(n2) bytes, 256-byte aligned) and
 // launches the three ordering kernels; on return *perm points into ws.
 cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStream_t s);
+// The first bucket counter and the permutation of an ordering workspace.
+void order_workspace_parts(void *ws, long long n2, unsigned **hist, int **perm);
+
+// FP64 retry of the columns whose status has COL_NOCONV (cape_retry.cu), on
+// `s` after the lift; ws (nullable) is the lift's ordering workspace, reused
+// for the list of those columns.  a.status must be set.
+cudaError_t launch_retry64(const CapeArgs &a, void *ws, cudaStream_t s);
 
 // Records msg as the calling thread's xc_last_error() text (capi.cu).
 int set_error(int code, const char *msg);
