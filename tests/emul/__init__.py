@@ -46,7 +46,7 @@ def lib():
         L.emu_guess_eval.restype = f
         L.emu_guess_eval_packed.argtypes = [vp, f, f, f]
         L.emu_guess_eval_packed.restype = f
-        L.emu_guess_pairs.argtypes = [ll, ctypes.c_ulonglong, vp, vp, vp]
+        L.emu_guess_pairs.argtypes = [ll, ctypes.c_ulonglong, vp, vp, vp, vp]
         L.emu_accel_map.argtypes = [i] + [f] * 10 + [vp]
         L.emu_accel_map.restype = f
         L.emu_request_layout.argtypes = [vp]

@@ -176,8 +176,9 @@ extern "C" float emu_accel_map(int ice, float x, float p2, float pi2, float lp, 
 }
 
 extern "C" void emu_guess_pairs(long long n, unsigned long long seed, float *feats,
-                                float *targets, int *iters) {
-  for (long long i = 0; i < n; ++i) iters[i] = guess_pair(seed, i, feats + 3 * i, targets + i);
+                                float *targets, int *iters, int *adiabats) {
+  for (long long i = 0; i < n; ++i)
+    iters[i] = guess_pair(seed, i, feats + 3 * i, targets + i, adiabats ? adiabats + i : nullptr);
 }
 
 // Size and field offsets of xc_cape_request, for the ctypes layout check.

@@ -4,8 +4,9 @@ the gradient and inference checks.
 forward(..., bf16_hidden=True) reproduces the GPU training/inference
 forward pass: the 64x64 hidden layer multiplies BF16-rounded activations by
 BF16-rounded weights (exact products, accumulated here in FP64); everything
-else is FP64.  backward() follows guess_train_kernel: dW2 uses the FP32
-activations, dH1 the FP32 master weights.
+else is FP64.  loss_and_grad() follows guess_train_kernel, whose two
+backward products run on the tensor cores too: dW2 = dZ2^T H1 and
+dH1 = dZ2 W2 take BF16-rounded operands (exact products, FP64 sums here).
 """
 import numpy as np
 
@@ -44,9 +45,10 @@ def loss_and_grad(w, x, t):
     g[OFF_W3:OFF_B3] = h2.T @ dy
     g[OFF_B3] = dy.sum()
     dz2 = (dy[:, None] * w3[None, :]) * (z2 > 0)
-    g[OFF_W2:OFF_B2] = (dz2.T @ h1).ravel()
+    q = lambda a: bf16_round(np.asarray(a, np.float32)).astype(np.float64)
+    g[OFF_W2:OFF_B2] = (q(dz2).T @ q(h1)).ravel()
     g[OFF_B2:OFF_W3] = dz2.sum(0)
-    dz1 = (dz2 @ W2) * (h1 > 0)
+    dz1 = (q(dz2) @ q(W2)) * (h1 > 0)
     g[OFF_W1:OFF_B1] = (dz1.T @ x).ravel()
     g[OFF_B1:OFF_W2] = dz1.sum(0)
     return loss, g

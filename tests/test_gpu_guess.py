@@ -49,7 +49,7 @@ def test_pairs_match_host_build(pairs):
     f, y, it = pairs
     n = len(y)
     fh, yh, ith = (np.zeros((n, 3), np.float32), np.zeros(n, np.float32), np.zeros(n, np.int32))
-    emul.lib().emu_guess_pairs(n, 123, fh.ctypes.data, yh.ctypes.data, ith.ctypes.data)
+    emul.lib().emu_guess_pairs(n, 123, fh.ctypes.data, yh.ctypes.data, ith.ctypes.data, None)
     # same draws; CUDA's and glibc's expf/powf/logf differ by an ulp or two,
     # and the iteration stops anywhere within its 2e-4 K tolerance
     np.testing.assert_allclose(f, fh, rtol=1e-5, atol=1e-5)

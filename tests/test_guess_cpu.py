@@ -41,25 +41,44 @@ def test_host_guess_eval_matches_numpy():
     np.testing.assert_array_equal(packed, got)
 
 
-def emulated_pairs(n, seed):
+def emulated_pairs(n, seed, with_adiabat=False):
     L = emul.lib()
     f = np.zeros((n, 3), np.float32)
     y = np.zeros(n, np.float32)
     it = np.zeros(n, np.int32)
-    L.emu_guess_pairs(n, seed, f.ctypes.data, y.ctypes.data, it.ctypes.data)
-    return f, y, it
+    adi = np.zeros(n, np.int32)
+    L.emu_guess_pairs(n, seed, f.ctypes.data, y.ctypes.data, it.ctypes.data, adi.ctypes.data)
+    return (f, y, it, adi) if with_adiabat else (f, y, it)
 
 
-def test_training_pairs_are_physical():
-    f, y, it = emulated_pairs(20000, 3)
+def test_training_pairs_cover_the_state_box():
+    """Pairs over the four adiabats, p 100..1050 hPa and T -80..40 degC
+    (saturation mixing ratio capped at 40 g/kg; the reversible adiabats
+    carry up to 10 g/kg of condensate).  Within atmospheric states
+    (theta-e below 380 K) the plain iteration solves every pair, and below
+    400 K all but a few hot, moist ones near the ground, where FP32 rounding
+    locks it into a cycle (as in real columns); it gives up mostly in the
+    hot, moist corners of the box at low pressure.  Training leaves the
+    unsolved pairs out."""
+    f, y, it, adi = emulated_pairs(40000, 3, with_adiabat=True)
     p2 = G_P_MID + G_P_SCALE * f[:, 0]
     assert p2.min() > 9000 and p2.max() < 105000
-    assert np.all(f[:, 2] * 0.02 + 0.01 <= 0.04 + 1e-6)   # qt <= 40 g/kg
-    assert np.all(it > 0), "the plain iteration solves every pair"
-    # the moist-adiabat increment: positive, largest for warm moist parcels
-    assert y.min() > 0 and y.max() < 1.5
-    warm = f[:, 2] > 0.0  # qt > 10 g/kg
-    assert y[warm].mean() > 2 * y[~warm].mean()
+    qt = (f[:, 2] + 0.5) / 50.0
+    assert np.all(qt <= 0.05 + 1e-6)
+    assert sorted(set(adi.tolist())) == [1, 2, 3, 4]
+    for a in (1, 2, 3, 4):
+        assert abs(np.mean(adi == a) - 0.25) < 0.02
+    the = 320.0 + 40.0 * f[:, 1]
+    assert np.all(it[the < 380.0] > 0), "the plain iteration solves every atmospheric pair"
+    atm = the < 400.0
+    assert np.mean(it[atm] > 0) > 0.999
+    assert np.mean(it > 0) > 0.8
+    # the moist-adiabat increment of solved atmospheric pairs: non-negative,
+    # largest for warm moist parcels
+    ok = atm & (it > 0)
+    assert y[ok].min() > -0.05 and y[ok].max() < 2.0
+    warm = ok & (qt > 0.01)
+    assert y[warm].mean() > 2 * y[ok & (qt <= 0.01)].mean()
 
 
 def test_pairs_are_deterministic():

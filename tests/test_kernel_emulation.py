@@ -377,3 +377,24 @@ def test_emulated_fp64_plain_solver_vs_fp64_oracle(source, adiabat):
     # in double precision the plain iteration converges where FP32 cycled
     f32 = _oracle(2, plev, t, td, ps, ts, tds, source, adiabat)
     assert (got["status"] & 1).sum() <= (f32["status"] & 1).sum()
+
+
+@pytest.mark.parametrize("guess", [1, 2, 3])
+@pytest.mark.parametrize("source", SOURCES)
+def test_emulated_surface_on_a_pressure_level(source, guess):
+    """ps exactly equal to a pressure level: the first sub-step above the
+    surface has no pressure drop.  The accelerated solvers extrapolate the
+    previous sub-step's increment per unit pressure, which such a step does
+    not define; they must stay finite and agree with the FP64 oracle like
+    every other column (the plain solver is pinned bit for bit elsewhere)."""
+    from xcape_gb300 import guess as G
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(16, 48), seed=17)
+    ps = ps.copy().ravel()
+    ps[::2] = plev[np.arange(ps.size // 2) % 12].astype(ps.dtype)  # 1000..725 hPa
+    w = G.bf16_round(G.init_weights(5, 0.3)) if guess == 1 else None
+    got = _emu_cape(2, plev, t, td, ps, ts, tds, source, 1, guess=guess, guess_w=w)
+    ref = _oracle(2, plev, t, td, ps, ts, tds, source, 1, precision="f64")
+    assert np.all(np.isfinite(got["cape"])) and np.all(np.isfinite(got["cin"]))
+    conv = ((ref["status"] & 1) == 0) & (got["mulvl"] == ref["mulvl"])
+    d = np.abs(got["cape"][conv].astype(np.float64) - ref["cape"][conv])
+    assert np.all(d <= np.maximum(1.0, 1e-3 * np.abs(ref["cape"][conv]))), d.max()

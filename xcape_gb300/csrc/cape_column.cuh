@@ -399,7 +399,10 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
       f_prev = th2;
       thlast = root_step(thlast, th2, q);
     }
-    ss.rate = fast_div(th2 - th1, dp);
+    // a sub-step without a pressure drop (a level at the pressure of the
+    // one below it, e.g. the surface exactly on a pressure level) has no
+    // rate to extrapolate: 0/0 would make every later guess NaN
+    if (dp != 0.0f) ss.rate = fast_div(th2 - th1, dp);
   } else {
     if constexpr (SOLVER == SOLVE_LEARNED_ALL) {
       float dth_net;
@@ -440,7 +443,7 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
     }
   }
   if constexpr (SOLVER == SOLVE_LEARNED) {
-    if (ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y) {
+    if (ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y && dp != 0.0f) {
       // the parcel has just saturated: the increment extrapolated into the
       // next sub-step is the network's, not this sub-step's partial one
       ss.rate = -GUESS_SLOPE_SCALE * ss.lcl_y * fast_div(lp, dp);
@@ -456,31 +459,57 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
   return true;
 }
 
-// Training pair i of the guess network: a saturated pseudo-adiabatic parcel
-// state (p1 in 100..1050 hPa, T1 in a 60 K band whose warm edge cools from
-// 30 degC at 1050 hPa to -40 degC at 100 hPa, never below -80 degC, at most
-// 40 g/kg of water), a pressure step dp log-uniform in 50..2000 Pa, and the
-// plain solver's (the reference's iteration's) solution of that sub-step.
-// Writes the features and the target y of guess_mlp.cuh; returns the
-// iteration count, negative when the plain iteration gave up.
-XC_HD int guess_pair(uint64_t seed, long long i, float *f, float *y) {
+// Liquid fraction of the ice adiabats' condensate at temperature t (K): the
+// linear ramp between 233.15 and 273.15 K of the map (:441-444).
+XC_HD float liquid_fraction(float t) {
+  return fmax_f(fmin_f((t - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
+}
+
+// Training pair i of the guess network, over the four adiabats: the adiabat
+// (pseudo/reversible x liquid/ice, uniform), a saturated parcel state with p1
+// uniform in 100..1050 hPa (less the step) and T1 uniform in -80..40 degC,
+// cooled in 2 K steps until its saturation mixing ratio is at most 40 g/kg
+// (the warm corner of that box at low pressure holds more water than any
+// atmosphere); the reversible adiabats carry 0..10 g/kg of condensate, split
+// into liquid and ice by the ramp; a pressure step dp log-uniform in
+// 50..2000 Pa; and the plain solver's (the reference's iteration's) solution
+// of that sub-step.  Writes the features and the target y of guess_mlp.cuh
+// and, when adiabat_out is set, the adiabat code; returns the iteration
+// count, negative when the plain iteration gave up.
+XC_HD int guess_pair(uint64_t seed, long long i, float *f, float *y, int *adiabat_out = nullptr) {
+  const int adiabat = 1 + (int)fminf(3.0f, 4.0f * guess_uniform01(seed, i, 3));
+  const bool ice = adiabat >= 3, pseudo = adiabat == 1 || adiabat == 3;
   const float dp = 50.0f * expf(3.6888795f * guess_uniform01(seed, i, 1));  // 50 * 40^u
   const float p1 = 10000.0f + dp + (95000.0f - dp) * guess_uniform01(seed, i, 0);
-  const float t_hi = 303.15f - 70.0f * (1.0f - p1 / 105000.0f);
-  const float t_lo = fmaxf(193.15f, t_hi - 60.0f);
-  float t1 = t_lo + (t_hi - t_lo) * guess_uniform01(seed, i, 2);
-  float qv1 = getqvs(p1, t1);
+  float t1 = 193.15f + 120.0f * guess_uniform01(seed, i, 2);
+  auto qsat = [&](float t) {
+    if (!ice) return getqvs(p1, t);
+    const float fl = liquid_fraction(t);
+    return fl * getqvs(p1, t) + (1.0f - fl) * getqvi(p1, t);
+  };
+  float qv1 = qsat(t1);
   for (int k = 0; k < 64 && !(qv1 > 0.0f && qv1 <= 0.04f); ++k) {
     t1 -= 2.0f;
-    qv1 = getqvs(p1, t1);
+    qv1 = qsat(t1);
   }
+  const float cond = pseudo ? 0.0f : 0.01f * guess_uniform01(seed, i, 4);
+  const float fl = ice ? liquid_fraction(t1) : 1.0f;
   const float th1 = t1 / powf(p1 * RP00, RDDCP);
-  float p2 = p1, t2 = t1, th2 = th1, qv2 = qv1, ql2 = 0.0f, qi2 = 0.0f, qt = qv1;
+  float p2 = p1, t2 = t1, th2 = th1, qv2 = qv1, ql2 = fl * cond, qi2 = (1.0f - fl) * cond;
+  float qt = qv1 + cond;
+  const float qt1 = qt;
   int niter = 0;
   SolverState ss;
-  const bool ok = substep<false, true, SOLVE_PLAIN>(dp, p2, t2, th2, qv2, ql2, qi2, qt, niter, ss);
-  guess_features(p2, getthe(p1, t1, t1, qv1), qv1, f[0], f[1], f[2]);
+  bool ok;
+  switch (adiabat) {
+    case 1: ok = substep<false, true, SOLVE_PLAIN>(dp, p2, t2, th2, qv2, ql2, qi2, qt, niter, ss); break;
+    case 2: ok = substep<false, false, SOLVE_PLAIN>(dp, p2, t2, th2, qv2, ql2, qi2, qt, niter, ss); break;
+    case 3: ok = substep<true, true, SOLVE_PLAIN>(dp, p2, t2, th2, qv2, ql2, qi2, qt, niter, ss); break;
+    default: ok = substep<true, false, SOLVE_PLAIN>(dp, p2, t2, th2, qv2, ql2, qi2, qt, niter, ss); break;
+  }
+  guess_features(p2, getthe(p1, t1, t1, qv1), qt1, f[0], f[1], f[2]);
   *y = (th2 - th1) / (GUESS_SLOPE_SCALE * logf(p1 / p2));
+  if (adiabat_out) *adiabat_out = adiabat;
   return ok ? niter : -niter;
 }
 

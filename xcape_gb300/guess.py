@@ -105,13 +105,25 @@ def evaluate(weights, feats):
     return out
 
 
-def train(n_pairs=1 << 21, epochs=12, batch=8192, lr=2e-3, seed=7, log=print):
-    """Trains the network on the GPU; returns (weights rounded to BF16, meta)."""
+# outputs outside this range are not used by the solvers (guess_mlp.cuh)
+Y_MIN, Y_MAX = -0.2, 2.0
+
+
+def train(n_pairs=10_000_000, epochs=12, batch=16384, lr=2e-3, seed=7, log=print):
+    """Trains the network on the GPU; returns (weights rounded to BF16, meta).
+
+    The pairs cover the four adiabats over p 100..1050 hPa and T -80..40 degC
+    (xc_guess_pairs); those the plain iteration could not solve, and those
+    whose increment lies outside the range the solvers accept from the
+    network, are left out."""
     torch = _torch()
     t0 = time.time()
     feats, targets, iters = make_pairs(n_pairs, seed)
-    n_val = n_pairs // 32
-    n_tr = n_pairs - n_val
+    keep = (iters > 0) & (targets >= Y_MIN) & (targets <= Y_MAX)
+    kept = int(keep.sum().item())
+    feats, targets = feats[keep].contiguous(), targets[keep].contiguous()
+    n_val = kept // 32
+    n_tr = kept - n_val
     fv, tv = feats[n_tr:], targets[n_tr:]
     w = torch.as_tensor(init_weights(seed, float(targets[:n_tr].mean().item()))).cuda()
     m = torch.zeros_like(w)
@@ -146,7 +158,10 @@ def train(n_pairs=1 << 21, epochs=12, batch=8192, lr=2e-3, seed=7, log=print):
                      torch.sqrt(torch.mean(tv ** 2))).item())
     it = iters.cpu().numpy()
     meta = {"version": FORMAT_VERSION, "target": "y = (theta2 - theta1) / (50 K ln(p1/p2))",
-            "pairs": n_pairs, "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
+            "pairs": n_pairs, "pairs_kept": kept,
+            "pair_box": "four adiabats, p 100..1050 hPa, T -80..40 degC (saturation mixing "
+                        "ratio <= 40 g/kg), reversible condensate 0..10 g/kg, dp 50..2000 Pa",
+            "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
             "train_rms_y": curve, "val_rms_y_bf16": val_rms, "val_rel_rms_bf16": val_rel,
             "plain_iterations_mean": float(np.abs(it).mean()),
             "plain_gave_up": int((it < 0).sum()), "seconds": time.time() - t0}
@@ -203,7 +218,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m xcape_gb300.guess")
     sub = ap.add_subparsers(dest="cmd", required=True)
     tr = sub.add_parser("train")
-    tr.add_argument("--pairs", type=int, default=1 << 21)
+    tr.add_argument("--pairs", type=int, default=10_000_000)
     tr.add_argument("--epochs", type=int, default=12)
     tr.add_argument("--out", default=DEFAULT_PATH)
     args = ap.parse_args(argv)
