@@ -64,7 +64,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--guess", default="learned",
-                    choices=["plain", "extrapolated", "learned", "secant", "learned-every"])
+                    choices=["plain", "extrapolated", "learned", "secant", "learned-every",
+                             "learned-warp"])
     ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve", "adiabats", "cape_srh"])
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the request trace of --workload serve")
@@ -478,10 +479,11 @@ def run_ours(args):
     L = _lib.lib()
     guess = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
              "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT,
-             "learned-every": _lib.XC_GUESS_LEARNED_EVERY}[args.guess]
-    if guess in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY):
-        from xcape_gb300 import guess as guess_net
-        guess_net.ensure_loaded()
+             "learned-every": _lib.XC_GUESS_LEARNED_EVERY,
+             "learned-warp": _lib.XC_GUESS_LEARNED_WARP}[args.guess]
+    # the network serves the headline and the lockstep variant timed beside it
+    from xcape_gb300 import guess as guess_net
+    guess_net.ensure_loaded()
 
     n_total = GRID_SHAPE[0] * GRID_SHAPE[1]
     lo, hi = shard(n_total, world, rank)
@@ -569,10 +571,26 @@ def run_ours(args):
     sb_ms = {args.guess: time_source(1, scratch)}
     if compare:
         sb_ms["plain"] = time_source(1, scratch, _lib.XC_GUESS_PLAIN)
+    # the learned solver against the method without the network
+    # (extrapolated), and the network evaluated by each warp at every
+    # saturated sub-step on the tensor cores (learned-warp): the same launches
+    variant_ms, variant_work = {}, {}
+    for vname, vcode in (("extrapolated", _lib.XC_GUESS_EXTRAPOLATED),
+                         ("learned-warp", _lib.XC_GUESS_LEARNED_WARP)):
+        if vcode == guess:
+            continue
+        launch(SOURCES[0][1], scratch, g=vcode)
+        variant_ms[vname] = {src: time_source(code, scratch, vcode) for src, code in SOURCES}
+        cnt.zero_()
+        launch(SOURCES[0][1], scratch, cnt.data_ptr(), g=vcode)
+        torch.cuda.synchronize()
+        variant_work[vname] = [int(x) for x in cnt.cpu()]
     # every rank times its own shard: the job's time is the slowest rank's
     per_src_ms = {k: max_over_ranks(dist, v, dev) for k, v in per_src_ms.items()}
     plain_ms = {k: max_over_ranks(dist, v, dev) for k, v in plain_ms.items()}
     sb_ms = {k: max_over_ranks(dist, v, dev) for k, v in sb_ms.items()}
+    variant_ms = {k: {s_: max_over_ranks(dist, v, dev) for s_, v in d.items()}
+                  for k, d in variant_ms.items()}
 
     # end to end through the public API from pinned host memory
     import xcape_gb300 as X
@@ -660,6 +678,18 @@ def run_ours(args):
                       "surface_based_speedup": sb_ms["plain"] / sb_ms[args.guess]}
                      if compare else {"surface_based_ms": sb_ms}),
         "work": {k: {"substeps": v[0], "iterations": v[1]} for k, v in work.items()},
+        "vs_extrapolated": {
+            "per_source_ms": {args.guess: per_src_ms, **variant_ms},
+            "speedup_over_extrapolated": {
+                k: sum(variant_ms["extrapolated"].values()) / sum(v.values())
+                for k, v in {args.guess: per_src_ms, **variant_ms}.items()}
+            if "extrapolated" in variant_ms else None,
+            "iterations_per_substep_most_unstable": {
+                args.guess: work[SOURCES[0][0]][1] / max(1, work[SOURCES[0][0]][0]),
+                **{k: v[1] / max(1, v[0]) for k, v in variant_work.items()}},
+            "note": "extrapolated: the same Newton/secant solver without the network; "
+                    "learned-warp: the network evaluated by every warp at every saturated "
+                    "sub-step, in lockstep, on the tensor cores"},
         "e2e": {"value": cols_all / e2e_dt, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "api": "xcape_gb300.calc_cape_sources(numpy, pinned), both sources in one call"},

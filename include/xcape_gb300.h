@@ -77,6 +77,11 @@ extern "C" {
 #define XC_GUESS_SECANT 3       /* first guess th1 (the reference's), secant steps */
 #define XC_GUESS_LEARNED_EVERY 4 /* the network's guess on every sub-step that starts
                                     saturated, th1 on the others; secant steps */
+#define XC_GUESS_LEARNED_WARP 5 /* the network's guess on every sub-step that starts
+                                   saturated, the extrapolated one on the others;
+                                   Newton then secant steps; each warp evaluates the
+                                   network for its 32 columns in lockstep at every
+                                   sub-step on the tensor cores */
 
 /* Flag OR'ed into `guess` (xc_loopcape_ex, xc_loopcape_ex_host,
  * xc_loopcape_multi_host, xc_loopcape_ex_noalloc): after the FP32 lift, the

@@ -23,6 +23,7 @@ XC_GUESS_LEARNED = 1
 XC_GUESS_EXTRAPOLATED = 2
 XC_GUESS_SECANT = 3
 XC_GUESS_LEARNED_EVERY = 4
+XC_GUESS_LEARNED_WARP = 5
 XC_GUESS_NPARAM = 4481
 XC_MAX_LEVELS = 4096
 XC_NOALLOC_MAX_COLUMNS = 1048576

@@ -47,7 +47,7 @@ _VERTICAL = {"sigma": 1, "model": 1, "pressure": 2}
 _OUTPUT = {"srh": 1, "all": 2}
 _GUESS = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED,
           "extrapolated": _lib.XC_GUESS_EXTRAPOLATED, "secant": _lib.XC_GUESS_SECANT,
-          "learned-every": _lib.XC_GUESS_LEARNED_EVERY}
+          "learned-every": _lib.XC_GUESS_LEARNED_EVERY, "learned-warp": _lib.XC_GUESS_LEARNED_WARP}
 
 
 def _is_torch(a):
@@ -267,7 +267,7 @@ def _calc_cape_numpy(*args, source="surface", ml_depth=500.0, adiabat="pseudo-li
     if method != "cuda":
         raise ValueError("invalid method")
 
-    if gs in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY):
+    if gs in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY, _lib.XC_GUESS_LEARNED_WARP):
         from . import guess as _guess
         _guess.ensure_loaded()
     b = _Batch([t, td], [ps, ts, tds], p, grid)
@@ -317,7 +317,7 @@ def calc_cape_sources(p, t, td, ps, ts, tds, sources=("most-unstable", "mixed-la
     vl = _option(_VERTICAL, vertical_lev, "vertical_lev")
     gs = _option(_GUESS, guess, "guess")
     grid, original_shape = _cape_grid(p, t, td, ps, ts, tds, vl)
-    if gs in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY):
+    if gs in (_lib.XC_GUESS_LEARNED, _lib.XC_GUESS_LEARNED_EVERY, _lib.XC_GUESS_LEARNED_WARP):
         from . import guess as _guess
         _guess.ensure_loaded()
     b = _Batch([t, td], [ps, ts, tds], p, grid)

@@ -159,6 +159,13 @@ constexpr int SOLVE_ACCEL = 1;
 constexpr int SOLVE_LEARNED = 2;
 constexpr int SOLVE_SECANT = 3;
 constexpr int SOLVE_LEARNED_ALL = 4;
+// SOLVE_LEARNED_WARP: SOLVE_ACCEL's Newton and secant steps, with the guess
+// network's increment as the first guess of every sub-step that starts
+// saturated (the extrapolated guess on the others); the warp evaluates the
+// network for its 32 lanes in lockstep at every sub-step, on the tensor cores
+// (ascend_col_warp, cape_learned.cuh), and hands each lane its increment in
+// SolverState::net_dth.
+constexpr int SOLVE_LEARNED_WARP = 5;
 
 struct SolverState {
   // (SOLVE_ACCEL, SOLVE_LEARNED) (th2 - th1) / dp of the previous sub-step;
@@ -170,6 +177,7 @@ struct SolverState {
   float lcl_y = NAN;
   float lnp = 0.0f;         // ln of the parcel pressure (accelerated modes)
   const float *guess_w = nullptr;  // packed guess network (guess_packed_value), SOLVE_LEARNED*
+  float net_dth = NAN;      // (SOLVE_LEARNED_WARP) this sub-step's network increment, or NaN
 };
 
 // The guess network's output y at the lifting condensation level of a parcel
@@ -380,12 +388,16 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
   }
   R thlast = th1;
   R x_prev = XC_LIT(R, 0.0), f_prev = XC_LIT(R, 0.0);
-  constexpr bool EXTRAP = SOLVER == SOLVE_ACCEL || SOLVER == SOLVE_LEARNED;
+  constexpr bool EXTRAP =
+      SOLVER == SOLVE_ACCEL || SOLVER == SOLVE_LEARNED || SOLVER == SOLVE_LEARNED_WARP;
   if constexpr (EXTRAP) {
     // the first evaluation, at the extrapolated guess, also gives the map's
     // slope: a Newton step from it, then secant steps through the last two
     // evaluations (Newton again where x repeated)
     thlast = th1 + ss.rate * dp;
+    if constexpr (SOLVER == SOLVE_LEARNED_WARP) {
+      if (ss.net_dth == ss.net_dth) thlast = th1 + ss.net_dth;
+    }
     float dex = 0.0f;
     for (int i = 1;; ++i) {
       th2 = accel_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, i == 1, t2, qv2,
@@ -450,7 +462,8 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
       ss.lcl_y = NAN;
     }
   }
-  if constexpr (SOLVER == SOLVE_LEARNED_ALL) ss.saturated = ql2 + qi2 > 0.0f;
+  if constexpr (SOLVER == SOLVE_LEARNED_ALL || SOLVER == SOLVE_LEARNED_WARP)
+    ss.saturated = ql2 + qi2 > 0.0f;
   if (PSEUDO) {  // :487-491
     qt = qv2;
     ql2 = XC_LIT(R, 0.0);

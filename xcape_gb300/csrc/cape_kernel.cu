@@ -85,6 +85,29 @@ __global__ void __launch_bounds__(LEARNED_THREADS, 7) cape_learned_kernel(CapeAr
   }
 }
 
+// SOLVE_LEARNED_WARP (cape_learned.cuh): the network evaluated by each warp
+// at every sub-step, in lockstep.
+template <typename T, int GRID, bool ICE, bool PSEUDO>
+__global__ void __launch_bounds__(LEARNED_THREADS) cape_learned_warp_kernel(CapeArgs a) {
+  __shared__ WarpNetSmem net;
+  copy_warp_net(net, &g_warp_net);
+  __syncthreads();
+  int nsub, niter;
+  learned_warp_column<T, GRID, ICE, PSEUDO>(a, net, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                                            nsub, niter);
+  if (a.counters) {
+    long long sb = nsub, it = niter;
+    for (int o = 16; o > 0; o >>= 1) {
+      sb += __shfl_down_sync(0xffffffffu, sb, o);
+      it += __shfl_down_sync(0xffffffffu, it, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd((unsigned long long *)&a.counters[0], (unsigned long long)sb);
+      atomicAdd((unsigned long long *)&a.counters[1], (unsigned long long)it);
+    }
+  }
+}
+
 template <typename T>
 __global__ void pres_lev_pos_kernel(const T *p1d, const T *ps, int nk, long long n2, int *start) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -246,9 +269,21 @@ static void launch_learned(const CapeArgs &a, cudaStream_t s) {
   else cape_learned_kernel<T, GRID, false, false><<<blocks, threads, 0, s>>>(a);
 }
 
+template <typename T, int GRID>
+static void launch_learned_warp(const CapeArgs &a, cudaStream_t s) {
+  const int threads = LEARNED_THREADS;
+  const unsigned blocks = (unsigned)((a.n2 + threads - 1) / threads);
+  const bool ice = a.adiabat >= 3;
+  const bool pseudo = (a.adiabat == 1 || a.adiabat == 3);
+  if (ice && pseudo) cape_learned_warp_kernel<T, GRID, true, true><<<blocks, threads, 0, s>>>(a);
+  else if (ice) cape_learned_warp_kernel<T, GRID, true, false><<<blocks, threads, 0, s>>>(a);
+  else if (pseudo) cape_learned_warp_kernel<T, GRID, false, true><<<blocks, threads, 0, s>>>(a);
+  else cape_learned_warp_kernel<T, GRID, false, false><<<blocks, threads, 0, s>>>(a);
+}
+
 // guess codes (include/xcape_gb300.h): 0 plain, 1 learned, 2 extrapolated,
 // 3 plain first guess with secant steps, 4 the network on every saturated
-// sub-step.
+// sub-step (per thread), 5 the same per warp in lockstep on the tensor cores.
 template <typename T, int GRID>
 static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
   const int threads = 128;
@@ -259,6 +294,7 @@ static cudaError_t launch_cape_t(const CapeArgs &a, cudaStream_t s) {
     case 1: launch_learned<T, GRID>(a, s); break;
     case 2: launch_cape_s<T, GRID, SOLVE_ACCEL>(a, blocks, threads, s); break;
     case 3: launch_cape_s<T, GRID, SOLVE_SECANT>(a, blocks, threads, s); break;
+    case 5: launch_learned_warp<T, GRID>(a, s); break;
     default: launch_cape_s<T, GRID, SOLVE_LEARNED_ALL>(a, blocks, threads, s); break;
   }
   return cudaGetLastError();

@@ -282,3 +282,223 @@ __device__ __forceinline__ void learned_column(const CapeArgs &a, const WarpNetS
 }
 
 }  // namespace xc
+
+namespace xc {
+
+// The ascent (:355-559) of SOLVE_LEARNED_WARP, in warp lockstep: every lane
+// walks its own column, but one sub-step at a time for the whole warp, so
+// that before each sub-step the warp evaluates the guess network for the 32
+// lanes' states at once on the tensor cores (warp_guess_eval).  A lane
+// between levels finishes the level it has sub-stepped through (buoyancy,
+// areas) and prepares the next one (advance) before the next evaluation;
+// lanes that are done, or whose parcel does not start the sub-step
+// saturated, take part in the evaluation with zero inputs and discard the
+// output.  The map, the stopping test and the result are those of every
+// accelerated solver; only the first guess of a saturated sub-step comes
+// from the network: theta1 + 50 K y ln(p1/p2), with y the network's output
+// at (p2, theta-e of the saturated parcel, total water).
+// All 32 lanes of the warp must call it; `live` is false for lanes without
+// an ascent (past n2, ts <= 0, bad start, no ascent from the source).
+template <bool ICE, bool PSEUDO, typename T, int GRID>
+__device__ CapeResult ascend_col_warp(const ColumnReader<T, GRID> &col, int ncl, float pinc,
+                                      int source, const SourceSel &sel, const WarpNetSmem &net,
+                                      bool live) {
+  CapeResult r;
+  r.mulvl = sel.mulvl;
+  r.z_out = -999999.f;
+  r.cape = 0.0f;
+  r.cin = 0.0f;
+  r.status = 0;
+  r.nsub = 0;
+  r.niter = 0;
+  const int kmax = sel.kmax;
+  const float avgth = sel.avgth, avgqv = sel.avgqv;
+  Env prev, cur;
+  prev.p = prev.t = prev.td = prev.pi = prev.q = prev.th = prev.thv = 0.0f;
+  cur = prev;
+  float z = 0.0f, dz = 0.0f, dp = 0.0f, b1 = 0.0f;
+  float th2 = 0.f, p2 = 0.f, t2 = 0.f, qv2 = 0.f, b2 = 0.f, ql2 = 0.f, qi2 = 0.f, qt = 0.f;
+  float narea = 0.0f;
+  SolverState ss;
+  Acc<true> cape_acc, cin_acc;
+  int k = 1, n = 0, nloop = 0;
+  bool done = !live, aborted = false;
+  auto init_parcel = [&](const Env &e) {
+    if (source == 3) {
+      th2 = avgth;
+      qv2 = avgqv;
+      const float thv2 = th2 * (1.0f + REPS * qv2) / (1.0f + qv2);
+      p2 = e.p;
+      t2 = th2 * e.pi;
+      b2 = G * (thv2 - e.thv) / e.thv;
+    } else {
+      th2 = e.th;
+      p2 = e.p;
+      t2 = e.t;
+      qv2 = e.q;
+      b2 = 0.0f;
+    }
+    ql2 = 0.0f;
+    qi2 = 0.0f;
+    qt = qv2;
+    ss.lnp = fast_log(p2);
+  };
+  // Finishes the level whose sub-steps are done and walks up to the next
+  // level that needs sub-steps (or to the end of the ascent).
+  auto advance = [&]() {
+    while (!done) {
+      if (n < nloop) return;
+      if (nloop > 0) {
+        // :501-557, as ascend_col
+        const float thv2 = fast_div(th2 * (1.0f + REPS * qv2), 1.0f + qv2 + ql2 + qi2);
+        b2 = fast_div(G * (thv2 - cur.thv), cur.thv);
+        float parea;
+        if ((b2 >= 0.0f) && (b1 < 0.0f)) {
+          const float frac = b2 / (b2 - b1);
+          parea = 0.5f * b2 * dz * frac;
+          narea = narea - 0.5f * b1 * dz * (1.0f - frac);
+          cin_acc.add(narea);
+          narea = 0.0f;
+        } else if ((b2 < 0.0f) && (b1 > 0.0f)) {
+          const float frac = b1 / (b1 - b2);
+          parea = 0.5f * b1 * dz * frac;
+          narea = -0.5f * b2 * dz * (1.0f - frac);
+        } else if (b2 < 0.0f) {
+          parea = 0.0f;
+          narea = narea - 0.5f * dz * (b1 + b2);
+        } else {
+          parea = 0.5f * dz * (b1 + b2);
+          narea = 0.0f;
+        }
+        cape_acc.add(fmax_f(0.0f, parea));
+        r.z_out = z;
+        nloop = 0;
+        if ((cur.p <= 10000.0f) && (b2 < 0.0f)) {
+          done = true;
+          return;
+        }
+        prev = cur;
+      }
+      if (++k > ncl) {
+        done = true;
+        return;
+      }
+      cur = col.template env_above<true>(k);
+      dz = -CPDG * 0.5f * (cur.thv + prev.thv) * (cur.pi - prev.pi);
+      z = z + dz;
+      if (k <= kmax) {
+        if (k == kmax) init_parcel(cur);
+        prev = cur;
+        continue;
+      }
+      b1 = b2;
+      dp = prev.p - cur.p;
+      if (dp < pinc) {
+        nloop = 1;
+      } else {
+        const float f = dp / pinc;
+        if (!(f < (float)MAX_SUBSTEPS)) {
+          r.status |= COL_TOOMANYSTEPS;
+          done = aborted = true;
+          return;
+        }
+        nloop = 1 + (int)f;
+        dp = dp / (float)nloop;
+      }
+      if (r.nsub + nloop > MAX_SUBSTEPS) {
+        r.status |= COL_TOOMANYSTEPS;
+        done = aborted = true;
+        return;
+      }
+      n = 0;
+    }
+  };
+  if (live) {
+    prev = col.template env<true>(1);
+    if (kmax == 1) init_parcel(prev);
+  }
+  advance();
+  while (__any_sync(0xffffffffu, !done)) {
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, lpn = 0.0f;
+    const bool use_net = !done && ss.saturated;
+    if (use_net) {
+      const float pn = p2 - dp;
+      lpn = fast_log(pn) - ss.lnp;
+      guess_features(pn, getthe_fast(p2, t2, t2, qv2), qt, f0, f1, f2);
+    }
+    __syncwarp();
+    const float y = warp_guess_eval(net, f0, f1, f2);
+    if (!done) {
+      ss.net_dth = (use_net && y >= GUESS_Y_MIN && y <= GUESS_Y_MAX) ? -GUESS_SLOPE_SCALE * y * lpn
+                                                                    : NAN;
+      ++r.nsub;
+      ++n;
+      if (!substep<ICE, PSEUDO, SOLVE_LEARNED_WARP>(dp, p2, t2, th2, qv2, ql2, qi2, qt, r.niter,
+                                                    ss)) {
+        r.status |= COL_NOCONV;  // :471-473
+        done = aborted = true;
+      } else {
+        advance();
+      }
+    }
+  }
+  if (!aborted) {
+    r.cape = cape_acc.s;
+    r.cin = cin_acc.s;
+  }
+  return r;
+}
+
+// Column perm[t] (t when unordered) of SOLVE_LEARNED_WARP for thread t of a
+// LEARNED_THREADS-thread block whose shared memory holds the network; every
+// thread of the block calls it, also past n2.
+template <typename T, int GRID, bool ICE, bool PSEUDO>
+__device__ __forceinline__ void learned_warp_column(const CapeArgs &a, const WarpNetSmem &net,
+                                                    long long t, int &nsub, int &niter) {
+  const bool active = t < a.n2;
+  const long long i = active ? (a.perm ? (long long)__ldg(a.perm + t) : t) : 0;
+  const long long stride = a.ld > 0 ? a.ld : a.nk;
+  int start = 1, status = 0;
+  SourceSel sel;
+  sel.kmax = 1;
+  sel.mulvl = 0;
+  sel.avgth = sel.avgqv = 0.0f;
+  sel.ascend = false;
+  ColumnReader<T, GRID> col;
+  col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, 0, 3);
+  col.ps = col.ts = col.tds = 0.0f;
+  bool gate = false, live = false;
+  if (active) {
+    const float ts = ldf((const T *)a.ts + i);
+    if (GRID != 1)
+      start = a.start ? __ldg(a.start + i)
+                      : pres_lev_pos_col<T>((const T *)a.p, __ldg((const T *)a.ps + i), a.nk);
+    gate = ts > 0.0f;  // CAPE_CODE_model_lev.f90:77
+    if (gate) {
+      if (start < 1 || start > a.nk) {
+        status = COL_BADSTART;
+      } else {
+        col.set((const T *)a.p, (const T *)a.t, (const T *)a.td, i * stride, start);
+        col.ps = ldf((const T *)a.ps + i);
+        col.ts = ts;
+        col.tds = ldf((const T *)a.tds + i);
+        sel = select_source<true>(col, a.nk - start + 2, a.source, a.ml_depth);
+        live = sel.ascend;
+      }
+    }
+  }
+  CapeResult r = ascend_col_warp<ICE, PSEUDO, T, GRID>(col, a.nk - start + 2, a.pinc, a.source,
+                                                       sel, net, live);
+  nsub = r.nsub;
+  niter = r.niter;
+  if (active) {
+    const bool ran = gate && status == 0;
+    a.cape[i] = ran ? r.cape : 0.0f;
+    a.cin[i] = ran ? r.cin : 0.0f;
+    a.mulvl[i] = ran ? r.mulvl : 0;
+    a.z_out[i] = ran ? r.z_out : 0.0f;
+    if (a.status) a.status[i] = ran ? r.status : status;
+  }
+}
+
+}  // namespace xc

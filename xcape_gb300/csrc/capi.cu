@@ -227,11 +227,12 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
   const bool retry = (guess & XC_RETRY_FP64) != 0;
   guess &= ~XC_RETRY_FP64;
-  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_EVERY)
+  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_WARP)
     return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
   if (retry && !status) return fail(XC_ERR_INVALID, "XC_RETRY_FP64 needs the status array");
   const float *guess_w = nullptr;
-  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY) {
+  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY ||
+      guess == XC_GUESS_LEARNED_WARP) {
     rc = guess_weights(&guess_w);
     if (rc) return rc;
   }
@@ -397,10 +398,11 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
   if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
   const bool retry = (guess & XC_RETRY_FP64) != 0;
   guess &= ~XC_RETRY_FP64;
-  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_EVERY)
+  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_WARP)
     return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
   const float *guess_w = nullptr;
-  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY) {
+  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY ||
+      guess == XC_GUESS_LEARNED_WARP) {
     rc = guess_weights(&guess_w);
     if (rc) return rc;
   }
