@@ -66,7 +66,8 @@ def parse():
     ap.add_argument("--guess", default="learned",
                     choices=["plain", "extrapolated", "learned", "secant", "learned-every",
                              "learned-warp"])
-    ap.add_argument("--workload", default="cape", choices=["cape", "srh", "serve", "adiabats", "cape_srh"])
+    ap.add_argument("--workload", default="cape",
+                    choices=["cape", "srh", "serve", "adiabats", "cape_srh", "dask"])
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the request trace of --workload serve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -877,98 +878,85 @@ def serve_trace(seconds, seed=4):
 
 
 def run_serve(args):
-    """--workload serve: calc_cape requests arriving at 200/s, batched on the
-    device (xcape_gb300.batch: one graph launch per batch), for the learned
-    and the plain solver on the same trace."""
+    """--workload serve: calc_cape requests arriving at 200/s with their
+    inputs in host memory, served by xcape_gb300.serve.CapeServer: admitted
+    by device-memory budget, copied to the device and batched (one graph
+    launch per batch), with batch k + 1 prepared and launched while batch k
+    runs; for the learned and the plain solver on the same trace."""
     import torch
     from xcape_gb300 import synthetic as S
-    from xcape_gb300.batch import CapeBatch
+    from xcape_gb300.serve import CapeServer, Request
     world, rank, local = dist_env()
     if rank != 0:
         return 0
     torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
     nl = 137
     reps = SERVE_POOL // SERVE_BASE
 
-    def pool(arrs):
-        # tile SERVE_BASE synthetic columns to SERVE_POOL on the device
-        return [torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev).repeat(
-            (reps, 1) if a.ndim == 2 else (reps,)) for a in arrs]
+    def pinned_pool(a):
+        # SERVE_BASE synthetic columns tiled to SERVE_POOL, in pinned host
+        # memory: the buffers a service's clients write their requests into
+        a = np.ascontiguousarray(a, np.float32)
+        shape = (SERVE_POOL, nl) if a.ndim == 2 else (SERVE_POOL,)
+        out = torch.empty(shape, dtype=torch.float32).pin_memory().numpy()
+        out[...] = np.tile(a, (reps, 1) if a.ndim == 2 else reps)
+        return out
     sig = S.sigma_c0(shape=(SERVE_BASE,), nlev=nl, seed=31, dtype=np.float32)
-    sig_d = pool([np.reshape(a, (SERVE_BASE, nl)) if np.size(a) == SERVE_BASE * nl
-                  else np.ravel(a) for a in sig])
+    sig_h = [pinned_pool(a) for a in sig]
     prs = S.pressure_c1(shape=(SERVE_BASE,), nlev=nl, seed=32)
-    plev = torch.from_numpy(np.ascontiguousarray(prs[0], np.float32)).to(dev)
-    prs_d = [plev] + pool([np.reshape(a, (SERVE_BASE, nl)) if np.size(a) == SERVE_BASE * nl
-                           else np.ravel(a) for a in prs[1:]])
+    plev = np.ascontiguousarray(prs[0], np.float32)
+    prs_h = [plev] + [pinned_pool(a) for a in prs[1:]]
     trace = serve_trace(args.serve_seconds)
-    max_cols = 8 << 20
 
-    def descriptor(b, r):
+    def request(r):
         c0, n2, nk = r["c0"], r["n2"], r["nk"]
-        if r["grid"] == "sigma":
-            p, t, td, ps, ts, tds = sig_d
-            P = p[c0:c0 + n2, :nk]
-        else:
-            p, t, td, ps, ts, tds = prs_d
-            P = p[:nk]
-        return b.request(P, t[c0:c0 + n2, :nk], td[c0:c0 + n2, :nk], ps[c0:c0 + n2],
-                         ts[c0:c0 + n2], tds[c0:c0 + n2], source=r["source"],
-                         adiabat=r["adiabat"], vertical_lev=r["grid"])
+        src = sig_h if r["grid"] == "sigma" else prs_h
+        p = src[0][c0:c0 + n2] if r["grid"] == "sigma" else src[0]
+        return Request(p, *[x[c0:c0 + n2] for x in src[1:]], source=r["source"],
+                       adiabat=r["adiabat"], vertical_lev=r["grid"], nk=nk, tag=r)
 
     def serve(guess):
-        stream = torch.cuda.current_stream(dev)
-        host_out = torch.empty(2 * max_cols, dtype=torch.float32).pin_memory()
-        with CapeBatch(max_requests=4096, max_columns=max_cols, guess=guess) as b:
+        with CapeServer(memory_budget=8 << 30, guess=guess, staging_bytes=512 << 20) as srv:
             # warm-up: one batch of the first requests
-            b.run([descriptor(b, r) for r in trace[:8]])
+            srv.finish(srv.launch(srv.admit([request(r) for r in trace[:8]])))
             torch.cuda.synchronize()
-            lat, batches, busy, cols, nxt = [], [], 0.0, 0, 0
-            slowest = (0.0, 0, 0)  # the longest batch: seconds, requests, columns
+            lat, batches, cols, nxt = [], [], 0, 0
+            pending, inflight = [], None
+            busy, t_busy = 0.0, None
             t0 = time.perf_counter()
-            while nxt < len(trace):
+            while nxt < len(trace) or pending or inflight is not None:
                 now = time.perf_counter() - t0
-                if trace[nxt]["arrival"] > now:
-                    time.sleep(trace[nxt]["arrival"] - now)
-                    continue
-                # admit what has arrived, up to the executor's column capacity
-                take, used = [], 0
                 while nxt < len(trace) and trace[nxt]["arrival"] <= now:
-                    need = (trace[nxt]["n2"] + 31) // 32 * 32
-                    if take and used + need > max_cols:
-                        break
-                    take.append(trace[nxt])
-                    used += need
+                    pending.append(request(trace[nxt]))
                     nxt += 1
-                tb = time.perf_counter()
-                reqs = [descriptor(b, r) for r in take]
-                b.run(reqs)
-                off = 0
-                for q in reqs:  # results back to the host, on the same stream
-                    n = q.cape.numel()
-                    host_out[off:off + n].copy_(q.cape, non_blocking=True)
-                    host_out[max_cols + off:max_cols + off + n].copy_(q.cin, non_blocking=True)
-                    off += n
-                stream.synchronize()
-                done = time.perf_counter() - t0
-                dt = time.perf_counter() - tb
-                busy += dt
-                if dt > slowest[0]:
-                    slowest = (dt, len(take), sum(r["n2"] for r in take))
-                batches.append(len(take))
-                cols += sum(r["n2"] for r in take)
-                lat += [done - r["arrival"] for r in take]
+                if not pending and inflight is None:
+                    time.sleep(max(0.0, trace[nxt]["arrival"] - now))
+                    continue
+                batch = None
+                if pending:
+                    take = srv.admit(pending)
+                    if t_busy is None:
+                        t_busy = time.perf_counter()
+                    batch = srv.launch(take)
+                    batches.append(len(take))
+                if inflight is not None:
+                    results = srv.finish(inflight)
+                    done = time.perf_counter() - t0
+                    for q, _ in results:
+                        lat.append(done - q.tag["arrival"])
+                        cols += q.n2
+                    if batch is None:  # the device goes idle
+                        busy += time.perf_counter() - t_busy
+                        t_busy = None
+                inflight = batch
             wall = time.perf_counter() - t0
         lat_ms = np.array(lat) * 1e3
         return {"requests": len(lat), "columns": cols, "wall_s": wall,
                 "columns_per_s": cols / wall, "busy_fraction": busy / wall,
-                "columns_per_busy_s": cols / busy,
+                "columns_per_busy_s": cols / busy if busy else None,
                 "p50_ms": float(np.percentile(lat_ms, 50)),
                 "p99_ms": float(np.percentile(lat_ms, 99)),
                 "max_ms": float(lat_ms.max()), "batches": len(batches),
-                "slowest_batch": {"ms": slowest[0] * 1e3, "requests": slowest[1],
-                                  "columns": slowest[2]},
                 "mean_requests_per_batch": float(np.mean(batches)),
                 "graph_launches": len(batches)}
 
@@ -978,12 +966,13 @@ def run_serve(args):
                        "requests": len(trace), "columns": "log-uniform 1e3..1e6",
                        "levels": "uniform 20..137", "grids": "sigma, pressure (ragged)",
                        "sources": "surface, most-unstable, mixed-layer",
-                       "adiabats": "all four", "inputs": "device-resident pools",
-                       "results": "cape, cin copied to pinned host memory"},
+                       "adiabats": "all four",
+                       "inputs": "host memory (pinned client buffers, rows of 137 values), "
+                                 "copied to the device inside the loop",
+                       "admission": "device-memory budget 8 GiB (two 4 GiB arenas)",
+                       "results": "cape, cin, mulvl, z_out back to host memory"},
             "learned": res["learned"], "plain": res["plain"],
-            "p99_speedup": res["plain"]["p99_ms"] / res["learned"]["p99_ms"],
-            "busy_throughput_speedup": res["learned"]["columns_per_busy_s"] /
-            res["plain"]["columns_per_busy_s"]}
+            "p99_speedup": res["plain"]["p99_ms"] / res["learned"]["p99_ms"]}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -1091,6 +1080,62 @@ def _adiabat_accuracy(base, cape, code, n=4096):
             "frac_dcape_le_1": float(np.mean(dc <= 1.0))}
 
 
+DASK_METRIC = "calc_cape columns/s on numpy chunks of the 1M x 37 grid (dask-style, threads)"
+
+
+def run_dask(args):
+    """calc_cape on the 721 x 1440 x 37 pressure-level grid split into 16
+    chunks of columns, as dask's apply_gufunc hands them over (one numpy call
+    per chunk, pageable host memory), computed one after another and by 4
+    threads at once as dask's threaded scheduler does; beside one call over
+    the whole grid.  Each concurrent call takes its own host context
+    (streams, pinned staging, device workspace), so chunk k + 1's copies
+    overlap chunk k's lift.  most-unstable parcels, learned guess."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    import xcape_gb300 as X
+    from xcape_gb300 import guess as guess_net
+    torch.cuda.set_device(0)
+    guess_net.ensure_loaded()
+    plev, t, td, ps, ts, tds = cape_inputs(0, GRID_SHAPE[0] * GRID_SHAPE[1])
+    n2 = ps.shape[0]
+    nch = 16
+    bounds = np.linspace(0, n2, nch + 1).astype(int)
+    chunks = [(plev, t[lo:hi], td[lo:hi], ps[lo:hi], ts[lo:hi], tds[lo:hi])
+              for lo, hi in zip(bounds[:-1], bounds[1:])]
+    kw = dict(source="most-unstable", vertical_lev="pressure", guess=args.guess)
+
+    def one(c):
+        return X.calc_cape(*c, **kw)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 2)):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / args.steps
+
+    whole = timed(lambda: one((plev, t, td, ps, ts, tds)))
+    seq = timed(lambda: [one(c) for c in chunks])
+    with ThreadPoolExecutor(4) as pool:
+        par = timed(lambda: list(pool.map(one, chunks)))
+    line = {"metric": DASK_METRIC, "value": n2 / par, "unit": "columns/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 2), "ms_per_step": par * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "calc_cape most-unstable, 721x1440 cols x 37 pressure levels, "
+                                   f"{nch} numpy chunks of columns, guess {args.guess}"},
+            "threads_4": {"columns_per_s": n2 / par, "ms": par * 1e3},
+            "sequential_chunks": {"columns_per_s": n2 / seq, "ms": seq * 1e3},
+            "one_call": {"columns_per_s": n2 / whole, "ms": whole * 1e3},
+            "overlap_gain": seq / par}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1103,6 +1148,8 @@ def main():
         return run_adiabats(args)
     if args.workload == "cape_srh":
         return run_cape_srh(args)
+    if args.workload == "dask":
+        return run_dask(args)
     return run_ours(args)
 
 

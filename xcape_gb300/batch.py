@@ -75,8 +75,10 @@ class CapeBatch:
         self._h = h
 
     def request(self, p, t, td, ps, ts, tds, source="surface", adiabat="pseudo-liquid",
-                vertical_lev="sigma", pinc=500.0, ml_depth=500.0):
-        """Describes one calc_cape call and allocates its outputs."""
+                vertical_lev="sigma", pinc=500.0, ml_depth=500.0, outputs=None):
+        """Describes one calc_cape call and allocates its outputs, or uses
+        `outputs` = [cape, cin, mulvl, z_out] (contiguous CUDA tensors of n2
+        float32, float32, int32, float32; no status output then)."""
         torch = _torch()
         if source not in _SOURCES:
             raise ValueError(f"source must be one of {sorted(_SOURCES)}")
@@ -100,17 +102,27 @@ class CapeBatch:
         for x, name in ((ps, "ps"), (ts, "ts"), (tds, "tds")):
             _check_1d(x, name, n2)
         dev = t.device
-        cape = torch.empty(n2, dtype=torch.float32, device=dev)
-        cin = torch.empty_like(cape)
-        z_out = torch.empty_like(cape)
-        mulvl = torch.empty(n2, dtype=torch.int32, device=dev)
-        status = torch.empty_like(mulvl)
+        if outputs is None:
+            cape = torch.empty(n2, dtype=torch.float32, device=dev)
+            cin = torch.empty_like(cape)
+            z_out = torch.empty_like(cape)
+            mulvl = torch.empty(n2, dtype=torch.int32, device=dev)
+            status = torch.empty_like(mulvl)
+        else:
+            cape, cin, mulvl, z_out = outputs
+            for x, name in ((cape, "cape"), (cin, "cin"), (z_out, "z_out")):
+                _check_1d(x, name, n2)
+            if not (isinstance(mulvl, torch.Tensor) and mulvl.is_cuda and
+                    mulvl.dtype == torch.int32 and mulvl.shape == (n2,) and mulvl.is_contiguous()):
+                raise TypeError("mulvl must be a contiguous int32 CUDA tensor of n2 elements")
+            status = None
         d = _lib.CapeRequest(grid=grid, nk=nk, n2=n2, ld=ld, p=p.data_ptr(), t3d=t.data_ptr(),
                              td3d=td.data_ptr(), ps=ps.data_ptr(), ts=ts.data_ptr(),
                              tds=tds.data_ptr(), pinc=float(pinc), source=_SOURCES[source],
                              ml_depth=float(ml_depth), adiabat=_ADIABATS[adiabat],
                              cape=cape.data_ptr(), cin=cin.data_ptr(), mulvl=mulvl.data_ptr(),
-                             z_out=z_out.data_ptr(), status=status.data_ptr())
+                             z_out=z_out.data_ptr(),
+                             status=status.data_ptr() if status is not None else None)
         return Request(d, (p, t, td, ps, ts, tds), cape, cin, mulvl, z_out, status)
 
     def run(self, requests, stream=None):

@@ -10,6 +10,8 @@
 #include <string.h>
 
 #include <atomic>
+#include <condition_variable>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -50,19 +52,6 @@ int check_cape_opts(float pinc, int source, float ml_depth, int adiabat) {
   return XC_OK;
 }
 
-// Device workspace of the *_host entry points: one grow-only buffer per
-// device, serialised by a mutex (a host call holds it until its outputs are
-// back, so the buffer is never shared between calls in flight).
-struct Workspace {
-  void *ptr = nullptr;
-  size_t cap = 0;
-};
-std::mutex g_ws_mu;
-std::vector<Workspace> g_ws;
-
-// Two non-blocking streams per device for the pipelined host paths (chunk
-// c + 1's copies overlap chunk c's kernels), and an event that chains them
-// to the caller's stream.  Created on first use, kept for the process.
 // Columns per chunk of the pipelined host path: at least this many, at most
 // HOST_CHUNKS chunks; the chunks' device buffers (a ring of slots) take at
 // most host_ring_bytes(), and at least two slots.
@@ -81,7 +70,28 @@ size_t host_ring_bytes() {
   return (size_t)4 << 30;
 }
 
-struct Pipeline {
+// Host calls in flight at once on one device: 4, or the environment's
+// XC_HOST_CONTEXTS (1..64).  Calls beyond that wait for a context.
+int host_contexts() {
+  const char *e = getenv("XC_HOST_CONTEXTS");
+  if (e && *e) {
+    const int v = atoi(e);
+    if (v >= 1 && v <= 64) return v;
+  }
+  return 4;
+}
+
+// Everything one host-pointer call uses on its device, owned by that call
+// while it runs: two non-blocking streams for the chunks' kernels and
+// output copies and one for their input copies (chunk c + 1's copies
+// overlap chunk c's kernels), events, pinned output staging and the device
+// workspace (grow-only).  Contexts are created on first use and kept for the
+// process; calls from several host threads -- dask's threaded scheduler
+// computing chunks at once -- each take their own context, so their copies
+// and kernels overlap on the GPU instead of queueing behind one lock.
+struct HostCtx {
+  int dev = -1;
+  bool busy = false;
   cudaStream_t s[2] = {nullptr, nullptr};  // kernels and output copies, alternating
   cudaStream_t copy = nullptr;             // input copies, in chunk order
   cudaEvent_t start = nullptr;
@@ -89,65 +99,100 @@ struct Pipeline {
   cudaEvent_t done[HOST_CHUNKS] = {};      // slot k's outputs are in its staging
   char *pinned = nullptr;                  // pinned output staging, grow-only
   size_t pinned_cap = 0;
+  void *ws = nullptr;                      // device workspace, grow-only
+  size_t ws_cap = 0;
 };
-std::vector<Pipeline> g_pipe;
+std::mutex g_ctx_mu;
+std::condition_variable g_ctx_cv;
+std::vector<std::unique_ptr<HostCtx>> g_ctx;
 
-int pipeline_get(Pipeline **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if ((int)g_pipe.size() <= dev) g_pipe.resize(dev + 1);
-  Pipeline &pl = g_pipe[dev];
-  for (int k = 0; k < 2 && e == cudaSuccess; ++k)
-    if (!pl.s[k]) e = cudaStreamCreateWithFlags(&pl.s[k], cudaStreamNonBlocking);
-  if (e == cudaSuccess && !pl.copy) e = cudaStreamCreateWithFlags(&pl.copy, cudaStreamNonBlocking);
-  for (int k = 0; k < HOST_CHUNKS && e == cudaSuccess; ++k) {
-    if (!pl.done[k]) e = cudaEventCreateWithFlags(&pl.done[k], cudaEventDisableTiming);
-    if (e == cudaSuccess && !pl.loaded[k])
-      e = cudaEventCreateWithFlags(&pl.loaded[k], cudaEventDisableTiming);
+// Takes a free context of the current device (creating one while fewer than
+// host_contexts() exist), waiting for one otherwise; releases it on scope
+// exit.
+struct HostCtxLease {
+  HostCtx *c = nullptr;
+  int acquire() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    {
+      std::unique_lock<std::mutex> lk(g_ctx_mu);
+      for (;;) {
+        int count = 0;
+        for (auto &x : g_ctx) {
+          if (x->dev != dev) continue;
+          ++count;
+          if (!x->busy) {
+            c = x.get();
+            break;
+          }
+        }
+        if (!c && count < host_contexts()) {
+          g_ctx.push_back(std::unique_ptr<HostCtx>(new HostCtx()));
+          c = g_ctx.back().get();
+          c->dev = dev;
+        }
+        if (c) {
+          c->busy = true;
+          break;
+        }
+        g_ctx_cv.wait(lk);
+      }
+    }
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+      if (!c->s[k]) e = cudaStreamCreateWithFlags(&c->s[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !c->copy) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    for (int k = 0; k < HOST_CHUNKS && e == cudaSuccess; ++k) {
+      if (!c->done[k]) e = cudaEventCreateWithFlags(&c->done[k], cudaEventDisableTiming);
+      if (e == cudaSuccess && !c->loaded[k])
+        e = cudaEventCreateWithFlags(&c->loaded[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess && !c->start)
+      e = cudaEventCreateWithFlags(&c->start, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "creating the host-path streams");
+    return XC_OK;
   }
-  if (e == cudaSuccess && !pl.start) e = cudaEventCreateWithFlags(&pl.start, cudaEventDisableTiming);
-  if (e != cudaSuccess) return cuda_fail(e, "creating the host-path streams");
-  *out = &pl;
-  return XC_OK;
-}
+  ~HostCtxLease() {
+    if (!c) return;
+    {
+      std::lock_guard<std::mutex> lk(g_ctx_mu);
+      c->busy = false;
+    }
+    g_ctx_cv.notify_all();
+  }
+};
 
-int pipeline_pinned(Pipeline *pl, size_t bytes) {
-  if (pl->pinned_cap >= bytes) return XC_OK;
-  if (pl->pinned) cudaFreeHost(pl->pinned);
-  pl->pinned = nullptr;
-  pl->pinned_cap = 0;
-  const cudaError_t e = xc::host_malloc((void **)&pl->pinned, bytes);
+int ctx_pinned(HostCtx *c, size_t bytes) {
+  if (c->pinned_cap >= bytes) return XC_OK;
+  if (c->pinned) cudaFreeHost(c->pinned);
+  c->pinned = nullptr;
+  c->pinned_cap = 0;
+  const cudaError_t e = xc::host_malloc((void **)&c->pinned, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(XC_ERR_NOMEM, "cudaMallocHost(%zu) for the host-path staging: %s", bytes,
                 cudaGetErrorString(e));
   }
-  pl->pinned_cap = bytes;
+  c->pinned_cap = bytes;
   return XC_OK;
 }
 
-int ws_get(size_t bytes, void **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if ((int)g_ws.size() <= dev) g_ws.resize(dev + 1);
-  Workspace &w = g_ws[dev];
-  if (w.cap < bytes) {
-    if (w.ptr) {
-      cudaFree(w.ptr);
-      w.ptr = nullptr;
-      w.cap = 0;
+int ctx_workspace(HostCtx *c, size_t bytes, void **out) {
+  if (c->ws_cap < bytes) {
+    if (c->ws) {
+      cudaFree(c->ws);
+      c->ws = nullptr;
+      c->ws_cap = 0;
     }
-    e = xc::dev_malloc(&w.ptr, bytes);
+    const cudaError_t e = xc::dev_malloc(&c->ws, bytes);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(XC_ERR_NOMEM, "cudaMalloc(%zu) for the host-path workspace: %s", bytes,
                   cudaGetErrorString(e));
     }
-    w.cap = bytes;
+    c->ws_cap = bytes;
   }
-  *out = w.ptr;
+  *out = c->ws;
   return XC_OK;
 }
 
@@ -196,15 +241,16 @@ const char *xc_version(void) { return "xcape_gb300 0.1.0 (sm_103a)"; }
 long long xc_alloc_count(void) { return g_allocs.load(std::memory_order_relaxed); }
 
 int xc_release_workspace(void) {
-  std::lock_guard<std::mutex> lk(g_ws_mu);
+  // frees the workspaces of the contexts no call holds
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
   int prev = 0;
   cudaGetDevice(&prev);
-  for (size_t d = 0; d < g_ws.size(); ++d) {
-    if (g_ws[d].ptr) {
-      cudaSetDevice((int)d);
-      cudaFree(g_ws[d].ptr);
-      g_ws[d] = Workspace();
-    }
+  for (auto &c : g_ctx) {
+    if (c->busy || !c->ws) continue;
+    cudaSetDevice(c->dev);
+    cudaFree(c->ws);
+    c->ws = nullptr;
+    c->ws_cap = 0;
   }
   cudaSetDevice(prev);
   return XC_OK;
@@ -432,10 +478,10 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
   const bool has_start = grid != 1 && start_3d;
   // cape, cin, mulvl, z_out (, status: the caller's, or the retry's flags) per source
   const int nout = (status || retry) ? 5 : 4;
-  std::lock_guard<std::mutex> lk(g_ws_mu);
-  Pipeline *pl = nullptr;
-  rc = pipeline_get(&pl);
+  HostCtxLease lease;
+  rc = lease.acquire();
   if (rc) return rc;
+  HostCtx *pl = lease.c;
   struct Slot {
     size_t p, t, td, ps, ts, tds, st, out, ord;
   } sl[HOST_CHUNKS];
@@ -465,10 +511,10 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
   Carver cv;
   for (int k = 0; k < nslot; ++k) carve(cv, sl[k]);
   void *base = nullptr;
-  rc = ws_get(cv.off, &base);
+  rc = ctx_workspace(pl, cv.off, &base);
   if (rc) return rc;
   char *b = (char *)base;
-  rc = pipeline_pinned(pl, out_bytes * nslot);
+  rc = ctx_pinned(pl, out_bytes * nslot);
   if (rc) return rc;
   // output array j of source s in a slot (device or its pinned staging)
   auto out_off = [&](int s_, int j) { return ((size_t)s_ * nout + j) * C * 4; };
@@ -781,7 +827,9 @@ int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
   const size_t es = dtype == XC_F32 ? 4 : 8;
   const size_t n3 = (size_t)n2 * nk;
   const size_t p_bytes = (grid == 2 ? (size_t)nk : n3) * es;
-  std::lock_guard<std::mutex> lk(g_ws_mu);
+  HostCtxLease lease;
+  rc = lease.acquire();
+  if (rc) return rc;
   Carver cv;
   const size_t o_p = cv.take(p_bytes), o_t = cv.take(n3 * es), o_td = cv.take(n3 * es),
                o_u = cv.take(n3 * es), o_v = cv.take(n3 * es);
@@ -792,10 +840,15 @@ int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
   const size_t o_rm = rm ? cv.take(n2 * 8) : 0, o_lm = rm ? cv.take(n2 * 8) : 0,
                o_mean = rm ? cv.take(n2 * 8) : 0;
   void *base = nullptr;
-  rc = ws_get(cv.off, &base);
+  rc = ctx_workspace(lease.c, cv.off, &base);
   if (rc) return rc;
   char *b = (char *)base;
-  cudaStream_t s = (cudaStream_t)stream;
+  // on the context's first stream, after the caller's stream, so that
+  // concurrent calls from several threads overlap on the GPU
+  cudaStream_t s = lease.c->s[0];
+  cudaError_t e0 = cudaEventRecord(lease.c->start, (cudaStream_t)stream);
+  if (e0 == cudaSuccess) e0 = cudaStreamWaitEvent(s, lease.c->start, 0);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "ordering the host path after the caller's stream");
   cudaError_t e = cudaSuccess;
 #define H2D(off, src, bytes)                                                         \
   if (e == cudaSuccess) e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, s)
