@@ -920,6 +920,7 @@ def run_serve(args):
             # warm-up: one batch of the first requests
             srv.finish(srv.launch(srv.admit([request(r) for r in trace[:8]])))
             torch.cuda.synchronize()
+            srv.stats = {k: 0 for k in srv.stats}
             lat, batches, cols, nxt = [], [], 0, 0
             pending, inflight = [], None
             busy, t_busy = 0.0, None
@@ -950,8 +951,10 @@ def run_serve(args):
                         t_busy = None
                 inflight = batch
             wall = time.perf_counter() - t0
+            st = dict(srv.stats)
         lat_ms = np.array(lat) * 1e3
-        return {"requests": len(lat), "columns": cols, "wall_s": wall,
+        st["h2d_gbs"] = st["h2d_bytes"] / (st["h2d_ms"] * 1e-3) / 1e9 if st["h2d_ms"] else None
+        return {"requests": len(lat), "columns": cols, "wall_s": wall, "device_time": st,
                 "columns_per_s": cols / wall, "busy_fraction": busy / wall,
                 "columns_per_busy_s": cols / busy if busy else None,
                 "p50_ms": float(np.percentile(lat_ms, 50)),

@@ -89,8 +89,11 @@ def _pinned(a):
 
 
 class _Batch:
-    def __init__(self, slot, reqs, views, done):
-        self.slot, self.reqs, self.views, self.done = slot, reqs, views, done
+    def __init__(self, slot, reqs, views, events):
+        self.slot, self.reqs, self.views = slot, reqs, views
+        self.events = events  # copies start, copies in, run done, results out
+        self.done = events[-1]
+        self.h2d_bytes = 0
 
 
 class CapeServer:
@@ -120,6 +123,10 @@ class CapeServer:
         self.max_requests = max_requests
         self.slot = 0
         self.busy = [None, None]
+        # per finished batch: host-to-device copies, executor run and
+        # device-to-host copies (ms, CUDA events) and bytes copied in
+        self.stats = {"batches": 0, "h2d_ms": 0.0, "run_ms": 0.0, "d2h_ms": 0.0,
+                      "h2d_bytes": 0}
 
     def admit(self, pending):
         """Takes requests from the front of `pending` (a list, consumed) while
@@ -180,8 +187,10 @@ class CapeServer:
             for name in ("cape", "cin", "mulvl", "z_out"):
                 v[name] = alloc(4 * r.n2)
             views.append(v)
-        copied = torch.cuda.Event()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        copied = ev[1]
         with torch.cuda.stream(self.copy_stream):
+            ev[0].record(self.copy_stream)
             for o, h in copies:
                 arena[o:o + h.numel()].copy_(h, non_blocking=True)
             copied.record(self.copy_stream)
@@ -208,10 +217,11 @@ class CapeServer:
                                                for n in ("cape", "cin", "mulvl", "z_out")])
             descs.append(q)
         self.compute_stream.wait_event(copied)
-        done = torch.cuda.Event()
+        done = ev[3]
         with torch.cuda.stream(self.compute_stream):
             if descs:
                 self.executor.run(descs, stream=self.compute_stream)
+            ev[2].record(self.compute_stream)
             # the outputs back into the staging (the inputs staged there have
             # been copied: the compute stream waited for the copies)
             for v in views:
@@ -219,7 +229,8 @@ class CapeServer:
                     o, n, so = v[name]
                     stage[so:so + n].copy_(arena[o:o + n], non_blocking=True)
             done.record(self.compute_stream)
-        b = _Batch(k, reqs, views, done)
+        b = _Batch(k, reqs, views, ev)
+        b.h2d_bytes = sum(h.numel() for _, h in copies)
         self.busy[k] = b
         return b
 
@@ -227,6 +238,12 @@ class CapeServer:
         """Waits for `batch`; returns [(request, (cape, cin, mulvl, z_out))]
         with the results as numpy arrays (copies)."""
         batch.done.synchronize()
+        e = batch.events
+        self.stats["batches"] += 1
+        self.stats["h2d_ms"] += e[0].elapsed_time(e[1])
+        self.stats["run_ms"] += e[1].elapsed_time(e[2])
+        self.stats["d2h_ms"] += e[2].elapsed_time(e[3])
+        self.stats["h2d_bytes"] += batch.h2d_bytes
         st = self.staging[batch.slot].numpy()
         out = []
         for r, v in zip(batch.reqs, batch.views):
