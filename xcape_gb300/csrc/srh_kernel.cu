@@ -144,6 +144,180 @@ __global__ void __launch_bounds__(SRH_TILE) srh_tile_kernel(SrhArgs a) {
   srh_column_body<true>(a, i, lv, sf, nk - st + 2);
 }
 
+// FP32 path for float inputs, level-parallel: a segment of SRH_SEG lanes
+// sweeps one column, lane l taking levels j = 2 + SRH_SEG s + l at step s,
+// so that each step reads SRH_SEG consecutive levels of every input row
+// (coalesced, no shared-memory staging) and a column's dependent chain is
+// ncl / SRH_SEG steps long instead of ncl.  Per step:
+//   * each lane computes its level's virtual temperature and hypsometric
+//     increment (the level below comes from the lane below by shuffle, or
+//     from the previous step's last lane);
+//   * the heights are the segment's inclusive scan of the increments on top
+//     of the previous step's last height;
+//   * a lane whose layer [H(j-1), H(j)) holds a Bunkers target height
+//     interpolates the winds there (DINTERP2DZ's weights) into the column's
+//     target slots in shared memory;
+//   * the first level above `depth` (the lowest crossing lane of the first
+//     step that crosses) interpolates the winds at `depth` (INTERP1), and
+//     every level up to it adds its term of the helicity sums' storm-motion
+//     free part A = sum(u_k dv_k - v_k du_k).
+// The sums over k = 2..ktop of (u_k - c_u) dv_k - (v_k - c_v) du_k then
+// follow for both storm motions: A - c_u (v_top - v_s) + c_v (u_top - u_s),
+// since dv and du telescope.  This needs heights that increase with level:
+// each target then falls in exactly one layer, the highest bracket
+// DINTERP2DZ keeps.  A column whose heights do not increase (a non-finite
+// input, pressures that are not decreasing) is redone by its segment's
+// first lane with the one-thread column routine of the FP32 path
+// (srh_column_run), which follows the reference's scan rules for any
+// column.  Its contract is the FP32 path's: agreement with the FP64
+// reference within tolerance.
+constexpr int SRH_SEG = 8;
+constexpr int SRH_SEG_THREADS = 128;
+
+template <int GRID>
+__global__ void __launch_bounds__(SRH_SEG_THREADS) srh_seg_kernel(SrhArgs a) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int COLS = SRH_SEG_THREADS / SRH_SEG;  // columns per block
+  __shared__ float slot_u[COLS][12], slot_v[COLS][12];
+  const int lane = threadIdx.x & 31;
+  const int sl = lane & (SRH_SEG - 1);
+  const unsigned seg_mask = 0xffu << (lane & ~(SRH_SEG - 1));
+  const int cb = threadIdx.x / SRH_SEG;  // column within the block
+  const long long i = (long long)blockIdx.x * COLS + cb;
+  const bool active = i < a.n2;
+  const int nk = a.nk;
+  const float *gp = (const float *)a.p, *gt = (const float *)a.t, *gtd = (const float *)a.td;
+  const float *gu = (const float *)a.u, *gv = (const float *)a.v;
+  // the column's surface and level window
+  float ps = 1000.0f, ts = 0.0f, tds = 0.0f, us = 0.0f, vs = 0.0f;
+  int st = 1, ncl = 1;
+  long long row = 0;
+  if (active) {
+    ps = __ldg((const float *)a.ps + i);
+    ts = __ldg((const float *)a.ts + i);
+    tds = __ldg((const float *)a.tds + i);
+    us = __ldg((const float *)a.us + i);
+    vs = __ldg((const float *)a.vs + i);
+    if (GRID == 2) {
+      st = a.start ? __ldg(a.start + i) : pres_lev_pos_col<float>(gp, ps, nk);
+      st = st < 1 ? 1 : (st > nk + 1 ? nk + 1 : st);
+    }
+    ncl = nk - st + 2;
+    row = i * nk;
+  }
+  const int base = st - 3;  // 0-based input index of assembled level j: base + j
+  for (int k = sl; k < 24; k += SRH_SEG) {
+    if (k < 12) slot_u[cb][k] = VMSG;
+    else slot_v[cb][k - 12] = VMSG;
+  }
+  __syncwarp();
+  const float depth = (float)a.depth, aglh0 = (float)a.aglh0;
+  // the level below the step's first lane: the surface to begin with
+  float Pc = ps, Tvc = stdh_tv_f(ps, ts, tds), uc = us, vc = vs, Hc = aglh0;
+  bool mono = true;
+  int ktop = 0;
+  float utop = 0.0f, vtop = 0.0f, A = 0.0f;
+  const int nsteps = active ? (ncl - 1 + SRH_SEG - 1) / SRH_SEG : 0;
+  const int wsteps = __reduce_max_sync(FULL, nsteps);
+  for (int s = 0; s < wsteps; ++s) {
+    const int j = 2 + s * SRH_SEG + sl;
+    const bool valid = s < nsteps && j <= ncl;
+    float P = Pc, T = 0.0f, Td = 0.0f, u = uc, v = vc, Tv = Tvc;
+    if (valid) {
+      const int m = base + j;
+      P = __ldg(GRID == 2 ? gp + m : gp + row + m);
+      T = __ldg(gt + row + m);
+      Td = __ldg(gtd + row + m);
+      u = __ldg(gu + row + m);
+      v = __ldg(gv + row + m);
+      Tv = stdh_tv_f(P, T, Td);
+    }
+    // level j - 1
+    float Pm = __shfl_up_sync(FULL, P, 1, SRH_SEG), Tvm = __shfl_up_sync(FULL, Tv, 1, SRH_SEG);
+    float um = __shfl_up_sync(FULL, u, 1, SRH_SEG), vm = __shfl_up_sync(FULL, v, 1, SRH_SEG);
+    if (sl == 0) {
+      Pm = Pc;
+      Tvm = Tvc;
+      um = uc;
+      vm = vc;
+    }
+    const float dh = valid ? stdh_dh_f(Tv, Tvm, P, Pm) : 0.0f;
+    mono = mono && (!valid || dh > 0.0f);
+    float x = dh;  // inclusive scan of the increments over the segment
+#pragma unroll
+    for (int d = 1; d < SRH_SEG; d <<= 1) {
+      const float y = __shfl_up_sync(FULL, x, d, SRH_SEG);
+      if (sl >= d) x += y;
+    }
+    const float H = Hc + x;
+    float Hm = __shfl_up_sync(FULL, H, 1, SRH_SEG);
+    if (sl == 0) Hm = Hc;
+    if (valid && mono)
+      bunkers_bracket<false>(Hm, H, um, u, vm, v, slot_u[cb], slot_v[cb]);
+    // the SREH top level: the lowest lane of the first crossing step
+    const unsigned cm = __ballot_sync(FULL, valid && ktop == 0 && H > depth) & seg_mask;
+    const int first = cm ? (__ffs(cm) - 1) & (SRH_SEG - 1) : SRH_SEG;
+    if (ktop == 0 && valid) {
+      if (sl < first) {
+        A += nc_mul(u, v - vm) - nc_mul(v, u - um);
+      } else if (sl == first) {
+        // INTERP1 (SREH_model_lev.f90:123-129): X1 = aglh(ktop), X3 = aglh(ktop-1)
+        float x1 = H;
+        const float x3 = Hm;
+        if (x3 == x1) x1 = x1 - 0.01f;
+        utop = u + nc_mul((um - u), ((depth - x1) / (x3 - x1)));
+        if (x3 == x1) x1 = x1 - 0.01f;
+        vtop = v + nc_mul((vm - v), ((depth - x1) / (x3 - x1)));
+        A += nc_mul(utop, vtop - vm) - nc_mul(vtop, utop - um);
+      }
+    }
+    if (ktop == 0 && cm) ktop = 2 + s * SRH_SEG + first;
+    // what the next step's first lane needs: this step's last level
+    Pc = __shfl_sync(FULL, P, SRH_SEG - 1, SRH_SEG);
+    Tvc = __shfl_sync(FULL, Tv, SRH_SEG - 1, SRH_SEG);
+    uc = __shfl_sync(FULL, u, SRH_SEG - 1, SRH_SEG);
+    vc = __shfl_sync(FULL, v, SRH_SEG - 1, SRH_SEG);
+    Hc = __shfl_sync(FULL, H, SRH_SEG - 1, SRH_SEG);
+  }
+  // utop and vtop live in the crossing lane: the segment's sums
+  float ut = utop, vt = vtop;
+#pragma unroll
+  for (int d = SRH_SEG / 2; d > 0; d >>= 1) {
+    A += __shfl_xor_sync(FULL, A, d, SRH_SEG);
+    ut += __shfl_xor_sync(FULL, ut, d, SRH_SEG);
+    vt += __shfl_xor_sync(FULL, vt, d, SRH_SEG);
+  }
+  const bool all_mono = (__ballot_sync(FULL, !mono) & seg_mask) == 0;
+  __syncwarp();
+  if (!active || sl != 0) return;
+  if (!all_mono) {
+    srh_column_run<float, GRID, true>(a, i);  // any column, the reference's scan rules
+    return;
+  }
+  float u6[12], v6[12];
+  for (int k = 0; k < 12; ++k) {
+    u6[k] = slot_u[cb][k];
+    v6[k] = slot_v[cb][k];
+  }
+  float rm[2], lm[2], mean[2];
+  bunkers_finish(us, vs, u6, v6, rm, lm, mean);
+  double srh_rm = -0.0, srh_lm = -0.0;
+  if (ktop > 0) {
+    const float dv = vt - vs, du = ut - us;
+    srh_rm = -(double)(A - nc_mul(rm[0], dv) + nc_mul(rm[1], du));
+    srh_lm = -(double)(A - nc_mul(lm[0], dv) + nc_mul(lm[1], du));
+  }
+  srh_write(a, i, rm, lm, mean, srh_rm, srh_lm);
+}
+
+template <int GRID>
+static cudaError_t launch_srh_seg(const SrhArgs &a, cudaStream_t s) {
+  const long long cols = SRH_SEG_THREADS / SRH_SEG;
+  const unsigned blocks = (unsigned)((a.n2 + cols - 1) / cols);
+  srh_seg_kernel<GRID><<<blocks, SRH_SEG_THREADS, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int GRID>
 static cudaError_t launch_srh_tile(const SrhArgs &a, size_t smem, cudaStream_t s) {
   static std::atomic<int> attr[kMaxAttrDevices];
@@ -178,9 +352,13 @@ cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s) {
   const unsigned blocks = blocks_for(a.n2, 128);
   if (blocks == 0) return cudaSuccess;
   if (a.precision == 1 && a.dtype == 0) {
-    const size_t smem = srh_tile_smem(a.grid, a.nk);
-    if (smem <= SRH_TILE_SMEM_MAX)
-      return a.grid == 1 ? launch_srh_tile<1>(a, smem, s) : launch_srh_tile<2>(a, smem, s);
+    if (a.srh_kernel == 1) {
+      const size_t smem = srh_tile_smem(a.grid, a.nk);
+      if (smem <= SRH_TILE_SMEM_MAX)
+        return a.grid == 1 ? launch_srh_tile<1>(a, smem, s) : launch_srh_tile<2>(a, smem, s);
+    } else {
+      return a.grid == 1 ? launch_srh_seg<1>(a, s) : launch_srh_seg<2>(a, s);
+    }
   }
   if (a.precision == 1)
     launch_srh_p<true>(a, blocks, s);

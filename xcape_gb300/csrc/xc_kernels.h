@@ -105,6 +105,7 @@ struct SrhArgs {
   double *srh_rm, *srh_lm;
   float *rm, *lm, *mean6;  // nullable, [n2][2]
   int precision;           // 0: reference precisions (FP64 stdheight/SREH), 1: FP32
+  int srh_kernel = 0;      // FP32 path, f32 inputs: 0 level-parallel segments, 1 staged tile
 };
 
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
