@@ -920,7 +920,7 @@ def run_serve(args):
             # warm-up: one batch of the first requests
             srv.finish(srv.launch(srv.admit([request(r) for r in trace[:8]])))
             torch.cuda.synchronize()
-            srv.stats = {k: 0 for k in srv.stats}
+            srv.stats = {k: [] if isinstance(v, list) else 0 for k, v in srv.stats.items()}
             lat, batches, cols, nxt = [], [], 0, 0
             pending, inflight = [], None
             busy, t_busy = 0.0, None
@@ -953,6 +953,16 @@ def run_serve(args):
             wall = time.perf_counter() - t0
             st = dict(srv.stats)
         lat_ms = np.array(lat) * 1e3
+        # host-to-device rate of the batches by their input volume
+        pb = np.array(st.pop("per_batch"), dtype=np.float64).reshape(-1, 3)
+        st["h2d_by_batch_size"] = {}
+        for name, lo, hi in (("<64MB", 0, 64e6), ("64MB-1GB", 64e6, 1e9), (">1GB", 1e9, 1e30)):
+            sel = (pb[:, 0] >= lo) & (pb[:, 0] < hi)
+            if sel.any():
+                st["h2d_by_batch_size"][name] = {
+                    "batches": int(sel.sum()), "gbs": float(pb[sel, 0].sum() /
+                                                           (pb[sel, 1].sum() * 1e-3) / 1e9),
+                    "run_ms_mean": float(pb[sel, 2].mean())}
         st["h2d_gbs"] = st["h2d_bytes"] / (st["h2d_ms"] * 1e-3) / 1e9 if st["h2d_ms"] else None
         return {"requests": len(lat), "columns": cols, "wall_s": wall, "device_time": st,
                 "columns_per_s": cols / wall, "busy_fraction": busy / wall,

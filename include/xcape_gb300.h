@@ -280,10 +280,10 @@ int xc_calc_srh_host(int grid, const void *p, const void *t3d, const void *td3d,
  * optional).  CAPE options and outputs as xc_loopcape_ex, with guess
  * XC_GUESS_PLAIN or XC_GUESS_LEARNED; depth, aglh0, precision and the SRH
  * outputs as xc_calc_srh_ex.  workspace (nullable, as xc_loopcape_ex)
- * orders the columns for the lift.  With guess XC_GUESS_LEARNED, precision
- * XC_SRH_FP32 and f32 inputs the call runs the two kernels back to back
- * instead, which is faster there (the SRH kernel's rows are read coalesced
- * through shared memory). */
+ * orders the columns for the lift.  With precision XC_SRH_FP32 and f32
+ * inputs the call runs the lift and calc_srh's level-parallel FP32 kernel
+ * back to back instead, which is faster there (that kernel reads each
+ * column's rows coalesced with eight lanes per column). */
 int xc_cape_srh(int grid, const void *p, const void *t3d, const void *td3d, const void *u3d,
                 const void *v3d, const void *ps, const void *ts, const void *tds, const void *us,
                 const void *vs, int dtype, float pinc, int source, float ml_depth, int adiabat,

@@ -794,13 +794,14 @@ int xc_cape_srh(int grid, const void *p, const void *t3d, const void *td3d, cons
     e = xc::launch_order(a, workspace, &a.perm, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
   }
-  if (guess == XC_GUESS_LEARNED && precision == XC_SRH_FP32 && dtype == XC_F32) {
-    // Here the learned lift and the FP32 SRH tile kernel back to back are
-    // faster than the fused kernel: the tile kernel reads its rows
-    // coalesced through shared memory, while the fused kernel's per-thread
-    // walk of the ordered (scattered) columns costs more than the shared
-    // reads save (3.73 against 3.95 ms at 1M columns x 50 levels).  With
-    // the FP64 SRH stages, or the plain solver, the fused kernel wins.
+  if (precision == XC_SRH_FP32 && dtype == XC_F32) {
+    // With the FP32 SRH stages and f32 inputs the SRH part runs the
+    // level-parallel kernel of calc_srh (eight lanes per column, coalesced
+    // reads, no staging), which a fused kernel's one-thread walk of the
+    // ordered (scattered) columns cannot match: the lift and that kernel run
+    // back to back, and their results are those of the two calls.  With the
+    // FP64 SRH stages, or f64 inputs, the fused kernel lets the lift and the
+    // FP64 stages share the SMs.
     e = xc::launch_cape(a, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
     e = xc::launch_srh(h, (cudaStream_t)stream);

@@ -145,22 +145,25 @@ __global__ void __launch_bounds__(SRH_TILE) srh_tile_kernel(SrhArgs a) {
 }
 
 // FP32 path for float inputs, level-parallel: a segment of SRH_SEG lanes
-// sweeps one column, lane l taking levels j = 2 + SRH_SEG s + l at step s,
-// so that each step reads SRH_SEG consecutive levels of every input row
-// (coalesced, no shared-memory staging) and a column's dependent chain is
-// ncl / SRH_SEG steps long instead of ncl.  Per step:
-//   * each lane computes its level's virtual temperature and hypsometric
-//     increment (the level below comes from the lane below by shuffle, or
-//     from the previous step's last lane);
-//   * the heights are the segment's inclusive scan of the increments on top
-//     of the previous step's last height;
-//   * a lane whose layer [H(j-1), H(j)) holds a Bunkers target height
-//     interpolates the winds there (DINTERP2DZ's weights) into the column's
-//     target slots in shared memory;
-//   * the first level above `depth` (the lowest crossing lane of the first
-//     step that crosses) interpolates the winds at `depth` (INTERP1), and
-//     every level up to it adds its term of the helicity sums' storm-motion
-//     free part A = sum(u_k dv_k - v_k du_k).
+// sweeps one column in rounds of SRH_SEG * SRH_RUN levels, lane l taking the
+// run of SRH_RUN consecutive levels j = j0 + SRH_RUN l .. of the round.
+// Each lane reads its run of every input row (the warp's loads cover four
+// columns' rows, and the run's sectors stay in L1 between its levels: no
+// shared-memory staging), so a column's dependent chain is SRH_RUN levels
+// long instead of ncl, and the lanes talk only once per round:
+//   * phase 1, per lane: the virtual temperature of each level of the run
+//     and its hypsometric increment (the level below the run's first comes
+//     from the lane below by shuffle, or from the previous round);
+//   * the heights: each lane's running sum of its increments on top of the
+//     segment's exclusive scan of the lanes' totals and of the previous
+//     round's last height;
+//   * phase 2, per lane: a level whose layer [H(j-1), H(j)) holds a Bunkers
+//     target height interpolates the winds there (DINTERP2DZ's weights) into
+//     the column's target slots in shared memory; the first level above
+//     `depth` (the lowest lane's first such level, in the first round that
+//     has one) interpolates the winds at `depth` (INTERP1); every level up
+//     to it adds its term of the helicity sums' storm-motion free part
+//     A = sum(u_k dv_k - v_k du_k).
 // The sums over k = 2..ktop of (u_k - c_u) dv_k - (v_k - c_v) du_k then
 // follow for both storm motions: A - c_u (v_top - v_s) + c_v (u_top - u_s),
 // since dv and du telescope.  This needs heights that increase with level:
@@ -172,6 +175,7 @@ __global__ void __launch_bounds__(SRH_TILE) srh_tile_kernel(SrhArgs a) {
 // column.  Its contract is the FP32 path's: agreement with the FP64
 // reference within tolerance.
 constexpr int SRH_SEG = 8;
+constexpr int SRH_RUN = 8;
 constexpr int SRH_SEG_THREADS = 128;
 
 template <int GRID>
@@ -212,72 +216,112 @@ __global__ void __launch_bounds__(SRH_SEG_THREADS) srh_seg_kernel(SrhArgs a) {
   }
   __syncwarp();
   const float depth = (float)a.depth, aglh0 = (float)a.aglh0;
-  // the level below the step's first lane: the surface to begin with
+  // the level below the round's first level: the surface to begin with
   float Pc = ps, Tvc = stdh_tv_f(ps, ts, tds), uc = us, vc = vs, Hc = aglh0;
   bool mono = true;
   int ktop = 0;
   float utop = 0.0f, vtop = 0.0f, A = 0.0f;
-  const int nsteps = active ? (ncl - 1 + SRH_SEG - 1) / SRH_SEG : 0;
-  const int wsteps = __reduce_max_sync(FULL, nsteps);
-  for (int s = 0; s < wsteps; ++s) {
-    const int j = 2 + s * SRH_SEG + sl;
-    const bool valid = s < nsteps && j <= ncl;
-    float P = Pc, T = 0.0f, Td = 0.0f, u = uc, v = vc, Tv = Tvc;
-    if (valid) {
-      const int m = base + j;
-      P = __ldg(GRID == 2 ? gp + m : gp + row + m);
-      T = __ldg(gt + row + m);
-      Td = __ldg(gtd + row + m);
-      u = __ldg(gu + row + m);
-      v = __ldg(gv + row + m);
-      Tv = stdh_tv_f(P, T, Td);
+  constexpr int ROUND = SRH_SEG * SRH_RUN;
+  const int nrounds = active ? (ncl - 1 + ROUND - 1) / ROUND : 0;
+  const int wrounds = __reduce_max_sync(FULL, nrounds);
+  for (int r = 0; r < wrounds; ++r) {
+    const int j0 = 2 + r * ROUND + sl * SRH_RUN;  // this lane's first level
+    float P[SRH_RUN], Tv[SRH_RUN], u[SRH_RUN], v[SRH_RUN], h[SRH_RUN];
+    int nv = r < nrounds ? ncl - j0 + 1 : 0;  // valid levels of the run
+    nv = nv < 0 ? 0 : (nv > SRH_RUN ? SRH_RUN : nv);
+#pragma unroll
+    for (int c = 0; c < SRH_RUN; ++c) {
+      P[c] = 1.0f;
+      Tv[c] = 0.0f;
+      u[c] = 0.0f;
+      v[c] = 0.0f;
+      if (c < nv) {
+        const int m = base + j0 + c;
+        P[c] = __ldg(GRID == 2 ? gp + m : gp + row + m);
+        const float T = __ldg(gt + row + m), Td = __ldg(gtd + row + m);
+        u[c] = __ldg(gu + row + m);
+        v[c] = __ldg(gv + row + m);
+        Tv[c] = stdh_tv_f(P[c], T, Td);
+      }
     }
-    // level j - 1
-    float Pm = __shfl_up_sync(FULL, P, 1, SRH_SEG), Tvm = __shfl_up_sync(FULL, Tv, 1, SRH_SEG);
-    float um = __shfl_up_sync(FULL, u, 1, SRH_SEG), vm = __shfl_up_sync(FULL, v, 1, SRH_SEG);
+    // the level below the run: the lane below's last level, or the carry
+    const float Pl = P[SRH_RUN - 1], Tvl = Tv[SRH_RUN - 1], ul = u[SRH_RUN - 1], vl = v[SRH_RUN - 1];
+    float Pm = __shfl_up_sync(FULL, Pl, 1, SRH_SEG), Tvm = __shfl_up_sync(FULL, Tvl, 1, SRH_SEG);
+    float um = __shfl_up_sync(FULL, ul, 1, SRH_SEG), vm = __shfl_up_sync(FULL, vl, 1, SRH_SEG);
     if (sl == 0) {
       Pm = Pc;
       Tvm = Tvc;
       um = uc;
       vm = vc;
     }
-    const float dh = valid ? stdh_dh_f(Tv, Tvm, P, Pm) : 0.0f;
-    mono = mono && (!valid || dh > 0.0f);
-    float x = dh;  // inclusive scan of the increments over the segment
+    // increments and the run's running sum
+    float run = 0.0f;
+#pragma unroll
+    for (int c = 0; c < SRH_RUN; ++c) {
+      float dh = 0.0f;
+      if (c < nv) {
+        dh = stdh_dh_f(Tv[c], c == 0 ? Tvm : Tv[c - 1], P[c], c == 0 ? Pm : P[c - 1]);
+        mono = mono && dh > 0.0f;
+      }
+      run += dh;
+      h[c] = run;
+    }
+    // heights: the exclusive scan of the lanes' run totals
+    float x = run;
 #pragma unroll
     for (int d = 1; d < SRH_SEG; d <<= 1) {
       const float y = __shfl_up_sync(FULL, x, d, SRH_SEG);
       if (sl >= d) x += y;
     }
-    const float H = Hc + x;
-    float Hm = __shfl_up_sync(FULL, H, 1, SRH_SEG);
-    if (sl == 0) Hm = Hc;
-    if (valid && mono)
-      bunkers_bracket<false>(Hm, H, um, u, vm, v, slot_u[cb], slot_v[cb]);
-    // the SREH top level: the lowest lane of the first crossing step
-    const unsigned cm = __ballot_sync(FULL, valid && ktop == 0 && H > depth) & seg_mask;
-    const int first = cm ? (__ffs(cm) - 1) & (SRH_SEG - 1) : SRH_SEG;
-    if (ktop == 0 && valid) {
-      if (sl < first) {
-        A += nc_mul(u, v - vm) - nc_mul(v, u - um);
-      } else if (sl == first) {
-        // INTERP1 (SREH_model_lev.f90:123-129): X1 = aglh(ktop), X3 = aglh(ktop-1)
-        float x1 = H;
-        const float x3 = Hm;
-        if (x3 == x1) x1 = x1 - 0.01f;
-        utop = u + nc_mul((um - u), ((depth - x1) / (x3 - x1)));
-        if (x3 == x1) x1 = x1 - 0.01f;
-        vtop = v + nc_mul((vm - v), ((depth - x1) / (x3 - x1)));
-        A += nc_mul(utop, vtop - vm) - nc_mul(vtop, utop - um);
+    const float below = Hc + (x - run);  // height of the level below the run
+    // phase 2: Bunkers targets, the SREH top and the helicity terms
+    float hp = below, up = um, vp = vm;
+    int first = SRH_RUN;  // this lane's first level above depth
+#pragma unroll
+    for (int c = 0; c < SRH_RUN; ++c) {
+      const float H = below + h[c];
+      h[c] = H;
+      if (c < nv) {
+        if (mono && hp <= 6000.0f)  // no target above 6 km
+          bunkers_bracket<false>(hp, H, up, u[c], vp, v[c], slot_u[cb], slot_v[cb]);
+        if (first == SRH_RUN && H > depth) first = c;
+      }
+      hp = H;
+      up = u[c];
+      vp = v[c];
+    }
+    const unsigned cm = __ballot_sync(FULL, ktop == 0 && first < SRH_RUN) & seg_mask;
+    const int fl = cm ? (__ffs(cm) - 1) & (SRH_SEG - 1) : SRH_SEG;  // the crossing lane
+    if (ktop == 0 && sl <= fl) {
+      const int upto = sl < fl ? nv : first;  // levels whose terms this lane adds
+      hp = below;
+      up = um;
+      vp = vm;
+#pragma unroll
+      for (int c = 0; c < SRH_RUN; ++c) {
+        if (c < upto) A += nc_mul(u[c], v[c] - vp) - nc_mul(v[c], u[c] - up);
+        if (sl == fl && c == first) {
+          // INTERP1 (SREH_model_lev.f90:123-129): X1 = aglh(ktop), X3 = aglh(ktop-1)
+          float x1 = h[c];
+          const float x3 = hp;
+          if (x3 == x1) x1 = x1 - 0.01f;
+          utop = u[c] + nc_mul((up - u[c]), ((depth - x1) / (x3 - x1)));
+          if (x3 == x1) x1 = x1 - 0.01f;
+          vtop = v[c] + nc_mul((vp - v[c]), ((depth - x1) / (x3 - x1)));
+          A += nc_mul(utop, vtop - vp) - nc_mul(vtop, utop - up);
+        }
+        hp = h[c];
+        up = u[c];
+        vp = v[c];
       }
     }
-    if (ktop == 0 && cm) ktop = 2 + s * SRH_SEG + first;
-    // what the next step's first lane needs: this step's last level
-    Pc = __shfl_sync(FULL, P, SRH_SEG - 1, SRH_SEG);
-    Tvc = __shfl_sync(FULL, Tv, SRH_SEG - 1, SRH_SEG);
-    uc = __shfl_sync(FULL, u, SRH_SEG - 1, SRH_SEG);
-    vc = __shfl_sync(FULL, v, SRH_SEG - 1, SRH_SEG);
-    Hc = __shfl_sync(FULL, H, SRH_SEG - 1, SRH_SEG);
+    if (ktop == 0 && cm) ktop = 1;  // found (its index itself is not needed)
+    // the round's last level, for the next round's first lane
+    Pc = __shfl_sync(FULL, Pl, SRH_SEG - 1, SRH_SEG);
+    Tvc = __shfl_sync(FULL, Tvl, SRH_SEG - 1, SRH_SEG);
+    uc = __shfl_sync(FULL, ul, SRH_SEG - 1, SRH_SEG);
+    vc = __shfl_sync(FULL, vl, SRH_SEG - 1, SRH_SEG);
+    Hc = __shfl_sync(FULL, h[SRH_RUN - 1], SRH_SEG - 1, SRH_SEG);
   }
   // utop and vtop live in the crossing lane: the segment's sums
   float ut = utop, vt = vtop;

@@ -126,7 +126,7 @@ class CapeServer:
         # per finished batch: host-to-device copies, executor run and
         # device-to-host copies (ms, CUDA events) and bytes copied in
         self.stats = {"batches": 0, "h2d_ms": 0.0, "run_ms": 0.0, "d2h_ms": 0.0,
-                      "h2d_bytes": 0}
+                      "h2d_bytes": 0, "per_batch": []}
 
     def admit(self, pending):
         """Takes requests from the front of `pending` (a list, consumed) while
@@ -244,6 +244,8 @@ class CapeServer:
         self.stats["run_ms"] += e[1].elapsed_time(e[2])
         self.stats["d2h_ms"] += e[2].elapsed_time(e[3])
         self.stats["h2d_bytes"] += batch.h2d_bytes
+        self.stats["per_batch"].append((batch.h2d_bytes, e[0].elapsed_time(e[1]),
+                                        e[1].elapsed_time(e[2])))
         st = self.staging[batch.slot].numpy()
         out = []
         for r, v in zip(batch.reqs, batch.views):
