@@ -271,6 +271,26 @@ def test_srh_fp32_level_parallel_kernel_matches_column_path(depth):
             np.testing.assert_allclose(g, w, rtol=0, atol=1e-4)
 
 
+@pytest.mark.parametrize("nlev", [137, 100])
+def test_srh_fp32_level_parallel_kernel_several_rounds(nlev):
+    """Columns deeper than one round of the level-parallel kernel (137 sigma
+    levels: three rounds of 8 lanes x 6 levels; 100 pressure levels with
+    ragged starts: three rounds of 8 x 5) against the FP64 oracle, at the
+    FP32 path's tolerance."""
+    cases = ((S.srh_c2(shape=(20, 24), nlev=nlev), "model") if nlev == 137 else
+             (S.pressure_srh(shape=(20, 24), nlev=nlev), "pressure"))
+    args, vl = cases
+    args = [np.asarray(x, np.float32) for x in args]
+    for depth in (1000, 3000):
+        got = X.calc_srh(*args, depth=depth, vertical_lev=vl, output_var="all", precision="fp32")
+        want = O.calc_srh(*[x.astype(np.float64) for x in args], depth=depth, vertical_lev=vl,
+                          output_var="all", precision="f64")
+        for g, w in zip(got[:2], want[:2]):
+            np.testing.assert_allclose(g, w, rtol=0, atol=0.05)
+        for g, w in zip(got[2:], want[2:]):
+            np.testing.assert_allclose(g, w, rtol=0, atol=1e-3)
+
+
 def test_srh_fp32_level_parallel_kernel_falls_back_on_irregular_columns():
     """Columns whose heights do not increase with level -- pressure rising
     with level, a NaN, a level below the previous one -- are redone by the

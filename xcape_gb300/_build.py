@@ -22,7 +22,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC", "-I", INCLUDE]
 
 SOURCES = ["capi.cu", "cape_kernel.cu", "srh_kernel.cu", "noalloc.cu", "guess_mlp.cu", "batch.cu",
-           "cape_diag.cu", "cape_srh.cu", "pipe_peaks.cu", "cape_retry.cu"]
+           "cape_diag.cu", "cape_srh.cu", "pipe_peaks.cu", "cape_retry.cu",
+           "srh_seg.cu"]
 
 # Per-file flags.  The SRH path is FP64 hypsometry feeding FP32 Bunkers
 # arithmetic whose reference goldens are pinned to 1e-5: it is built without

@@ -177,10 +177,8 @@ struct SrhColumn {
   int base;  // start - 3: the 0-based input index of assembled level j is base + j
 };
 
-// Level readers of the fused path.  GlobalLevels reads the input arrays of
-// one column (the virtual temperature computed from p, t, td as the level
-// is reached); SharedLevels reads rows that srh_tile_kernel staged in shared
-// memory, with the virtual temperature already computed.
+// Level reader of the column path: the input arrays of one column, the
+// virtual temperature computed from p, t, td as the level is reached.
 template <bool F32, typename T>
 struct GlobalLevels {
   typedef typename SrhReal<F32>::type R;
@@ -192,14 +190,6 @@ struct GlobalLevels {
   }
   XC_HD R u(int m) const { return F32 ? (R)ldf(c->u + m) : (R)ldd(c->u + m); }
   XC_HD R v(int m) const { return F32 ? (R)ldf(c->v + m) : (R)ldd(c->v + m); }
-};
-
-struct SharedLevels {  // FP32 path only
-  const float *P, *TV, *U, *V;
-  XC_HD float p(int m) const { return P[m]; }
-  XC_HD float tv(int m, float) const { return TV[m]; }
-  XC_HD float u(int m) const { return U[m]; }
-  XC_HD float v(int m) const { return V[m]; }
 };
 
 // Surface values and level window of one column.
@@ -218,8 +208,7 @@ struct SrhPass1 {
 // order, one step per level: the hypsometric height (FP64, or FP32 with
 // Kahan compensation when F32), the 12 Bunkers targets (DEC selects the
 // scan rule) and the SREH top level.  srh_pass1 feeds it the levels through
-// a reader: global memory (GlobalLevels) or rows that srh_tile_kernel staged
-// in shared memory (SharedLevels); the operations are the same.
+// a reader (GlobalLevels).
 template <bool DEC, bool F32>
 struct SrhSweep {
   typedef typename SrhReal<F32>::type R;

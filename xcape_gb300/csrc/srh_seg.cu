@@ -1,0 +1,350 @@
+// srh_seg.cu -- the FP32 storm-relative helicity kernel for float inputs
+// (calc_srh with precision='fp32'): stdheight -> Bunkers -> SREH of one
+// column per segment of SEG = 8 lanes, four columns per warp.
+//
+// A segment sweeps its column in rounds of SEG * RUN levels, lane l taking the
+// RUN consecutive levels j0 = 2 + round * SEG * RUN + l * RUN .. j0 + RUN - 1 of
+// the assembled column (level 1 is the surface).  Each lane reads its run of
+// every input row (a run's sectors stay in L1 between its levels), so the
+// per-column dependent chain is RUN levels long, and the lanes talk once per
+// round:
+//   * per lane, straight-line: the virtual temperature of each level and the
+//     hypsometric increment from the level below (the level below the run's
+//     first comes from the lane below by shuffle, or from the previous
+//     round);
+//   * the heights: each lane's running sum on top of the segment's exclusive
+//     scan of the lanes' totals and of the previous round's last height;
+//   * per lane: a level whose layer [z(j-1), z(j)) holds Bunkers targets
+//     interpolates the winds there (DINTERP2DZ, Bunkers_model_lev.f90:
+//     188-236) into the column's target slots in shared memory; the first
+//     level above `depth` interpolates the winds at `depth` (INTERP1,
+//     SREH_model_lev.f90:123-129); every level up to it adds its term of the
+//     storm-motion free part of the helicity sums,
+//       A = sum_k (u_k dv_k - v_k du_k) = sum_k (u_(k-1) v_k - u_k v_(k-1)).
+// The helicity for storm motion (c_u, c_v) then is
+//   sum_k (u_k - c_u) dv_k - (v_k - c_v) du_k = A - c_u (v_top - v_s) + c_v (u_top - u_s)
+// since dv and du telescope.  This needs heights that increase with level:
+// each target then falls in exactly one layer, the highest bracket that
+// DINTERP2DZ keeps.  A column whose heights do not increase (pressures that
+// do not decrease, a non-finite input) is redone by its segment's first lane
+// with the one-thread FP32 column routine (srh_column_run), which follows
+// the reference's scan rules for any column.
+//
+// The arithmetic is FP32 with approximate transcendentals; the contract is
+// the FP32 path's, agreement with the FP64 reference within tolerance:
+//   E  = 6.112 exp(53.49 - 6808/Td - 5.09 ln Td)   (Td in K, E in hPa)
+//   Tv = T (w + eps) / (eps (1 + w)),  w = eps E / (P - E)
+//      = T P / (P - (1 - eps) E)
+// (stdheight_2D_model_lev.f90:116-131), one reciprocal instead of three
+// divides, and log2 E = K0 - K1/Td - 5.09 log2 Td; the hypsometric step
+// (:147, :155) between level b (below) and level a
+//   dz = (R/|g|) (Tv_a + Tv_b)/2 ln(P_b / P_a) = (C Tv_a + C Tv_b) log2(P_b / P_a),
+// with C = (R/|g|) ln(2) / 2 folded into the virtual temperature.  The
+// transcendentals are the PTX approximations with subnormals flushed to zero:
+// their operands (temperatures in K, pressures in hPa and their ratios) are
+// far from the subnormal range for any physical column.
+//
+// Loads are clamped to the column's last level (and columns past the end to
+// the last column), so every lane loads and computes unconditionally; the
+// levels past a column's top are masked out of the sums.
+#include "srh_column.cuh"
+#include "xc_kernels.h"
+
+namespace xc {
+namespace {
+
+constexpr int SEG = 8;
+constexpr int SEG_THREADS = 128;
+
+__device__ __forceinline__ float rcp_a(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_a(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float ex2_a(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+constexpr float SEG_K0 = 79.78140228f;  // log2(6.112) + 53.49 log2(e)
+constexpr float SEG_K1 = (float)(6808.0 * 1.4426950408889634);  // 6808 log2(e)
+constexpr float SEG_K2 = 5.09f;
+constexpr float SEG_OME = (float)(1.0 - (double)0.6219800858985514f);  // 1 - eps
+constexpr float SEG_C = (float)((double)287.04f / (double)9.80665f * 0.5 * 0.6931471805599453);
+
+// C Tv of a level: P in hPa, T and Td in degC.
+__device__ __forceinline__ float seg_ctv(float P, float T, float Td) {
+  const float tdk = Td + 273.15f;
+  const float l2e = fmaf(-SEG_K2, lg2_a(tdk), fmaf(-SEG_K1, rcp_a(tdk), SEG_K0));
+  const float den = fmaf(-SEG_OME, ex2_a(l2e), P);
+  return fmaf(SEG_C, T, SEG_C * 273.15f) * P * rcp_a(den);
+}
+
+// Number of the Bunkers targets 500, 1000, ..., 6000 m lying below z (0 for
+// NaN).  It is monotone in z, so with heights increasing the targets of the
+// layer [z_lo, z_hi) are those numbered seg_below(z_lo) .. seg_below(z_hi) - 1
+// and every target falls in exactly one layer; a target within rounding of a
+// layer boundary may fall in the layer on the other side, where its
+// interpolation weight is 0 or 1 within rounding.
+__device__ __forceinline__ int seg_below(float z) {
+  const int k = __float2int_ru(z * (1.0f / 500.0f));
+  return min(max(k, 1), 13) - 1;
+}
+
+}  // namespace
+
+template <int GRID, int RUN>
+__global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int COLS = SEG_THREADS / SEG;  // columns per block
+  constexpr int ROUND = SEG * RUN;
+  __shared__ float slot_u[COLS][12], slot_v[COLS][12];
+  const int lane = threadIdx.x & 31;
+  const int sl = lane & (SEG - 1);
+  const unsigned seg_mask = 0xffu << (lane & ~(SEG - 1));
+  const int cb = threadIdx.x / SEG;  // column within the block
+  const long long i = (long long)blockIdx.x * COLS + cb;
+  const bool active = i < a.n2;
+  const long long ic = active ? i : a.n2 - 1;  // the column whose inputs this segment reads
+  const int nk = a.nk;
+  const float *gp = (const float *)a.p, *gt = (const float *)a.t, *gtd = (const float *)a.td;
+  const float *gu = (const float *)a.u, *gv = (const float *)a.v;
+  const float ps = __ldg((const float *)a.ps + ic), ts = __ldg((const float *)a.ts + ic);
+  const float tds = __ldg((const float *)a.tds + ic);
+  const float us = __ldg((const float *)a.us + ic), vs = __ldg((const float *)a.vs + ic);
+  int st = 1;
+  if (GRID == 2) {
+    st = a.start ? __ldg(a.start + ic) : pres_lev_pos_col<float>(gp, ps, nk);
+    st = st < 1 ? 1 : (st > nk + 1 ? nk + 1 : st);
+  }
+  const int ncl = nk - st + 2;  // assembled levels: 1 (surface) .. ncl
+  const long long row = ic * nk;
+  const int base = st - 3;  // 0-based input index of assembled level j: base + j
+  for (int k = sl; k < 24; k += SEG) {
+    if (k < 12) slot_u[cb][k] = VMSG;
+    else slot_v[cb][k - 12] = VMSG;
+  }
+  __syncwarp();
+  const float depth = (float)a.depth;
+  // the level below the round's first level: the surface to begin with
+  float Pc = ps, Cc = seg_ctv(ps, ts, tds), uc = us, vc = vs, Hc = (float)a.aglh0;
+  bool mono = true;
+  int ktop = 0;
+  float utop = 0.0f, vtop = 0.0f, A = 0.0f;
+  const int nrounds = active ? (ncl - 1 + ROUND - 1) / ROUND : 0;
+  const int wrounds = __reduce_max_sync(FULL, nrounds);
+  for (int r = 0; r < wrounds; ++r) {
+    const int j0 = 2 + r * ROUND + sl * RUN;  // this lane's first level
+    int nv = r < nrounds ? ncl - j0 + 1 : 0;  // valid levels of the run
+    nv = nv < 0 ? 0 : (nv > RUN ? RUN : nv);
+    float u[RUN], v[RUN], z[RUN];
+    float Pf = 0.0f, Cf = 0.0f, Pl = 0.0f, Cl = 0.0f;  // first and last level's P and C Tv
+    float s = 0.0f;  // running sum of the increments of levels 1 .. RUN-1 of the run
+#pragma unroll
+    for (int c = 0; c < RUN; ++c) {
+      const int m = min(base + j0 + c, nk - 1);
+      const float P = __ldg(GRID == 2 ? gp + m : gp + row + m);
+      const float T = __ldg(gt + row + m), Td = __ldg(gtd + row + m);
+      u[c] = __ldg(gu + row + m);
+      v[c] = __ldg(gv + row + m);
+      const float ct = seg_ctv(P, T, Td);
+      if (c == 0) {
+        Pf = P;
+        Cf = ct;
+        z[0] = 0.0f;
+      } else {
+        const float dz = (ct + Cl) * lg2_a(Pl * rcp_a(P));
+        const bool ok = c < nv;
+        mono = mono && (!ok || dz > 0.0f);
+        s += ok ? dz : 0.0f;
+        z[c] = s;
+      }
+      Pl = P;
+      Cl = ct;
+    }
+    // the level below the run: the lane below's last level, or the carry
+    float Pm = __shfl_up_sync(FULL, Pl, 1, SEG), Cm = __shfl_up_sync(FULL, Cl, 1, SEG);
+    float um = __shfl_up_sync(FULL, u[RUN - 1], 1, SEG);
+    float vm = __shfl_up_sync(FULL, v[RUN - 1], 1, SEG);
+    if (sl == 0) {
+      Pm = Pc;
+      Cm = Cc;
+      um = uc;
+      vm = vc;
+    }
+    float dz0 = (Cf + Cm) * lg2_a(Pm * rcp_a(Pf));
+    mono = mono && (nv == 0 || dz0 > 0.0f);
+    dz0 = nv > 0 ? dz0 : 0.0f;
+    // heights: the exclusive scan of the lanes' run totals
+    const float tot = dz0 + s;
+    float x = tot;
+#pragma unroll
+    for (int d = 1; d < SEG; d <<= 1) {
+      const float y = __shfl_up_sync(FULL, x, d, SEG);
+      if (sl >= d) x += y;
+    }
+    float ex = __shfl_up_sync(FULL, x, 1, SEG);
+    if (sl == 0) ex = 0.0f;
+    const float below = Hc + ex;  // height of the level below the run
+    const float b0 = below + dz0;
+    z[0] = b0;
+#pragma unroll
+    for (int c = 1; c < RUN; ++c) z[c] = b0 + z[c];
+    // Bunkers targets of each layer, and the levels at or below depth
+    int ka = seg_below(below);
+    int nle = 0;
+    float za = below, ua = um, va = vm;
+#pragma unroll
+    for (int c = 0; c < RUN; ++c) {
+      const float zb = z[c];
+      const int kb = seg_below(zb);
+      for (int k = ka; k < kb; ++k) {
+        const float w = (500.0f * (float)(k + 1) - za) * rcp_a(zb - za);
+        slot_u[cb][k] = fmaf(w, u[c] - ua, ua);
+        slot_v[cb][k] = fmaf(w, v[c] - va, va);
+      }
+      nle += (c < nv && zb <= depth) ? 1 : 0;
+      ka = kb;
+      za = zb;
+      ua = u[c];
+      va = v[c];
+    }
+    // the lane holding the first level above depth (the lowest such lane in
+    // the first round that has one), and the helicity terms below it
+    const unsigned cm = __ballot_sync(FULL, ktop == 0 && nle < nv) & seg_mask;
+    const int fl = cm ? (__ffs(cm) - 1) & (SEG - 1) : SEG;
+    const int lim = (ktop != 0 || sl > fl) ? 0 : (sl < fl ? nv : nle);
+    const int tsel = (ktop == 0 && sl == fl) ? nle : -1;
+    float zl = below, ul = um, vl = vm, zh = 0.0f, uh = 0.0f, vh = 0.0f;
+    za = below;
+    ua = um;
+    va = vm;
+#pragma unroll
+    for (int c = 0; c < RUN; ++c) {
+      if (c < lim) A = fmaf(ua, v[c], fmaf(-u[c], va, A));
+      if (c == tsel) {
+        zl = za;
+        ul = ua;
+        vl = va;
+        zh = z[c];
+        uh = u[c];
+        vh = v[c];
+      }
+      za = z[c];
+      ua = u[c];
+      va = v[c];
+    }
+    if (tsel >= 0) {
+      // INTERP1 with X1 = aglh(ktop), X3 = aglh(ktop-1): X3 < X1 for
+      // increasing heights, so its X3 == X1 adjustment never applies here
+      const float w = (depth - zh) * rcp_a(zl - zh);
+      utop = fmaf(ul - uh, w, uh);
+      vtop = fmaf(vl - vh, w, vh);
+      A = fmaf(ul, vtop, fmaf(-utop, vl, A));
+    }
+    if (cm) ktop = 1;  // found (its index itself is not needed)
+    // the round's last level, for the next round's first lane
+    Pc = __shfl_sync(FULL, Pl, SEG - 1, SEG);
+    Cc = __shfl_sync(FULL, Cl, SEG - 1, SEG);
+    uc = __shfl_sync(FULL, u[RUN - 1], SEG - 1, SEG);
+    vc = __shfl_sync(FULL, v[RUN - 1], SEG - 1, SEG);
+    Hc = __shfl_sync(FULL, z[RUN - 1], SEG - 1, SEG);
+  }
+  // segment sums: A over the lanes; utop and vtop live in the crossing lane
+  float ut = utop, vt = vtop;
+#pragma unroll
+  for (int d = SEG / 2; d > 0; d >>= 1) {
+    A += __shfl_xor_sync(FULL, A, d, SEG);
+    ut += __shfl_xor_sync(FULL, ut, d, SEG);
+    vt += __shfl_xor_sync(FULL, vt, d, SEG);
+  }
+  const bool all_mono = (__ballot_sync(FULL, !mono) & seg_mask) == 0;
+  __syncwarp();
+  // Bunkers storm motions (bunkers_calc_ml, Bunkers_model_lev.f90:123-177):
+  // the 0-6 km mean wind of the surface and the 12 targets, and the shear
+  // from the 0-500 m mean to the 5.5-6 km mean
+  float su = slot_u[cb][sl] + (sl < 4 ? slot_u[cb][sl + 8] : 0.0f);
+  float sv = slot_v[cb][sl] + (sl < 4 ? slot_v[cb][sl + 8] : 0.0f);
+#pragma unroll
+  for (int d = SEG / 2; d > 0; d >>= 1) {
+    su += __shfl_xor_sync(FULL, su, d, SEG);
+    sv += __shfl_xor_sync(FULL, sv, d, SEG);
+  }
+  if (!active) return;
+  if (!all_mono) {
+    if (sl == 0) srh_column_run<float, GRID, true>(a, i);  // the reference's scan rules
+    return;
+  }
+  const float m0 = (us + su) * (1.0f / 13.0f), m1 = (vs + sv) * (1.0f / 13.0f);
+  const float ushr = 0.5f * (slot_u[cb][10] + slot_u[cb][11]) - 0.5f * (us + slot_u[cb][0]);
+  const float vshr = 0.5f * (slot_v[cb][10] + slot_v[cb][11]) - 0.5f * (vs + slot_v[cb][0]);
+  const float f = 7.5f * rsqrtf(fmaf(ushr, ushr, vshr * vshr));
+  const float rm0 = fmaf(f, vshr, m0), rm1 = fmaf(-f, ushr, m1);
+  const float lm0 = fmaf(-f, vshr, m0), lm1 = fmaf(f, ushr, m1);
+  // one output per lane of the segment
+  if (sl < 2) {
+    double h = -0.0;
+    if (ktop > 0) {
+      const float cu = sl == 0 ? rm0 : lm0, cv = sl == 0 ? rm1 : lm1;
+      h = -(double)fmaf(cv, ut - us, fmaf(-cu, vt - vs, A));
+    }
+    (sl == 0 ? a.srh_rm : a.srh_lm)[i] = h;
+  } else if (a.rm) {
+    float *dst = sl < 4 ? a.rm : (sl < 6 ? a.lm : a.mean6);
+    const float val = sl == 2 ? rm0 : sl == 3 ? rm1 : sl == 4 ? lm0 : sl == 5 ? lm1
+                    : sl == 6 ? m0 : m1;
+    dst[2 * i + (sl & 1)] = val;
+  }
+}
+
+namespace {
+
+template <int GRID, int RUN>
+cudaError_t launch_seg(const SrhArgs &a, cudaStream_t s) {
+  constexpr long long cols = SEG_THREADS / SEG;
+  const unsigned blocks = (unsigned)((a.n2 + cols - 1) / cols);
+  srh_seg_kernel<GRID, RUN><<<blocks, SEG_THREADS, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int GRID>
+cudaError_t launch_seg_g(const SrhArgs &a, int run, cudaStream_t s) {
+  switch (run) {
+    case 5: return launch_seg<GRID, 5>(a, s);
+    case 6: return launch_seg<GRID, 6>(a, s);
+    case 7: return launch_seg<GRID, 7>(a, s);
+    default: return launch_seg<GRID, 8>(a, s);
+  }
+}
+
+}  // namespace
+
+// The run length of the levels above the surface (nk at most): the fewest
+// level slots rounds * RUN over RUN = 5..8, the longer run on a tie (fewer
+// rounds).  50 levels take one round of 8 x 7, 37 one of 8 x 5, 137 three
+// of 8 x 6.
+int srh_seg_run(int levels) {
+  int best = 8, best_slots = 1 << 30;
+  for (int run = 8; run >= 5; --run) {
+    const int rounds = (levels + SEG * run - 1) / (SEG * run);
+    if (rounds * run < best_slots) {
+      best = run;
+      best_slots = rounds * run;
+    }
+  }
+  return best;
+}
+
+cudaError_t launch_srh_seg(const SrhArgs &a, cudaStream_t s) {
+  if (a.n2 <= 0) return cudaSuccess;
+  const int run = srh_seg_run(a.nk);
+  return a.grid == 1 ? launch_seg_g<1>(a, run, s) : launch_seg_g<2>(a, run, s);
+}
+
+}  // namespace xc

@@ -105,10 +105,13 @@ struct SrhArgs {
   double *srh_rm, *srh_lm;
   float *rm, *lm, *mean6;  // nullable, [n2][2]
   int precision;           // 0: reference precisions (FP64 stdheight/SREH), 1: FP32
-  int srh_kernel = 0;      // FP32 path, f32 inputs: 0 level-parallel segments, 1 staged tile
 };
 
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
+// The FP32 level-parallel kernel for float inputs (srh_seg.cu), and its run
+// length for a column of `levels` levels above the surface.
+cudaError_t launch_srh_seg(const SrhArgs &a, cudaStream_t s);
+int srh_seg_run(int levels);
 // CAPE (guess 0 or 1) and SRH of the same columns in one kernel (cape_srh.cu).
 cudaError_t launch_cape_srh(const CapeArgs &a, const SrhArgs &s, cudaStream_t st);
 
