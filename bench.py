@@ -726,6 +726,7 @@ def run_srh(args):
     srm, slm = (torch.empty(n2, dtype=torch.float64, device="cuda") for _ in range(2))
     rm, lm, mean = (torch.empty(2 * n2, dtype=torch.float32, device="cuda") for _ in range(3))
     s = torch.cuda.current_stream().cuda_stream
+    ref_out = None  # the reference precision's outputs at depth 3000 m
 
     for prec, prec_name, dt in ((0, "reference", "f64+f32"), (1, "fp32", "f32")):
         def step():
@@ -745,6 +746,17 @@ def run_srh(args):
             e1.record()
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.steps
+        outs = (srm, slm, rm, lm, mean)  # those of the last launch, depth 3000 m
+        agree = None
+        if ref_out is None:
+            ref_out = [x.clone() for x in outs]
+        else:
+            # every column of the FP32 path against the reference precision
+            agree = {"columns": n2, "depth_m": 3000.0,
+                     "srh_max_abs_m2s2": max(float((x - y).abs().max())
+                                             for x, y in zip(outs[:2], ref_out[:2])),
+                     "storm_motion_max_abs_ms": max(float((x - y).abs().max())
+                                                    for x, y in zip(outs[2:], ref_out[2:]))}
         hbm_peak, kind = measured_peaks()
         # algorithmic bytes of one launch: p, t, td, u, v (50 levels) and five
         # surface fields in, two f64 helicities and three f32 pairs out
@@ -760,6 +772,7 @@ def run_srh(args):
                                        "unit": "GB/s", "frac": ach / hbm_peak,
                                        "peak_kind": kind},
                           "gpu_launches": 2 * args.steps,
+                          **({"agreement_vs_reference_precision": agree} if agree else {}),
                           "clocks": clk.summary()}), flush=True)
     return 0
 

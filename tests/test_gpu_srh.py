@@ -256,9 +256,13 @@ def test_srh_fp32_level_parallel_kernel_matches_column_path(depth):
     """float32 inputs take the level-parallel kernel (srh_seg_kernel: eight
     lanes per column, heights by a segmented scan, helicity from its
     storm-motion free part); the same values as float64 take the one-thread
-    FP32 column path.  Both are FP32 forms of the same arithmetic, summed in
-    different orders: SRH within 0.01 m^2/s^2, storm motion within 1e-4 m/s,
-    for sigma and pressure grids, ragged starts and a partial last block."""
+    FP32 column path.  Both are FP32 forms of the same formulas with
+    approximate transcendentals, but not the same forms (the kernel's
+    virtual temperature takes one reciprocal, its log is of the pressure
+    ratio taken the other way up) nor the same summation orders: SRH within
+    0.01 m^2/s^2, storm motion within 5e-4 m/s (each is within 1e-3 m/s of
+    the FP64 oracle, test_srh_fp32_precision_vs_fp64), for sigma and
+    pressure grids, ragged starts and a partial last block."""
     for args, vl in ((S.srh_c2(shape=(37, 41)), "model"),
                      (S.pressure_srh(shape=(29, 33)), "pressure")):
         a32 = [np.asarray(x, np.float32) for x in args]
@@ -268,7 +272,7 @@ def test_srh_fp32_level_parallel_kernel_matches_column_path(depth):
         for g, w in zip(got[:2], want[:2]):
             np.testing.assert_allclose(g, w, rtol=0, atol=1e-2)
         for g, w in zip(got[2:], want[2:]):
-            np.testing.assert_allclose(g, w, rtol=0, atol=1e-4)
+            np.testing.assert_allclose(g, w, rtol=0, atol=5e-4)
 
 
 @pytest.mark.parametrize("nlev", [137, 100])
@@ -285,6 +289,27 @@ def test_srh_fp32_level_parallel_kernel_several_rounds(nlev):
         got = X.calc_srh(*args, depth=depth, vertical_lev=vl, output_var="all", precision="fp32")
         want = O.calc_srh(*[x.astype(np.float64) for x in args], depth=depth, vertical_lev=vl,
                           output_var="all", precision="f64")
+        for g, w in zip(got[:2], want[:2]):
+            np.testing.assert_allclose(g, w, rtol=0, atol=0.05)
+        for g, w in zip(got[2:], want[2:]):
+            np.testing.assert_allclose(g, w, rtol=0, atol=1e-3)
+
+
+def test_srh_fp32_level_parallel_kernel_short_columns():
+    """A coarse pressure grid (9 levels, 1000-100 hPa) with ragged starts:
+    columns with fewer levels above the ground than one run of the
+    level-parallel kernel (5 levels here) are taken by the column routine;
+    all agree with the FP64 oracle at the FP32 path's tolerance."""
+    args = [np.asarray(x, np.float32).copy() for x in S.pressure_srh(shape=(24, 30), nlev=9,
+                                                                       seed=5)]
+    args[5].reshape(-1)[::3] = 520.0   # high ground: 4 levels above it
+    start = O.pres_lev_pos(args[0].astype(np.float64), np.ravel(args[5]).astype(np.float64))
+    assert (9 - np.ravel(start) + 1 < 5).any() and (9 - np.ravel(start) + 1 >= 5).any()
+    for depth in (1000, 3000):
+        got = X.calc_srh(*args, depth=depth, vertical_lev="pressure", output_var="all",
+                         precision="fp32")
+        want = O.calc_srh(*[x.astype(np.float64) for x in args], depth=depth,
+                          vertical_lev="pressure", output_var="all", precision="f64")
         for g, w in zip(got[:2], want[:2]):
             np.testing.assert_allclose(g, w, rtol=0, atol=0.05)
         for g, w in zip(got[2:], want[2:]):

@@ -62,7 +62,8 @@ static void launch_srh_p(const SrhArgs &a, unsigned blocks, cudaStream_t s) {
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s) {
   const unsigned blocks = blocks_for(a.n2, 128);
   if (blocks == 0) return cudaSuccess;
-  if (a.precision == 1 && a.dtype == 0) return launch_srh_seg(a, s);  // srh_seg.cu
+  if (a.precision == 1 && a.dtype == 0 && srh_seg_run(a.nk) > 0)
+    return launch_srh_seg(a, s);  // srh_seg.cu
   if (a.precision == 1)
     launch_srh_p<true>(a, blocks, s);
   else

@@ -26,9 +26,10 @@
 // since dv and du telescope.  This needs heights that increase with level:
 // each target then falls in exactly one layer, the highest bracket that
 // DINTERP2DZ keeps.  A column whose heights do not increase (pressures that
-// do not decrease, a non-finite input) is redone by its segment's first lane
-// with the one-thread FP32 column routine (srh_column_run), which follows
-// the reference's scan rules for any column.
+// do not decrease, a non-finite input), or that has fewer levels above the
+// ground than one run, is redone by its segment's first lane with the
+// one-thread FP32 column routine (srh_column_run), which follows the
+// reference's scan rules for any column.
 //
 // The arithmetic is FP32 with approximate transcendentals; the contract is
 // the FP32 path's, agreement with the FP64 reference within tolerance:
@@ -44,9 +45,12 @@
 // their operands (temperatures in K, pressures in hPa and their ratios) are
 // far from the subnormal range for any physical column.
 //
-// Loads are clamped to the column's last level (and columns past the end to
-// the last column), so every lane loads and computes unconditionally; the
-// levels past a column's top are masked out of the sums.
+// Every lane loads and computes unconditionally: it reads a window of RUN
+// levels inside its column's row (its run, or the row's last RUN levels for
+// a run that reaches past the column top), at fixed offsets from one
+// pointer per array, and a bit mask of the window's slots that hold its own
+// levels keeps the others out of the sums; segments past the last column
+// read the last column.  The window needs nk >= RUN.
 #include "srh_column.cuh"
 #include "xc_kernels.h"
 
@@ -134,33 +138,42 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
   const float depth = (float)a.depth;
   // the level below the round's first level: the surface to begin with
   float Pc = ps, Cc = seg_ctv(ps, ts, tds), uc = us, vc = vs, Hc = (float)a.aglh0;
-  bool mono = true;
+  // a column with fewer levels above the ground than one run would read
+  // levels below the ground into its first window: the column routine
+  // takes it, as it takes columns whose heights do not increase
+  bool mono = ncl - 1 >= RUN;
   int ktop = 0;
   float utop = 0.0f, vtop = 0.0f, A = 0.0f;
   const int nrounds = active ? (ncl - 1 + ROUND - 1) / ROUND : 0;
   const int wrounds = __reduce_max_sync(FULL, nrounds);
   for (int r = 0; r < wrounds; ++r) {
-    const int j0 = 2 + r * ROUND + sl * RUN;  // this lane's first level
-    int nv = r < nrounds ? ncl - j0 + 1 : 0;  // valid levels of the run
-    nv = nv < 0 ? 0 : (nv > RUN ? RUN : nv);
+    // this lane's levels: mb .. mb + RUN - 1 (0-based input indices), read
+    // through a window of RUN levels inside the row -- the run itself, or for
+    // a run that reaches past the column top the last RUN levels of the row,
+    // whose first `lo` slots are levels of the lane below
+    const int mb = base + 2 + r * ROUND + sl * RUN;
+    const int ws = min(mb, nk - RUN);
+    const int lo = r < nrounds ? min(mb - ws, RUN) : RUN;
+    const unsigned valid = (0xffu << lo) & ((1u << RUN) - 1);  // slots holding this lane's levels
+    const float *wp = GRID == 2 ? gp + ws : gp + row + ws;
+    const float *wt = gt + row + ws, *wtd = gtd + row + ws;
+    const float *wu = gu + row + ws, *wv = gv + row + ws;
     float u[RUN], v[RUN], z[RUN];
-    float Pf = 0.0f, Cf = 0.0f, Pl = 0.0f, Cl = 0.0f;  // first and last level's P and C Tv
-    float s = 0.0f;  // running sum of the increments of levels 1 .. RUN-1 of the run
+    float Pf = 0.0f, Cf = 0.0f, Pl = 0.0f, Cl = 0.0f;  // first and last slot's P and C Tv
+    float s = 0.0f;  // running sum of the increments of slots 1 .. RUN-1
 #pragma unroll
     for (int c = 0; c < RUN; ++c) {
-      const int m = min(base + j0 + c, nk - 1);
-      const float P = __ldg(GRID == 2 ? gp + m : gp + row + m);
-      const float T = __ldg(gt + row + m), Td = __ldg(gtd + row + m);
-      u[c] = __ldg(gu + row + m);
-      v[c] = __ldg(gv + row + m);
-      const float ct = seg_ctv(P, T, Td);
+      const float P = __ldg(wp + c);
+      u[c] = __ldg(wu + c);
+      v[c] = __ldg(wv + c);
+      const float ct = seg_ctv(P, __ldg(wt + c), __ldg(wtd + c));
       if (c == 0) {
         Pf = P;
         Cf = ct;
         z[0] = 0.0f;
       } else {
         const float dz = (ct + Cl) * lg2_a(Pl * rcp_a(P));
-        const bool ok = c < nv;
+        const bool ok = (valid >> c) & 1u;
         mono = mono && (!ok || dz > 0.0f);
         s += ok ? dz : 0.0f;
         z[c] = s;
@@ -168,7 +181,7 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
       Pl = P;
       Cl = ct;
     }
-    // the level below the run: the lane below's last level, or the carry
+    // the level below slot 0: the lane below's last slot, or the carry
     float Pm = __shfl_up_sync(FULL, Pl, 1, SEG), Cm = __shfl_up_sync(FULL, Cl, 1, SEG);
     float um = __shfl_up_sync(FULL, u[RUN - 1], 1, SEG);
     float vm = __shfl_up_sync(FULL, v[RUN - 1], 1, SEG);
@@ -179,9 +192,10 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
       vm = vc;
     }
     float dz0 = (Cf + Cm) * lg2_a(Pm * rcp_a(Pf));
-    mono = mono && (nv == 0 || dz0 > 0.0f);
-    dz0 = nv > 0 ? dz0 : 0.0f;
-    // heights: the exclusive scan of the lanes' run totals
+    mono = mono && (lo != 0 || dz0 > 0.0f);
+    dz0 = lo == 0 ? dz0 : 0.0f;
+    // heights: the exclusive scan of the lanes' run totals; slots below the
+    // lane's first level keep the height of the level below it
     const float tot = dz0 + s;
     float x = tot;
 #pragma unroll
@@ -191,12 +205,13 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
     }
     float ex = __shfl_up_sync(FULL, x, 1, SEG);
     if (sl == 0) ex = 0.0f;
-    const float below = Hc + ex;  // height of the level below the run
+    const float below = Hc + ex;  // height of the level below the lane's first level
     const float b0 = below + dz0;
     z[0] = b0;
 #pragma unroll
     for (int c = 1; c < RUN; ++c) z[c] = b0 + z[c];
-    // Bunkers targets of each layer, and the levels at or below depth
+    // Bunkers targets of each layer (empty for the slots below the lane's
+    // first level), and the slots at or below depth
     int ka = seg_below(below);
     int nle = 0;
     float za = below, ua = um, va = vm;
@@ -209,40 +224,41 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
         slot_u[cb][k] = fmaf(w, u[c] - ua, ua);
         slot_v[cb][k] = fmaf(w, v[c] - va, va);
       }
-      nle += (c < nv && zb <= depth) ? 1 : 0;
+      nle += zb <= depth ? 1 : 0;
       ka = kb;
       za = zb;
       ua = u[c];
       va = v[c];
     }
     // the lane holding the first level above depth (the lowest such lane in
-    // the first round that has one), and the helicity terms below it
-    const unsigned cm = __ballot_sync(FULL, ktop == 0 && nle < nv) & seg_mask;
+    // the first round that has one) and, in it, that level's slot; with
+    // increasing heights it follows the slots at or below depth, and the
+    // slots below the lane's first level count as such when the level
+    // below it does
+    const bool crosses = valid != 0 && z[RUN - 1] > depth;
+    const unsigned cm = __ballot_sync(FULL, ktop == 0 && crosses) & seg_mask;
     const int fl = cm ? (__ffs(cm) - 1) & (SEG - 1) : SEG;
-    const int lim = (ktop != 0 || sl > fl) ? 0 : (sl < fl ? nv : nle);
-    const int tsel = (ktop == 0 && sl == fl) ? nle : -1;
-    float zl = below, ul = um, vl = vm, zh = 0.0f, uh = 0.0f, vh = 0.0f;
-    za = below;
+    const int t = min(max(nle, lo), RUN - 1);
+    const int hi = (ktop != 0 || sl > fl) ? 0 : (sl < fl ? RUN : t);
+    const unsigned incl = valid & ((1u << hi) - 1);  // slots whose helicity terms this lane adds
+    const bool top = ktop == 0 && sl == fl;
+    float zl = below, zh = 0.0f;
     ua = um;
     va = vm;
 #pragma unroll
     for (int c = 0; c < RUN; ++c) {
-      if (c < lim) A = fmaf(ua, v[c], fmaf(-u[c], va, A));
-      if (c == tsel) {
-        zl = za;
-        ul = ua;
-        vl = va;
-        zh = z[c];
-        uh = u[c];
-        vh = v[c];
-      }
-      za = z[c];
+      if ((incl >> c) & 1u) A = fmaf(ua, v[c], fmaf(-u[c], va, A));
+      if (c == t - 1) zl = z[c];
+      if (c == t) zh = z[c];
       ua = u[c];
       va = v[c];
     }
-    if (tsel >= 0) {
+    if (top) {
       // INTERP1 with X1 = aglh(ktop), X3 = aglh(ktop-1): X3 < X1 for
-      // increasing heights, so its X3 == X1 adjustment never applies here
+      // increasing heights, so its X3 == X1 adjustment never applies here.
+      // The winds of the two levels are read again (from L1).
+      const float uh = __ldg(wu + t), vh = __ldg(wv + t);
+      const float ul = t > 0 ? __ldg(wu + t - 1) : um, vl = t > 0 ? __ldg(wv + t - 1) : vm;
       const float w = (depth - zh) * rcp_a(zl - zh);
       utop = fmaf(ul - uh, w, uh);
       vtop = fmaf(vl - vh, w, vh);
@@ -325,13 +341,14 @@ cudaError_t launch_seg_g(const SrhArgs &a, int run, cudaStream_t s) {
 
 }  // namespace
 
-// The run length of the levels above the surface (nk at most): the fewest
-// level slots rounds * RUN over RUN = 5..8, the longer run on a tie (fewer
-// rounds).  50 levels take one round of 8 x 7, 37 one of 8 x 5, 137 three
-// of 8 x 6.
+// The run length for columns of nk input levels: the fewest level slots
+// rounds * RUN over RUN = 5..min(8, nk), the longer run on a tie (fewer
+// rounds); 0 (no run: the column kernel serves) below 5 levels.  50 levels
+// take one round of 8 x 7, 37 one of 8 x 5, 137 three of 8 x 6.
 int srh_seg_run(int levels) {
-  int best = 8, best_slots = 1 << 30;
-  for (int run = 8; run >= 5; --run) {
+  if (levels < 5) return 0;
+  int best = 5, best_slots = 1 << 30;
+  for (int run = levels < 8 ? levels : 8; run >= 5; --run) {
     const int rounds = (levels + SEG * run - 1) / (SEG * run);
     if (rounds * run < best_slots) {
       best = run;
@@ -342,8 +359,9 @@ int srh_seg_run(int levels) {
 }
 
 cudaError_t launch_srh_seg(const SrhArgs &a, cudaStream_t s) {
-  if (a.n2 <= 0) return cudaSuccess;
   const int run = srh_seg_run(a.nk);
+  if (run == 0) return cudaErrorInvalidValue;  // the caller checks srh_seg_run first
+  if (a.n2 <= 0) return cudaSuccess;
   return a.grid == 1 ? launch_seg_g<1>(a, run, s) : launch_seg_g<2>(a, run, s);
 }
 

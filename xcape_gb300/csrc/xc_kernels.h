@@ -109,7 +109,7 @@ struct SrhArgs {
 
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
 // The FP32 level-parallel kernel for float inputs (srh_seg.cu), and its run
-// length for a column of `levels` levels above the surface.
+// length for nk input levels (0: fewer than 5 levels, which it does not take).
 cudaError_t launch_srh_seg(const SrhArgs &a, cudaStream_t s);
 int srh_seg_run(int levels);
 // CAPE (guess 0 or 1) and SRH of the same columns in one kernel (cape_srh.cu).
