@@ -465,6 +465,16 @@ int xc_batch_work(xc_batch *b, long long *substeps, long long *iterations);
 /* Waits for the executor's runs and frees it (NULL is a no-op). */
 int xc_batch_destroy(xc_batch *b);
 
+/* Queues n copies on `stream` in order, dst[k] <- src[k] of bytes[k] bytes,
+ * one cudaMemcpyAsync each with the direction taken from the pointers
+ * (unified addressing): the inputs of a service loop's batch into its
+ * device arena, or its results back, in one call from the host language
+ * instead of one call per array.  Copies from or to pinned host memory are
+ * asynchronous; the caller keeps the buffers alive and unchanged until the
+ * stream has passed them.  Zero-byte entries are skipped. */
+int xc_copy_list(int n, void *const *dst, const void *const *src,
+                 const unsigned long long *bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -127,3 +127,40 @@ def test_server_pinned_row_views_with_a_leading_dimension():
     for (ra, xa), (rb, xb) in zip(a, b):
         for u, v in zip(xa, xb):
             np.testing.assert_array_equal(u, v)
+
+
+def test_copy_list_round_trip():
+    """xc_copy_list: pinned and pageable host arrays to the device and back
+    in one call each, zero-byte entries skipped, a NULL pointer refused."""
+    torch = torch_cuda()
+    from xcape_gb300 import _lib
+    L = _lib.lib()
+    rng = np.random.default_rng(1)
+    sizes = [0, 4, 1000, 1 << 20, 3 << 20]
+    pinned = [torch.from_numpy(rng.integers(0, 255, n, dtype=np.uint8)).pin_memory()
+              for n in sizes]
+    host = [rng.integers(0, 255, n, dtype=np.uint8) for n in sizes]
+    dev = [torch.empty(2 * n, dtype=torch.uint8, device="cuda") for n in sizes]
+    s = torch.cuda.current_stream()
+    ptrs = []
+    for p, h, d, n in zip(pinned, host, dev, sizes):
+        ptrs.append((d.data_ptr(), p.data_ptr(), n))
+        ptrs.append((d.data_ptr() + n, h.ctypes.data, n))
+    c = np.array(ptrs, dtype=np.uint64)
+    dst, src, nb = (np.ascontiguousarray(c[:, k]) for k in range(3))
+    _lib.check(L.xc_copy_list(len(ptrs), dst.ctypes.data, src.ctypes.data, nb.ctypes.data,
+                              s.cuda_stream))
+    back = [torch.empty(2 * n, dtype=torch.uint8).pin_memory() for n in sizes]
+    c = np.array([(b.data_ptr(), d.data_ptr(), 2 * n) for b, d, n in zip(back, dev, sizes)],
+                 dtype=np.uint64)
+    dst, src, nb = (np.ascontiguousarray(c[:, k]) for k in range(3))
+    _lib.check(L.xc_copy_list(len(sizes), dst.ctypes.data, src.ctypes.data, nb.ctypes.data,
+                              s.cuda_stream))
+    s.synchronize()
+    for p, h, b, n in zip(pinned, host, back, sizes):
+        np.testing.assert_array_equal(b.numpy()[:n], p.numpy())
+        np.testing.assert_array_equal(b.numpy()[n:], h)
+    bad = np.array([0], dtype=np.uint64)
+    one = np.array([4], dtype=np.uint64)
+    assert L.xc_copy_list(1, bad.ctypes.data, bad.ctypes.data, one.ctypes.data,
+                          s.cuda_stream) != 0

@@ -85,6 +85,7 @@ SIGNATURES = {
     "xc_batch_run": [_vp, _vp, _i, _vp],
     "xc_batch_work": [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "xc_batch_destroy": [_vp],
+    "xc_copy_list": [_i, _vp, _vp, _vp, _vp],
 }
 
 XC_BATCH_MAX_REQUESTS = 65536

@@ -389,4 +389,18 @@ int xc_batch_destroy(xc_batch *b) {
   return XC_OK;
 }
 
+int xc_copy_list(int n, void *const *dst, const void *const *src,
+                 const unsigned long long *bytes, void *stream) {
+  if (n < 0 || (n > 0 && (!dst || !src || !bytes)))
+    return xc::set_error(XC_ERR_INVALID, "xc_copy_list: n < 0 or NULL arrays");
+  for (int k = 0; k < n; ++k) {
+    if (bytes[k] == 0) continue;
+    if (!dst[k] || !src[k]) return xc::set_error(XC_ERR_INVALID, "xc_copy_list: NULL pointer");
+    const cudaError_t e =
+        cudaMemcpyAsync(dst[k], src[k], (size_t)bytes[k], cudaMemcpyDefault, (cudaStream_t)stream);
+    if (e != cudaSuccess) return xc::set_error(XC_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return XC_OK;
+}
+
 }  // extern "C"

@@ -332,218 +332,18 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
   seg_finish<GRID>(a, i, active, mono, ktop, A, utop, vtop, us, vs, slot_u[cb], slot_v[cb]);
 }
 
-// The same sweep with the block's 16 columns staged in shared memory first
-// (srh_seg_tile_kernel): their rows of every input array are one contiguous
-// range, which the block reads with coalesced 16-byte loads (scalar loads
-// where an array is not 16-byte aligned), computing each level's C Tv on the
-// way, into a tile of (P, C Tv, u, v) per level, column after column.  A
-// lane then reads each level of its run with one 16-byte shared load, the
-// level below its first one included (the surface for the first lane of the
-// first round); reads past a column's top fall in the next column's row or
-// in the tile's end padding and are masked.  The run length is odd, so the
-// eight lanes of a segment read distinct 16-byte bank groups.  Without the
-// staging every lane's loads touch their own sectors, and L1 throughput,
-// not DRAM, bounds the sweep.
-constexpr int TILE_COLS = SEG_THREADS / SEG;
-
-__host__ __device__ inline int seg_tile_levels(int nk, int run) {
-  return 1 + TILE_COLS * nk + SEG * run;  // the level below the first, the rows, the padding
-}
-
-template <int GRID, int RUN>
-__global__ void __launch_bounds__(SEG_THREADS, 7) srh_seg_tile_kernel(SrhArgs a) {
-  constexpr unsigned FULL = 0xffffffffu;
-  constexpr int ROUND = SEG * RUN;
-  extern __shared__ float4 tile[];
-  __shared__ float slot_u[TILE_COLS][12], slot_v[TILE_COLS][12];
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const int sl = lane & (SEG - 1);
-  const unsigned seg_mask = 0xffu << (lane & ~(SEG - 1));
-  const int cb = tid / SEG;
-  const long long i0 = (long long)blockIdx.x * TILE_COLS;
-  const long long i = i0 + cb;
-  const bool active = i < a.n2;
-  const long long ic = active ? i : a.n2 - 1;
-  const int nk = a.nk;
-  const float *gp = (const float *)a.p, *gt = (const float *)a.t, *gtd = (const float *)a.td;
-  const float *gu = (const float *)a.u, *gv = (const float *)a.v;
-  // stage the block's rows: elements e = col * nk + m of its tile, the
-  // global element i0 * nk + e of every array
-  {
-    const long long g0 = i0 * nk;
-    const int ne = (int)min((long long)TILE_COLS * nk, a.n2 * nk - g0);
-    float4 *rows = tile + 1;
-    const bool vec = ((((uintptr_t)(gt + g0) | (uintptr_t)(gtd + g0) | (uintptr_t)(gu + g0) |
-                        (uintptr_t)(gv + g0) | (GRID == 1 ? (uintptr_t)(gp + g0) : 0)) & 15) == 0);
-    int done = 0;
-    if (vec) {
-      const int nq = ne >> 2;
-      for (int q = tid; q < nq; q += SEG_THREADS) {
-        const float4 t4 = __ldg(reinterpret_cast<const float4 *>(gt + g0) + q);
-        const float4 d4 = __ldg(reinterpret_cast<const float4 *>(gtd + g0) + q);
-        const float4 u4 = __ldg(reinterpret_cast<const float4 *>(gu + g0) + q);
-        const float4 v4 = __ldg(reinterpret_cast<const float4 *>(gv + g0) + q);
-        float4 p4;
-        if (GRID == 1) {
-          p4 = __ldg(reinterpret_cast<const float4 *>(gp + g0) + q);
-        } else {
-          int m = (4 * q) % nk;
-          p4.x = __ldg(gp + m);
-          m = m + 1 == nk ? 0 : m + 1;
-          p4.y = __ldg(gp + m);
-          m = m + 1 == nk ? 0 : m + 1;
-          p4.z = __ldg(gp + m);
-          m = m + 1 == nk ? 0 : m + 1;
-          p4.w = __ldg(gp + m);
-        }
-        const int e = 4 * q;
-        rows[e] = make_float4(p4.x, seg_ctv(p4.x, t4.x, d4.x), u4.x, v4.x);
-        rows[e + 1] = make_float4(p4.y, seg_ctv(p4.y, t4.y, d4.y), u4.y, v4.y);
-        rows[e + 2] = make_float4(p4.z, seg_ctv(p4.z, t4.z, d4.z), u4.z, v4.z);
-        rows[e + 3] = make_float4(p4.w, seg_ctv(p4.w, t4.w, d4.w), u4.w, v4.w);
-      }
-      done = nq << 2;
-    }
-    for (int e = done + tid; e < ne; e += SEG_THREADS) {
-      const float P = __ldg(GRID == 1 ? gp + g0 + e : gp + e % nk);
-      rows[e] = make_float4(P, seg_ctv(P, __ldg(gt + g0 + e), __ldg(gtd + g0 + e)),
-                            __ldg(gu + g0 + e), __ldg(gv + g0 + e));
-    }
-    // the element before the first row and the padding are read, never used
-    for (int e = tid; e < 1 + SEG * RUN + TILE_COLS * nk - ne; e += SEG_THREADS)
-      tile[e == 0 ? 0 : ne + e] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
-  }
-  const float ps = __ldg((const float *)a.ps + ic), ts = __ldg((const float *)a.ts + ic);
-  const float tds = __ldg((const float *)a.tds + ic);
-  const float us = __ldg((const float *)a.us + ic), vs = __ldg((const float *)a.vs + ic);
-  int st = 1;
-  if (GRID == 2) {
-    st = a.start ? __ldg(a.start + ic) : pres_lev_pos_col<float>(gp, ps, nk);
-    st = st < 1 ? 1 : (st > nk + 1 ? nk + 1 : st);
-  }
-  const int ncl = nk - st + 2;  // assembled levels: 1 (surface) .. ncl
-  for (int k = sl; k < 24; k += SEG) {
-    if (k < 12) slot_u[cb][k] = VMSG;
-    else slot_v[cb][k - 12] = VMSG;
-  }
-  __syncthreads();
-  const float4 *col = tile + 1 + cb * nk + (st - 1);  // level j (1-based, 2 .. ncl) at col[j - 2]
-  const float depth = (float)a.depth;
-  const float4 sfc = make_float4(ps, seg_ctv(ps, ts, tds), us, vs);
-  float Hc = (float)a.aglh0;  // height of the level below the round
-  bool mono = true;
-  int ktop = 0;
-  float utop = 0.0f, vtop = 0.0f, A = 0.0f;
-  const int nrounds = active ? (ncl - 1 + ROUND - 1) / ROUND : 0;
-  const int wrounds = __reduce_max_sync(FULL, nrounds);
-  for (int r = 0; r < wrounds; ++r) {
-    const int k0 = r < nrounds ? r * ROUND + sl * RUN : 0;  // this lane's first level - 2
-    int nv = r < nrounds ? ncl - 1 - k0 : 0;  // valid levels of the run
-    nv = nv < 0 ? 0 : (nv > RUN ? RUN : nv);
-    const float4 *run = col + k0;
-    float4 b = run[-1];  // the level below the run
-    if (r == 0 && sl == 0) b = sfc;
-    float u[RUN], v[RUN], z[RUN];
-    float s = 0.0f;
-    float Pp = b.x, Cp = b.y;
-#pragma unroll
-    for (int c = 0; c < RUN; ++c) {
-      const float4 q = run[c];
-      u[c] = q.z;
-      v[c] = q.w;
-      const float dz = (q.y + Cp) * lg2_a(Pp * rcp_a(q.x));
-      const bool ok = c < nv;
-      mono = mono && (!ok || dz > 0.0f);
-      s += ok ? dz : 0.0f;
-      z[c] = s;
-      Pp = q.x;
-      Cp = q.y;
-    }
-    // heights: the exclusive scan of the lanes' run totals
-    float x = s;
-#pragma unroll
-    for (int d = 1; d < SEG; d <<= 1) {
-      const float y = __shfl_up_sync(FULL, x, d, SEG);
-      if (sl >= d) x += y;
-    }
-    float ex = __shfl_up_sync(FULL, x, 1, SEG);
-    if (sl == 0) ex = 0.0f;
-    const float below = Hc + ex;  // height of the level below the run
-#pragma unroll
-    for (int c = 0; c < RUN; ++c) z[c] = below + z[c];
-    // Bunkers targets of each layer, and the levels at or below depth
-    int ka = seg_below(below);
-    int nle = 0;
-    float za = below, ua = b.z, va = b.w;
-#pragma unroll
-    for (int c = 0; c < RUN; ++c) {
-      const float zb = z[c];
-      const int kb = seg_below(zb);
-      for (int k = ka; k < kb; ++k) {
-        const float w = (500.0f * (float)(k + 1) - za) * rcp_a(zb - za);
-        slot_u[cb][k] = fmaf(w, u[c] - ua, ua);
-        slot_v[cb][k] = fmaf(w, v[c] - va, va);
-      }
-      nle += (c < nv && zb <= depth) ? 1 : 0;
-      ka = kb;
-      za = zb;
-      ua = u[c];
-      va = v[c];
-    }
-    // the lane holding the first level above depth (the lowest such lane in
-    // the first round that has one), and the helicity terms below it
-    const unsigned cm = __ballot_sync(FULL, ktop == 0 && nle < nv) & seg_mask;
-    const int fl = cm ? (__ffs(cm) - 1) & (SEG - 1) : SEG;
-    const int lim = (ktop != 0 || sl > fl) ? 0 : (sl < fl ? nv : nle);
-    float zl = below, zh = 0.0f;
-    ua = b.z;
-    va = b.w;
-#pragma unroll
-    for (int c = 0; c < RUN; ++c) {
-      if (c < lim) A = fmaf(ua, v[c], fmaf(-u[c], va, A));
-      if (c == nle - 1) zl = z[c];
-      if (c == nle) zh = z[c];
-      ua = u[c];
-      va = v[c];
-    }
-    if (ktop == 0 && sl == fl) {
-      // INTERP1 with X1 = aglh(ktop), X3 = aglh(ktop-1): X3 < X1 for
-      // increasing heights, so its X3 == X1 adjustment never applies here
-      const float4 qh = run[nle], ql = nle > 0 ? run[nle - 1] : b;
-      const float w = (depth - zh) * rcp_a(zl - zh);
-      utop = fmaf(ql.z - qh.z, w, qh.z);
-      vtop = fmaf(ql.w - qh.w, w, qh.w);
-      A = fmaf(ql.z, vtop, fmaf(-utop, ql.w, A));
-    }
-    if (cm) ktop = 1;  // found (its index itself is not needed)
-    Hc = __shfl_sync(FULL, z[RUN - 1], SEG - 1, SEG);  // for the next round's first lane
-  }
-  seg_finish<GRID>(a, i, active, mono, ktop, A, utop, vtop, us, vs, slot_u[cb], slot_v[cb]);
-}
-
 namespace {
-
-constexpr size_t SEG_TILE_SMEM_MAX = 46 * 1024;  // with the static slots, under 48 KB
 
 template <int GRID, int RUN>
 cudaError_t launch_seg(const SrhArgs &a, cudaStream_t s) {
-  const unsigned blocks = (unsigned)((a.n2 + TILE_COLS - 1) / TILE_COLS);
+  constexpr long long cols = SEG_THREADS / SEG;
+  const unsigned blocks = (unsigned)((a.n2 + cols - 1) / cols);
   srh_seg_kernel<GRID, RUN><<<blocks, SEG_THREADS, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-template <int GRID, int RUN>
-cudaError_t launch_seg_tile(const SrhArgs &a, cudaStream_t s) {
-  const unsigned blocks = (unsigned)((a.n2 + TILE_COLS - 1) / TILE_COLS);
-  const size_t smem = sizeof(float4) * (size_t)seg_tile_levels(a.nk, RUN);
-  srh_seg_tile_kernel<GRID, RUN><<<blocks, SEG_THREADS, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
 template <int GRID>
-cudaError_t launch_seg_g(const SrhArgs &a, int run, bool tiled, cudaStream_t s) {
-  if (tiled) return run == 5 ? launch_seg_tile<GRID, 5>(a, s) : launch_seg_tile<GRID, 7>(a, s);
+cudaError_t launch_seg_g(const SrhArgs &a, int run, cudaStream_t s) {
   switch (run) {
     case 5: return launch_seg<GRID, 5>(a, s);
     case 6: return launch_seg<GRID, 6>(a, s);
@@ -552,45 +352,30 @@ cudaError_t launch_seg_g(const SrhArgs &a, int run, bool tiled, cudaStream_t s) 
   }
 }
 
-// The fewest level slots rounds * RUN over the given run lengths, the
-// longer run on a tie (fewer rounds).
-int fewest_slots(int levels, const int *runs, int n) {
-  int best = runs[0], best_slots = 1 << 30;
-  for (int k = 0; k < n; ++k) {
-    const int rounds = (levels + SEG * runs[k] - 1) / (SEG * runs[k]);
-    if (rounds * runs[k] < best_slots || (rounds * runs[k] == best_slots && runs[k] > best)) {
-      best = runs[k];
-      best_slots = rounds * runs[k];
+}  // namespace
+
+// The run length for columns of nk input levels: the fewest level slots
+// rounds * RUN over RUN = 5..min(8, nk), the longer run on a tie (fewer
+// rounds); 0 (the column kernel serves) below 5 levels.  50 levels take one
+// round of 8 x 7, 37 one of 8 x 5, 137 three of 8 x 6.
+int srh_seg_run(int levels) {
+  if (levels < 5) return 0;
+  int best = 5, best_slots = 1 << 30;
+  for (int run = levels < 8 ? levels : 8; run >= 5; --run) {
+    const int rounds = (levels + SEG * run - 1) / (SEG * run);
+    if (rounds * run < best_slots) {
+      best = run;
+      best_slots = rounds * run;
     }
   }
   return best;
-}
-
-bool seg_tile_fits(int nk) {
-  return sizeof(float4) * (size_t)seg_tile_levels(nk, 7) <= SEG_TILE_SMEM_MAX;
-}
-
-}  // namespace
-
-// The run length for columns of nk input levels.  The staged kernel takes
-// odd runs (5 or 7: conflict-free shared loads): 50 levels take one round of
-// 8 x 7, 37 one of 8 x 5, 137 four of 8 x 5.  Without the tile (nk above
-// 180), runs of 5 to 8 levels: 200 levels take four rounds of 8 x 7.  0: the
-// level-parallel kernels do not take the columns (no tile and fewer than 5
-// levels, which cannot happen with the tile's limit).
-int srh_seg_run(int nk) {
-  static const int odd[2] = {5, 7}, all[4] = {5, 6, 7, 8};
-  if (nk < 1) return 0;
-  if (seg_tile_fits(nk)) return fewest_slots(nk, odd, 2);
-  return nk < 8 ? 0 : fewest_slots(nk, all, 4);
 }
 
 cudaError_t launch_srh_seg(const SrhArgs &a, cudaStream_t s) {
   const int run = srh_seg_run(a.nk);
   if (run == 0) return cudaErrorInvalidValue;  // the caller checks srh_seg_run first
   if (a.n2 <= 0) return cudaSuccess;
-  const bool tiled = seg_tile_fits(a.nk);
-  return a.grid == 1 ? launch_seg_g<1>(a, run, tiled, s) : launch_seg_g<2>(a, run, tiled, s);
+  return a.grid == 1 ? launch_seg_g<1>(a, run, s) : launch_seg_g<2>(a, run, s);
 }
 
 }  // namespace xc

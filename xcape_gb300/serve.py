@@ -6,7 +6,8 @@ launch per batch).
 ``CapeServer`` keeps two device arenas and two pinned staging areas.  A
 batch is admitted into the free arena (requests are taken in arrival order
 while their inputs and outputs fit), its inputs are copied host -> pinned ->
-device on a copy stream, the executor runs it on a compute stream once the
+device on a copy stream (one library call queues all of a batch's copies,
+xc_copy_list), the executor runs it on a compute stream once the
 copies are in, and its outputs (cape, cin, mulvl, z_out) go back to pinned
 memory on the same stream.  ``launch`` only queues that work; ``finish``
 waits for a batch and hands out each request's results.  A loop that
@@ -68,6 +69,7 @@ class Request:
             raise ValueError("surface arrays must have one value per column")
         self.source, self.adiabat, self.vertical_lev = source, adiabat, vertical_lev
         self.pinc, self.ml_depth, self.tag = pinc, ml_depth, tag
+        self.pinned = tuple(_pinned(a) for a in self.inputs())
 
     def inputs(self):
         return (self.p, self.t, self.td, self.ps, self.ts, self.tds)
@@ -79,13 +81,25 @@ class Request:
     def staging_bytes(self):
         """Pinned staging bytes of the request: its pageable inputs and the
         four outputs."""
-        return sum(_nbytes(a.nbytes) for a in self.inputs() if not _pinned(a)) + \
+        return sum(_nbytes(a.nbytes) for a, pin in zip(self.inputs(), self.pinned) if not pin) + \
             4 * _nbytes(4 * self.n2)
 
 
 def _pinned(a):
     import torch
     return torch.from_numpy(a.reshape(-1).view(np.uint8)).is_pinned()
+
+
+def _copy_list(copies, stream):
+    """Queues [(dst pointer, src pointer, bytes)] on `stream` with one
+    library call (xc_copy_list: one cudaMemcpyAsync per entry)."""
+    from . import _lib
+    if not copies:
+        return
+    c = np.array(copies, dtype=np.uint64).reshape(-1, 3)
+    dst, src, nb = (np.ascontiguousarray(c[:, k]) for k in range(3))
+    _lib.check(_lib.lib().xc_copy_list(len(copies), dst.ctypes.data, src.ctypes.data,
+                                       nb.ctypes.data, stream.cuda_stream))
 
 
 class _Batch:
@@ -159,19 +173,21 @@ class CapeServer:
             raise RuntimeError("the arena still holds an unfinished batch: finish it first")
         arena, stage = self.arena[k], self.staging[k]
         st = stage.numpy()
+        arena_ptr, stage_ptr = arena.data_ptr(), stage.data_ptr()
         off = soff = 0  # arena and staging offsets
         views = []
-        copies = []  # (arena offset, host tensor) of the inputs
+        copies = []  # (device pointer, host pointer, bytes) of the inputs
 
-        def place(a):
+        def place(a, pinned):
             nonlocal off, soff
             n = a.nbytes
-            h = torch.from_numpy(a.reshape(-1).view(np.uint8))
-            if not h.is_pinned():  # pageable: through the staging
+            if pinned:
+                src = a.ctypes.data
+            else:  # pageable: through the staging
                 st[soff:soff + n] = a.reshape(-1).view(np.uint8)
-                h = stage[soff:soff + n]
+                src = stage_ptr + soff
                 soff += _nbytes(n)
-            copies.append((off, h))
+            copies.append((arena_ptr + off, src, n))
             v = (off, n)
             off += _nbytes(n)
             return v
@@ -183,17 +199,16 @@ class CapeServer:
             soff += _nbytes(n)
             return v
         for r in reqs:
-            v = dict(zip(("p", "t", "td", "ps", "ts", "tds"), (place(a) for a in r.inputs())))
+            v = dict(zip(("p", "t", "td", "ps", "ts", "tds"),
+                         (place(a, pin) for a, pin in zip(r.inputs(), r.pinned))))
             for name in ("cape", "cin", "mulvl", "z_out"):
                 v[name] = alloc(4 * r.n2)
             views.append(v)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         copied = ev[1]
-        with torch.cuda.stream(self.copy_stream):
-            ev[0].record(self.copy_stream)
-            for o, h in copies:
-                arena[o:o + h.numel()].copy_(h, non_blocking=True)
-            copied.record(self.copy_stream)
+        ev[0].record(self.copy_stream)
+        _copy_list(copies, self.copy_stream)
+        copied.record(self.copy_stream)
 
         def dev(view, dtype, shape):
             o, n = view[0], view[1]
@@ -224,13 +239,12 @@ class CapeServer:
             ev[2].record(self.compute_stream)
             # the outputs back into the staging (the inputs staged there have
             # been copied: the compute stream waited for the copies)
-            for v in views:
-                for name in ("cape", "cin", "mulvl", "z_out"):
-                    o, n, so = v[name]
-                    stage[so:so + n].copy_(arena[o:o + n], non_blocking=True)
+            _copy_list([(stage_ptr + v[name][2], arena_ptr + v[name][0], v[name][1])
+                        for v in views for name in ("cape", "cin", "mulvl", "z_out")],
+                       self.compute_stream)
             done.record(self.compute_stream)
         b = _Batch(k, reqs, views, ev)
-        b.h2d_bytes = sum(h.numel() for _, h in copies)
+        b.h2d_bytes = sum(n for _, _, n in copies)
         self.busy[k] = b
         return b
 
