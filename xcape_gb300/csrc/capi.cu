@@ -53,10 +53,21 @@ int check_cape_opts(float pinc, int source, float ml_depth, int adiabat) {
 }
 
 // Columns per chunk of the pipelined host path: at least this many, at most
-// HOST_CHUNKS chunks; the chunks' device buffers (a ring of slots) take at
-// most host_ring_bytes(), and at least two slots.
+// host_chunks() chunks (HOST_CHUNKS at most); the chunks' device buffers (a
+// ring of slots) take at most host_ring_bytes(), and at least two slots.
 constexpr int HOST_CHUNK_MIN = 131072;
-constexpr int HOST_CHUNKS = 8;
+constexpr int HOST_CHUNKS = 16;
+
+// 8, or the environment's XC_HOST_CHUNKS (2..16; it changes only how the
+// work is pipelined, never a result).
+int host_chunks() {
+  const char *e = getenv("XC_HOST_CHUNKS");
+  if (e && *e) {
+    const int v = atoi(e);
+    if (v >= 2 && v <= HOST_CHUNKS) return v;
+  }
+  return 8;
+}
 
 // 4 GiB, or the environment's XC_HOST_RING_BYTES (it changes only how
 // many chunks are in flight, never a result).
@@ -456,7 +467,7 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
   if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
     return fail(XC_ERR_INVALID, "NULL array argument");
   int nchunk = (n2 + HOST_CHUNK_MIN - 1) / HOST_CHUNK_MIN;
-  if (nchunk > HOST_CHUNKS) nchunk = HOST_CHUNKS;
+  if (nchunk > host_chunks()) nchunk = host_chunks();
   // Chunk c holds columns [bound[c], bound[c + 1]).  With three or more
   // chunks the first and the last are half-size: the first lift starts
   // after a shorter copy, and less work is left after the last copy.
