@@ -365,9 +365,19 @@ int xc_guess_pairs(long long n, unsigned long long seed, float *feats, float *ta
                    void *stream);
 
 /* Adds the gradient of the mean squared error over the n pairs to grad
- * [XC_GUESS_NPARAM] and the loss to *loss (both must be zeroed first). */
+ * [XC_GUESS_NPARAM] and the loss to *loss (both must be zeroed first).  The
+ * three 64-wide products run on the tensor cores with mma.sync (BF16
+ * operands, FP32 accumulation). */
 int xc_guess_grad(const float *weights, const float *feats, const float *targets, long long n,
                   float *grad, float *loss, void *stream);
+
+/* xc_guess_grad with the three products on the 5th-generation tensor cores
+ * (tcgen05.mma, BF16 operands in shared memory, FP32 accumulators in tensor
+ * memory; dW2 stays in tensor memory over a block's tiles).  status: a
+ * device int (may be NULL) set to 1 if a wait for the tensor cores ran out,
+ * in which case grad and loss are incomplete; the caller zeroes it. */
+int xc_guess_grad_tc(const float *weights, const float *feats, const float *targets,
+                     long long n, float *grad, float *loss, int *status, void *stream);
 
 /* One Adam step (step >= 1) on the FP32 weights; zeroes grad. */
 int xc_guess_adam(float *weights, float *grad, float *m, float *v, float lr, int step,

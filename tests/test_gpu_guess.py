@@ -35,6 +35,13 @@ def pairs():
     return f.cpu().numpy(), t.cpu().numpy(), it.cpu().numpy()
 
 
+@pytest.fixture(scope="module")
+def many_pairs():
+    torch_cuda()
+    f, t, it = G.make_pairs(65536, seed=321)
+    return f.cpu().numpy(), t.cpu().numpy(), it.cpu().numpy()
+
+
 def test_pairs_over_the_state_box(pairs):
     """The GPU's pairs (four adiabats, p 100..1050 hPa, T -80..40 degC):
     the plain iteration solves every atmospheric one (theta-e below 380 K)
@@ -68,11 +75,16 @@ def test_pairs_match_host_build(pairs):
     assert np.mean(np.abs(it[both] - ith[both]) <= 1) > 0.98
 
 
-def test_training_gradient_matches_fp64_reference(pairs):
-    f, t, _ = pairs
-    n = 300  # two full blocks and a partial one
+@pytest.mark.parametrize("kernel", G.KERNELS)
+@pytest.mark.parametrize("n", [300, 50_000])
+def test_training_gradient_matches_fp64_reference(many_pairs, kernel, n):
+    """300 pairs: two full tiles of 128 and a partial one; 50,000: 391
+    tiles over one block per SM, so each block of the tcgen05 kernel adds
+    two or three tiles' dW2 in its tensor memory before writing it out."""
+    f, t, _ = many_pairs
+    assert len(t) >= n
     w = G.init_weights(11, float(t[:n].mean()))
-    g_gpu, loss_gpu = G.gradient(w, f[:n], t[:n])
+    g_gpu, loss_gpu = G.gradient(w, f[:n], t[:n], kernel=kernel)
     loss_ref, g_ref = loss_and_grad(w, f[:n], t[:n])
     assert abs(loss_gpu - loss_ref) <= 1e-4 * loss_ref + 1e-7
     scale = np.max(np.abs(g_ref))
@@ -80,6 +92,17 @@ def test_training_gradient_matches_fp64_reference(pairs):
     # and the direction is right: a small step along -grad lowers the loss
     w2 = w - 1e-3 * g_gpu / np.linalg.norm(g_gpu)
     assert loss_and_grad(w2, f[:n], t[:n])[0] < loss_ref
+
+
+def test_training_kernels_agree(many_pairs):
+    """The tcgen05 and mma.sync gradients of the same batch: the same BF16
+    operands with FP32 accumulation, summed in other orders."""
+    f, t, _ = many_pairs
+    w = G.init_weights(5, float(t[:20000].mean()))
+    g_tc, l_tc = G.gradient(w, f[:20000], t[:20000], kernel="tcgen05")
+    g_mma, l_mma = G.gradient(w, f[:20000], t[:20000], kernel="mma")
+    assert abs(l_tc - l_mma) <= 1e-5 * l_mma
+    np.testing.assert_allclose(g_tc, g_mma, rtol=1e-3, atol=1e-5 * np.max(np.abs(g_mma)))
 
 
 def test_tensor_core_inference_matches_reference(pairs):

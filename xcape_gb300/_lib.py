@@ -77,6 +77,7 @@ SIGNATURES = {
     "xc_guess_set_weights": [_vp, _i, _vp],
     "xc_guess_pairs": [ctypes.c_longlong, ctypes.c_ulonglong, _vp, _vp, _vp, _vp],
     "xc_guess_grad": [_vp, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp],
+    "xc_guess_grad_tc": [_vp, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp, _vp],
     "xc_guess_adam": [_vp, _vp, _vp, _vp, _f, _i, _vp],
     "xc_guess_eval": [_vp, _vp, ctypes.c_longlong, _vp, _vp],
     "xc_release_workspace": [],

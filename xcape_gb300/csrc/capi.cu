@@ -81,6 +81,20 @@ size_t host_ring_bytes() {
   return (size_t)4 << 30;
 }
 
+// Compute streams the host path's chunks take in turn: 4, or the
+// environment's XC_HOST_STREAMS (1..4; it changes only how the work overlaps
+// on the GPU, never a result).  With more launches in flight, the tails of
+// the chunks' lifts overlap: 1 stream 174, 2 streams 242, 4 streams 248 M
+// columns/s end to end on 1M columns x 37 levels, two sources.
+int host_streams() {
+  const char *e = getenv("XC_HOST_STREAMS");
+  if (e && *e) {
+    const int v = atoi(e);
+    if (v >= 1 && v <= 4) return v;
+  }
+  return 4;
+}
+
 // Host calls in flight at once on one device: 4, or the environment's
 // XC_HOST_CONTEXTS (1..64).  Calls beyond that wait for a context.
 int host_contexts() {
@@ -103,7 +117,7 @@ int host_contexts() {
 struct HostCtx {
   int dev = -1;
   bool busy = false;
-  cudaStream_t s[2] = {nullptr, nullptr};  // kernels and output copies, alternating
+  cudaStream_t s[4] = {};  // kernels and output copies, chunks in turn over host_streams()
   cudaStream_t copy = nullptr;             // input copies, in chunk order
   cudaEvent_t start = nullptr;
   cudaEvent_t loaded[HOST_CHUNKS] = {};    // slot k holds its chunk's inputs
@@ -150,7 +164,7 @@ struct HostCtxLease {
         g_ctx_cv.wait(lk);
       }
     }
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
       if (!c->s[k]) e = cudaStreamCreateWithFlags(&c->s[k], cudaStreamNonBlocking);
     if (e == cudaSuccess && !c->copy) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
     for (int k = 0; k < HOST_CHUNKS && e == cudaSuccess; ++k) {
@@ -548,7 +562,9 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
     return XC_OK;
   };
   cudaError_t e = cudaEventRecord(pl->start, (cudaStream_t)stream);
-  for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(pl->s[k], pl->start, 0);
+  const int nstream = host_streams();
+  for (int k = 0; k < nstream && e == cudaSuccess; ++k)
+    e = cudaStreamWaitEvent(pl->s[k], pl->start, 0);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->copy, pl->start, 0);
   if (e != cudaSuccess) return cuda_fail(e, "ordering the host path after the caller's stream");
   const char *hp = (const char *)p, *ht = (const char *)t3d, *htd = (const char *)td3d;
@@ -565,7 +581,7 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
       if (rc) return rc;
     }
     const Slot &q = sl[k];
-    cudaStream_t s = pl->s[c & 1];
+    cudaStream_t s = pl->s[c % nstream];
     const size_t r3 = (size_t)nc * nk * es, off3 = (size_t)c0 * nk * es, off1 = (size_t)c0 * es;
 #define H2D(off, src, bytes)                                                         \
     if (e == cudaSuccess)                                                            \
@@ -1026,6 +1042,16 @@ int xc_guess_grad(const float *weights, const float *feats, const float *targets
   cudaError_t e = xc::launch_guess_grad(weights, feats, targets, 0, n, grad, loss,
                                         (cudaStream_t)stream);
   return e == cudaSuccess ? XC_OK : cuda_fail(e, "guess training kernel launch");
+}
+
+int xc_guess_grad_tc(const float *weights, const float *feats, const float *targets,
+                     long long n, float *grad, float *loss, int *status, void *stream) {
+  if (n < 0) return fail(XC_ERR_INVALID, "n is negative");
+  if (n > 0 && (!weights || !feats || !targets || !grad || !loss))
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  cudaError_t e = xc::launch_guess_grad_tc(weights, feats, targets, 0, n, grad, loss, status,
+                                           (cudaStream_t)stream);
+  return e == cudaSuccess ? XC_OK : cuda_fail(e, "guess training kernel (tcgen05) launch");
 }
 
 int xc_guess_adam(float *weights, float *grad, float *m, float *v, float lr, int step,

@@ -35,6 +35,11 @@ cudaError_t launch_guess_pairs(long long n, unsigned long long seed, float *feat
 cudaError_t launch_guess_grad(const float *w, const float *feats, const float *targets,
                               long long batch0, long long nb, float *grad, float *loss,
                               cudaStream_t s);
+// The same gradient with the three products on tcgen05 (guess_train_tc_kernel);
+// *status (device, may be NULL) is set to 1 if a tensor-core wait ran out.
+cudaError_t launch_guess_grad_tc(const float *w, const float *feats, const float *targets,
+                                 long long batch0, long long nb, float *grad, float *loss,
+                                 int *status, cudaStream_t s);
 cudaError_t launch_guess_adam(float *w, float *grad, float *m, float *v, float lr, int step,
                               cudaStream_t s);
 cudaError_t launch_guess_eval(const float *w, const float *feats, long long n, float *out,

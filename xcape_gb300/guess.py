@@ -80,7 +80,21 @@ def make_pairs(n, seed=1):
     return f, t, it
 
 
-def gradient(weights, feats, targets):
+# training kernels: the products on tcgen05 (5th-generation tensor cores,
+# accumulators in tensor memory) or on mma.sync
+KERNELS = ("tcgen05", "mma")
+
+
+def _grad_call(kernel, w, f, t, n, g, loss, status, stream):
+    if kernel == "tcgen05":
+        _lib.call("xc_guess_grad_tc", w, f, t, n, g, loss, status, stream)
+    elif kernel == "mma":
+        _lib.call("xc_guess_grad", w, f, t, n, g, loss, stream)
+    else:
+        raise ValueError(f"kernel must be one of {KERNELS}")
+
+
+def gradient(weights, feats, targets, kernel="tcgen05"):
     """(grad [NPARAM], loss) of the mean squared error, on the GPU."""
     torch = _torch()
     w = torch.as_tensor(np.asarray(weights, np.float32)).cuda()
@@ -88,9 +102,12 @@ def gradient(weights, feats, targets):
     t = torch.as_tensor(np.asarray(targets, np.float32)).cuda().contiguous()
     g = torch.zeros(NPARAM, dtype=torch.float32, device="cuda")
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
-    _lib.call("xc_guess_grad", w.data_ptr(), f.data_ptr(), t.data_ptr(), t.numel(), g.data_ptr(),
-              loss.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _grad_call(kernel, w.data_ptr(), f.data_ptr(), t.data_ptr(), t.numel(), g.data_ptr(),
+               loss.data_ptr(), status.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
+    if int(status.item()):
+        raise RuntimeError("the tensor-core training kernel gave up waiting for its products")
     return g.cpu().numpy(), float(loss.item())
 
 
@@ -109,8 +126,10 @@ def evaluate(weights, feats):
 Y_MIN, Y_MAX = -0.2, 2.0
 
 
-def train(n_pairs=10_000_000, epochs=12, batch=16384, lr=2e-3, seed=7, log=print):
+def train(n_pairs=10_000_000, epochs=12, batch=16384, lr=2e-3, seed=7, log=print,
+          kernel="tcgen05"):
     """Trains the network on the GPU; returns (weights rounded to BF16, meta).
+    ``kernel`` is the gradient kernel, one of KERNELS.
 
     The pairs cover the four adiabats over p 100..1050 hPa and T -80..40 degC
     (xc_guess_pairs); those the plain iteration could not solve, and those
@@ -130,6 +149,7 @@ def train(n_pairs=10_000_000, epochs=12, batch=16384, lr=2e-3, seed=7, log=print
     v = torch.zeros_like(w)
     grad = torch.zeros_like(w)
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed)
@@ -143,10 +163,12 @@ def train(n_pairs=10_000_000, epochs=12, batch=16384, lr=2e-3, seed=7, log=print
         loss.zero_()
         for b in range(n_batches):
             step += 1
-            _lib.call("xc_guess_grad", w.data_ptr(), fe[b * batch:].data_ptr(),
-                      te[b * batch:].data_ptr(), batch, grad.data_ptr(), loss.data_ptr(), stream)
+            _grad_call(kernel, w.data_ptr(), fe[b * batch:].data_ptr(), te[b * batch:].data_ptr(),
+                       batch, grad.data_ptr(), loss.data_ptr(), status.data_ptr(), stream)
             _lib.call("xc_guess_adam", w.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(),
                       float(lr_ep), step, stream)
+        if int(status.item()):
+            raise RuntimeError("the tensor-core training kernel gave up waiting for its products")
         rms = float(np.sqrt(loss.item() / n_batches))
         curve.append(rms)
         if log:
@@ -161,7 +183,7 @@ def train(n_pairs=10_000_000, epochs=12, batch=16384, lr=2e-3, seed=7, log=print
             "pairs": n_pairs, "pairs_kept": kept,
             "pair_box": "four adiabats, p 100..1050 hPa, T -80..40 degC (saturation mixing "
                         "ratio <= 40 g/kg), reversible condensate 0..10 g/kg, dp 50..2000 Pa",
-            "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
+            "epochs": epochs, "batch": batch, "lr": lr, "seed": seed, "kernel": kernel,
             "train_rms_y": curve, "val_rms_y_bf16": val_rms, "val_rel_rms_bf16": val_rel,
             "plain_iterations_mean": float(np.abs(it).mean()),
             "plain_gave_up": int((it < 0).sum()), "seconds": time.time() - t0}
