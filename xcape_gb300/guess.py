@@ -12,8 +12,10 @@ test and the result are the reference's.
 Everything runs on the GPU through the library:
   * ``xc_guess_pairs``  -- training pairs, solved by the plain (reference)
     iteration;
-  * ``xc_guess_grad``   -- forward (hidden layer on the tensor cores, BF16
-    operands, FP32 accumulation) and backward pass of the squared error;
+  * ``xc_guess_grad_tc`` -- forward and backward pass of the squared error
+    with the three 64-wide products on the 5th-generation tensor cores
+    (tcgen05.mma, BF16 operands, FP32 accumulators in tensor memory);
+    ``xc_guess_grad`` the same with mma.sync;
   * ``xc_guess_adam``   -- Adam on FP32 master weights;
   * ``xc_guess_eval``   -- batched inference.
 The trained weights are stored rounded to BF16 in
@@ -243,8 +245,9 @@ def main(argv=None):
     tr.add_argument("--pairs", type=int, default=10_000_000)
     tr.add_argument("--epochs", type=int, default=12)
     tr.add_argument("--out", default=DEFAULT_PATH)
+    tr.add_argument("--kernel", choices=KERNELS, default="tcgen05")
     args = ap.parse_args(argv)
-    w, meta = train(n_pairs=args.pairs, epochs=args.epochs)
+    w, meta = train(n_pairs=args.pairs, epochs=args.epochs, kernel=args.kernel)
     save(args.out, w, meta)
     print(json.dumps(meta))
 
