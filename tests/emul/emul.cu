@@ -159,19 +159,25 @@ extern "C" float emu_guess_eval_packed(const float *w, float f0, float f1, float
 }
 
 // accel_map at x with the analytic slope: returns F(x) and writes out[0] =
-// F'(x) = F(x) pi2 d expo / d t2, out[1..4] = t2, qv2, ql2, qi2.
+// F'(x) = F(x) pi2 d expo / d t2, out[1..4] = t2, qv2, ql2, qi2, out[5..7] =
+// d/dt2 of qv2, ql2, qi2, out[8] = the saturation mixing ratio.
 extern "C" float emu_accel_map(int ice, float x, float p2, float pi2, float lp, float t1,
                                float th1, float qv1, float ql1, float qi1, float qt, float *out) {
-  float t2, qv2, ql2, qi2, dex = 0.0f;
+  float t2, qv2, ql2, qi2;
+  MapSlope ms = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   const float f = ice ? accel_map<true>(x, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, true, t2, qv2,
-                                        ql2, qi2, dex)
+                                        ql2, qi2, ms)
                       : accel_map<false>(x, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, true, t2,
-                                         qv2, ql2, qi2, dex);
-  out[0] = f * pi2 * dex;
+                                         qv2, ql2, qi2, ms);
+  out[0] = f * pi2 * ms.dex;
   out[1] = t2;
   out[2] = qv2;
   out[3] = ql2;
   out[4] = qi2;
+  out[5] = ms.dqv;
+  out[6] = ms.dql;
+  out[7] = ms.dqi;
+  out[8] = ms.qsat;
   return f;
 }
 

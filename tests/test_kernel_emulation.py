@@ -119,7 +119,7 @@ def test_emulated_map_slope_matches_finite_differences(ice, reversible):
     ramp's ends)."""
     L = emul.lib()
     rng = np.random.default_rng(11 + 2 * ice + int(reversible))
-    o0, op, om = (np.zeros(5, np.float32) for _ in range(3))
+    o0, op, om = (np.zeros(9, np.float32) for _ in range(3))
     rddcp = 287.04 / 1005.7
     h = 0.05
     checked = sat_checked = 0
@@ -150,6 +150,13 @@ def test_emulated_map_slope_matches_finite_differences(ice, reversible):
             continue  # the stencil straddles an end of the liquid/ice ramp
         fd = (np.float64(fp) - np.float64(fm)) / (2 * h)
         assert abs(o0[0] - fd) <= 3e-3 + 2e-2 * abs(fd), (o0[0], fd, t1, p1, sat)
+        # the state's derivatives that the Newton point's state is built
+        # from (d/dt2 of qv2, ql2, qi2; zero where unsaturated)
+        dt = np.float64(op[1]) - np.float64(om[1])
+        for j in (2, 3, 4):
+            fdq = (np.float64(op[j]) - np.float64(om[j])) / dt
+            scale = max(abs(fdq), 1e-6)
+            assert abs(o0[j + 3] - fdq) <= 2e-7 + 2e-2 * scale, (j, o0[j + 3], fdq, t1, p1, sat)
         checked += 1
         sat_checked += cond[1]
     assert checked > 300 and sat_checked > 150, (checked, sat_checked)

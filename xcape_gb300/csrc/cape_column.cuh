@@ -274,17 +274,25 @@ XC_HD R plain_map(R x, R p2, R pi2, R lp, R t1, R th1, R qv1, R ql1, R qi1, R qt
   return th1 * xexp(expo);
 }
 
+// What accel_map returns beside th2 when asked for the slope: dex = d expo /
+// d t2 at x, and d/dt2 of qv2, ql2 and qi2 there (zero where the parcel is
+// unsaturated); qsat is the saturation mixing ratio at x in every call.
+struct MapSlope {
+  float dex, dqv, dql, dqi, qsat;
+};
+
 // The same map for the accelerated solvers: the approximate exp and divides
 // of getqvs_fast / getqvi_fast, the exponent over one common denominator
 // (one approximate divide), and the clamps as single min/max operations
 // (equal to the reference's compare-and-select for the non-NaN bounds used
-// here).  With slope set it also returns dex = d expo / d t2 at x,
-// differentiated through the saturation mixing ratio (dqsat_dt), the
-// liquid/ice split and the exponent, for the Newton step of substep.
+// here).  With slope set it also returns the map's derivatives at x
+// (MapSlope), differentiated through the saturation mixing ratio
+// (dqsat_dt), the liquid/ice split and the exponent, for the Newton step of
+// substep and for the parcel state at the Newton point.
 template <bool ICE>
 XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th1, float qv1,
                       float ql1, float qi1, float qt, bool slope, float &t2, float &qv2,
-                      float &ql2, float &qi2, float &dex) {
+                      float &ql2, float &qi2, MapSlope &ms) {
   t2 = x * pi2;
   float fliq, fice, qsat;
   float dq = 0.0f, dql = 0.0f, dqi = 0.0f;  // d/dt2 of qv2, ql2, qi2 (slope)
@@ -323,6 +331,10 @@ XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th
     qi2 = 0.0f;
   }
   ql2 = fmaxf(qt - qv2 - qi2, 0.0f);
+  ms.dqv = dq;
+  ms.dql = dql;
+  ms.dqi = dqi;
+  ms.qsat = qsat;
   const float tbar = 0.5f * (t1 + t2);
   const float qvbar = 0.5f * (qv1 + qv2);
   const float qlbar = 0.5f * (ql1 + ql2);
@@ -343,9 +355,49 @@ XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th
       dnum += (LS1 - LS2 * tbar) * dqi - 0.5f * LS2 * (qi2 - qi1);
       dcpm += CPI * dqi;
     }
-    dex = fast_div(dnum - r * (0.5f * dcpm * tbar + 0.5f * cpm), den);
+    ms.dex = fast_div(dnum - r * (0.5f * dcpm * tbar + 0.5f * cpm), den);
   }
   return th1 * fast_exp(r - RDDCP * lp);
+}
+
+// The accelerated solvers' first Newton step x0 -> xn ends the sub-step when
+// it is below NEWTON_ACCEPT: the map is smooth there, so the fixed point
+// lies within F''/2 (xn - x0)^2 of xn -- under 1e-5 K for the map's
+// curvature (about 0.15 / K when saturated), far inside the 2e-4 K test --
+// and the parcel state at xn follows from the state and its derivatives at
+// x0 (MapSlope) to second order, without a second evaluation of the map.
+// Such a sub-step returns th2 = xn where the iteration returns the map's
+// value at its last guess, a few ulp away; summed over a column's sub-steps
+// that moves CAPE by up to 0.5 J/kg against the FP64 reference (0.17 J/kg
+// without this step, 15,350 columns of 37 pressure levels, most-unstable),
+// for 1.08 instead of 1.91 evaluations of the map per sub-step.
+// It does not end the sub-step when the step crosses the liquid/ice ramp's
+// corners (ICE) or the saturation point, where the map has a kink; nor when
+// the parcel is unsaturated at x0 with its saturation mixing ratio within
+// 1% of qt.  Returns whether it took the step, then with th2 = xn and the
+// state (t2, qv2, ql2, qi2) at xn.
+constexpr float NEWTON_ACCEPT = 0.01f;
+
+template <bool ICE>
+XC_HD bool newton_accept(float x0, float xn, float pi2, float qt, const MapSlope &ms, float &th2,
+                         float &t2, float &qv2, float &ql2, float &qi2) {
+  if (!(fabsf(xn - x0) <= NEWTON_ACCEPT)) return false;
+  const float tn = xn * pi2, dt = tn - t2;
+  if (ICE && ((t2 > 233.15f) != (tn > 233.15f) || (t2 < 273.15f) != (tn < 273.15f)))
+    return false;
+  if (ql2 + qi2 > 0.0f) {
+    // saturated at x0, and by a margin at xn
+    const float qln = ql2 + ms.dql * dt, qin = qi2 + ms.dqi * dt;
+    if (!(qln + qin > 1e-3f * (ql2 + qi2))) return false;
+    qv2 = qv2 + ms.dqv * dt;
+    ql2 = fmaxf(qln, 0.0f);
+    qi2 = fmaxf(qin, 0.0f);
+  } else if (!(qt < 0.99f * ms.qsat)) {
+    return false;  // unsaturated at x0, but close to saturation
+  }
+  t2 = tn;
+  th2 = xn;
+  return true;
 }
 
 // The step of F(x) - x from x with slope q (secant or Newton), q kept in
@@ -398,18 +450,20 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
     if constexpr (SOLVER == SOLVE_LEARNED_WARP) {
       if (ss.net_dth == ss.net_dth) thlast = th1 + ss.net_dth;
     }
-    float dex = 0.0f;
+    MapSlope ms = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     for (int i = 1;; ++i) {
       th2 = accel_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, i == 1, t2, qv2,
-                           ql2, qi2, dex);
+                           ql2, qi2, ms);
       ++niter;
       if (i > 100) return false;
       if (!(fabsf(th2 - thlast) > CONVERGE)) break;
       const float q = i >= 2 && thlast != x_prev ? fast_div(th2 - f_prev, thlast - x_prev)
-                                                 : th2 * pi2 * dex;
+                                                 : th2 * pi2 * ms.dex;
+      const float xn = root_step(thlast, th2, q);
+      if (i == 1 && newton_accept<ICE>(thlast, xn, pi2, qt, ms, th2, t2, qv2, ql2, qi2)) break;
       x_prev = thlast;
       f_prev = th2;
-      thlast = root_step(thlast, th2, q);
+      thlast = xn;
     }
     // a sub-step without a pressure drop (a level at the pressure of the
     // one below it, e.g. the surface exactly on a pressure level) has no
@@ -425,7 +479,7 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
     while (true) {
       i = i + 1;
       if constexpr (ACCEL_MATH) {
-        float unused;
+        MapSlope unused;
         th2 = accel_map<ICE>(thlast, p2, pi2, lp, t1, th1, qv1, ql1, qi1, qt, false, t2, qv2,
                              ql2, qi2, unused);
       } else {
