@@ -52,6 +52,7 @@
 // levels keeps the others out of the sums; segments past the last column
 // read the last column.  The window needs nk >= RUN.
 #include "srh_column.cuh"
+#include "tc05.cuh"
 #include "xc_kernels.h"
 
 namespace xc {
@@ -99,6 +100,20 @@ __device__ __forceinline__ float seg_ctv(float P, float T, float Td) {
 __device__ __forceinline__ int seg_below(float z) {
   const int k = __float2int_ru(z * (1.0f / 500.0f));
   return min(max(k, 1), 13) - 1;
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to shared memory, completing on the mbarrier's transaction
+// count (cp.async.bulk, non-tensor).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+      :: "r"(tc05::smem_u32(dst)), "l"(src), "r"(bytes), "r"(tc05::smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n"
+               :: "r"(tc05::smem_u32(bar)), "r"(bytes) : "memory");
 }
 
 }  // namespace
@@ -160,12 +175,21 @@ __device__ __forceinline__ void seg_finish(const SrhArgs &a, long long i, bool a
   }
 }
 
-template <int GRID, int RUN>
+// STAGED: the block's 16 rows of p (sigma grids), t, td, u and v are first
+// copied into shared memory by bulk copies (one per array: the rows are one
+// contiguous range), and the lanes read their windows from there; the
+// blocks must be full and the arrays 16-byte aligned.  A block whose copies
+// do not arrive within the wait's limit lets its first lane of each segment
+// run the column routine instead (results unchanged).
+template <int GRID, int RUN, bool STAGED>
 __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
   constexpr unsigned FULL = 0xffffffffu;
   constexpr int COLS = SEG_THREADS / SEG;  // columns per block
   constexpr int ROUND = SEG * RUN;
+  constexpr int NARR = GRID == 1 ? 5 : 4;  // staged arrays: t, td, u, v (, p)
   __shared__ float slot_u[COLS][12], slot_v[COLS][12];
+  extern __shared__ __align__(128) float stage[];  // [NARR][COLS * nk] when STAGED
+  __shared__ uint64_t stage_bar;
   const int lane = threadIdx.x & 31;
   const int sl = lane & (SEG - 1);
   const unsigned seg_mask = 0xffu << (lane & ~(SEG - 1));
@@ -185,8 +209,33 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
     st = st < 1 ? 1 : (st > nk + 1 ? nk + 1 : st);
   }
   const int ncl = nk - st + 2;  // assembled levels: 1 (surface) .. ncl
-  const long long row = ic * nk;
+  long long row = ic * nk;
   const int base = st - 3;  // 0-based input index of assembled level j: base + j
+  if (STAGED) {
+    const long long g0 = (long long)blockIdx.x * COLS * nk;
+    const uint32_t bytes = (uint32_t)(COLS * nk * sizeof(float));
+    if (threadIdx.x == 0) tc05::mbar_init(&stage_bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(&stage_bar, NARR * bytes);
+      const float *src[5] = {gt, gtd, gu, gv, gp};
+      for (int k = 0; k < NARR; ++k)
+        bulk_g2s(stage + k * COLS * nk, src[k] + g0, bytes, &stage_bar);
+    }
+    const bool arrived = __syncthreads_and(tc05::mbar_wait(&stage_bar, 0, 1u << 22));
+    if (!arrived) {
+      if (sl == 0 && active) srh_column_run<float, GRID, true>(a, i);
+      if (threadIdx.x == 0) tc05::mbar_wait(&stage_bar, 0, 1u << 22);  // the copies in flight
+      return;
+    }
+    // the lanes read their windows from the block's rows in shared memory
+    gt = stage;
+    gtd = stage + COLS * nk;
+    gu = stage + 2 * COLS * nk;
+    gv = stage + 3 * COLS * nk;
+    if (GRID == 1) gp = stage + 4 * COLS * nk;
+    row = (long long)cb * nk;
+  }
   for (int k = sl; k < 24; k += SEG) {
     if (k < 12) slot_u[cb][k] = VMSG;
     else slot_v[cb][k - 12] = VMSG;
@@ -220,10 +269,10 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
     float s = 0.0f;  // running sum of the increments of slots 1 .. RUN-1
 #pragma unroll
     for (int c = 0; c < RUN; ++c) {
-      const float P = __ldg(wp + c);
-      u[c] = __ldg(wu + c);
-      v[c] = __ldg(wv + c);
-      const float ct = seg_ctv(P, __ldg(wt + c), __ldg(wtd + c));
+      const float P = STAGED && GRID == 1 ? wp[c] : __ldg(wp + c);
+      u[c] = STAGED ? wu[c] : __ldg(wu + c);
+      v[c] = STAGED ? wv[c] : __ldg(wv + c);
+      const float ct = seg_ctv(P, STAGED ? wt[c] : __ldg(wt + c), STAGED ? wtd[c] : __ldg(wtd + c));
       if (c == 0) {
         Pf = P;
         Cf = ct;
@@ -314,8 +363,8 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
       // INTERP1 with X1 = aglh(ktop), X3 = aglh(ktop-1): X3 < X1 for
       // increasing heights, so its X3 == X1 adjustment never applies here.
       // The winds of the two levels are read again (from L1).
-      const float uh = __ldg(wu + t), vh = __ldg(wv + t);
-      const float ul = t > 0 ? __ldg(wu + t - 1) : um, vl = t > 0 ? __ldg(wv + t - 1) : vm;
+      const float uh = wu[t], vh = wv[t];
+      const float ul = t > 0 ? wu[t - 1] : um, vl = t > 0 ? wv[t - 1] : vm;
       const float w = (depth - zh) * rcp_a(zl - zh);
       utop = fmaf(ul - uh, w, uh);
       vtop = fmaf(vl - vh, w, vh);
@@ -334,11 +383,55 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
 
 namespace {
 
+constexpr long long SEG_COLS = SEG_THREADS / SEG;  // columns per block
+constexpr size_t SEG_STAGE_MAX = 46 * 1024;        // staged rows per block, bytes
+
+// The staged kernel's shared memory for nk levels (0: it does not fit).
+size_t seg_stage_bytes(int grid, int nk) {
+  const size_t b = (size_t)(grid == 1 ? 5 : 4) * SEG_COLS * nk * sizeof(float);
+  return b <= SEG_STAGE_MAX ? b : 0;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
 template <int GRID, int RUN>
 cudaError_t launch_seg(const SrhArgs &a, cudaStream_t s) {
-  constexpr long long cols = SEG_THREADS / SEG;
-  const unsigned blocks = (unsigned)((a.n2 + cols - 1) / cols);
-  srh_seg_kernel<GRID, RUN><<<blocks, SEG_THREADS, 0, s>>>(a);
+  const size_t stage = seg_stage_bytes(GRID, a.nk);
+  const bool staged = stage > 0 && aligned16(a.t) && aligned16(a.td) && aligned16(a.u) &&
+                      aligned16(a.v) && (GRID == 2 || aligned16(a.p));
+  const long long full = staged ? a.n2 / SEG_COLS : 0;  // blocks the staged kernel takes
+  if (full > 0) {
+    srh_seg_kernel<GRID, RUN, true><<<(unsigned)full, SEG_THREADS, stage, s>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  const long long c0 = full * SEG_COLS;  // the remaining columns: the direct kernel
+  if (c0 >= a.n2) return cudaSuccess;
+  SrhArgs t = a;
+  if (c0 > 0) {
+    const size_t nk = (size_t)a.nk;
+    t.n2 = a.n2 - c0;
+    if (GRID == 1) t.p = (const float *)a.p + c0 * nk;
+    t.t = (const float *)a.t + c0 * nk;
+    t.td = (const float *)a.td + c0 * nk;
+    t.u = (const float *)a.u + c0 * nk;
+    t.v = (const float *)a.v + c0 * nk;
+    t.ps = (const float *)a.ps + c0;
+    t.ts = (const float *)a.ts + c0;
+    t.tds = (const float *)a.tds + c0;
+    t.us = (const float *)a.us + c0;
+    t.vs = (const float *)a.vs + c0;
+    if (a.start) t.start = a.start + c0;
+    t.srh_rm = a.srh_rm + c0;
+    t.srh_lm = a.srh_lm + c0;
+    if (a.rm) {
+      t.rm = a.rm + 2 * c0;
+      t.lm = a.lm + 2 * c0;
+      t.mean6 = a.mean6 + 2 * c0;
+    }
+  }
+  const unsigned blocks = (unsigned)((t.n2 + SEG_COLS - 1) / SEG_COLS);
+  srh_seg_kernel<GRID, RUN, false><<<blocks, SEG_THREADS, 0, s>>>(t);
   return cudaGetLastError();
 }
 
