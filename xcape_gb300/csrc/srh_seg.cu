@@ -193,7 +193,11 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
   const int lane = threadIdx.x & 31;
   const int sl = lane & (SEG - 1);
   const unsigned seg_mask = 0xffu << (lane & ~(SEG - 1));
-  const int cb = threadIdx.x / SEG;  // column within the block
+  // the column within the block: segment 4w + j of warp w takes column
+  // 4w + j, or with seg_colmap 4j + w (the staged rows of columns four
+  // apart can start in other shared-memory banks)
+  const int seg = threadIdx.x / SEG;
+  const int cb = STAGED && a.seg_colmap ? ((seg & 3) << 2) | (seg >> 2) : seg;
   const long long i = (long long)blockIdx.x * COLS + cb;
   const bool active = i < a.n2;
   const long long ic = active ? i : a.n2 - 1;  // the column whose inputs this segment reads
@@ -394,8 +398,34 @@ size_t seg_stage_bytes(int grid, int nk) {
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
 
+// Which columns share a warp in the staged kernel: the assignment whose
+// first round of shared-memory reads (a column starting at its first level)
+// has the fewer bank conflicts, counted as the sum over the warps' loads of
+// the largest number of lanes on one bank.  With 50 levels, columns four
+// apart start 200 floats apart, 8 banks, and the 32 lanes of a load fall in
+// 32 banks.
+int seg_colmap_for(int nk, int run) {
+  int cost[2] = {0, 0};
+  for (int map = 0; map < 2; ++map)
+    for (int w = 0; w < 4; ++w)
+      for (int c = 0; c < run; ++c) {
+        int cnt[32] = {0}, mx = 0;
+        for (int lane = 0; lane < 32; ++lane) {
+          const int seg = 4 * w + lane / SEG, sl = lane % SEG;
+          const int cb = map ? ((seg & 3) << 2) | (seg >> 2) : seg;
+          const int ws = sl * run < nk - run ? sl * run : nk - run;
+          const int k = ++cnt[(cb * nk + ws + c) & 31];
+          mx = k > mx ? k : mx;
+        }
+        cost[map] += mx;
+      }
+  return cost[1] < cost[0] ? 1 : 0;
+}
+
 template <int GRID, int RUN>
-cudaError_t launch_seg(const SrhArgs &a, cudaStream_t s) {
+cudaError_t launch_seg(const SrhArgs &a0, cudaStream_t s) {
+  SrhArgs a = a0;
+  a.seg_colmap = seg_colmap_for(a.nk, RUN);
   const size_t stage = seg_stage_bytes(GRID, a.nk);
   const bool staged = stage > 0 && aligned16(a.t) && aligned16(a.td) && aligned16(a.u) &&
                       aligned16(a.v) && (GRID == 2 || aligned16(a.p));

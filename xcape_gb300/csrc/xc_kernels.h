@@ -110,6 +110,7 @@ struct SrhArgs {
   double *srh_rm, *srh_lm;
   float *rm, *lm, *mean6;  // nullable, [n2][2]
   int precision;           // 0: reference precisions (FP64 stdheight/SREH), 1: FP32
+  int seg_colmap = 0;      // FP32 level-parallel kernel: which columns share a warp (srh_seg.cu)
 };
 
 cudaError_t launch_srh(const SrhArgs &a, cudaStream_t s);
