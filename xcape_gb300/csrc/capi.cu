@@ -442,9 +442,9 @@ namespace {
 // The host-pointer CAPE path for nsrc sources of the same columns.  The
 // columns go through in chunks.  One stream copies the chunks' inputs in
 // order, once for all the sources; each chunk's ordering, its nsrc lifts and
-// its output copies run on one of two streams once its inputs are in, so
-// copies overlap lifts and one chunk's last warps overlap the next chunk's
-// first.  Every chunk has its own device slot when the ring budget allows
+// its output copies run on one of host_streams() compute streams, in turn,
+// once its inputs are in, so copies overlap lifts and one chunk's last warps
+// overlap the next chunks' first.  Every chunk has its own device slot when the ring budget allows
 // (the usual case), and then the calling thread queues the whole call
 // without waiting.  Outputs come back into pinned staging (a copy into
 // pageable memory would block this thread) and are moved into the caller's
