@@ -78,10 +78,17 @@ XC_HD float getthe(float p, float t, float td, float q) {
 // Approximate divide (a few ulp) for the accelerated solvers: their secant
 // quotients, the saturation mixing ratio and the exponent of their map, whose
 // contract is agreement with the FP64 run within tolerance rather than
-// bit-faithfulness to the FP32 Fortran.  Exact on the host.
+// bit-faithfulness to the FP32 Fortran.  On the device a times the PTX
+// reciprocal approximation; this and the two functions below use the
+// flush-to-zero forms, which skip the handling of subnormal operands and
+// results: the quantities they see (pressures, temperatures, mixing ratios
+// and their ratios) are far from the subnormal range, where a result would
+// only be flushed to zero.  Exact on the host.
 XC_HD float fast_div(float a, float b) {
 #if defined(__CUDA_ARCH__)
-  return __fdividef(a, b);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return a * r;
 #else
   return a / b;
 #endif
@@ -90,17 +97,21 @@ XC_HD float fast_div(float a, float b) {
 // error of a few ulp plus the rounding of x log2(e).  expf on the host.
 XC_HD float fast_exp(float x) {
 #if defined(__CUDA_ARCH__)
-  return __expf(x);
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x * 1.4426950408889634f));
+  return y;
 #else
   return expf(x);
 #endif
 }
 
-// Approximate natural log: lg2.approx of x times ln 2 (3 ulp at most for x
-// outside [0.5, 2]).  logf on the host.
+// Approximate natural log: lg2.approx of x times ln 2 (a few ulp for x
+// outside [0.5, 2], a small absolute error inside).  logf on the host.
 XC_HD float fast_log(float x) {
 #if defined(__CUDA_ARCH__)
-  return __logf(x);
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y * 0.6931471805599453f;
 #else
   return logf(x);
 #endif
