@@ -47,9 +47,9 @@ CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
 # share and active threads per warp instruction, from `ncu --set full`
 # captures of `bench.py --profile` (profiles/cape_kernel_pressure_1M.md).
 NCU_RECORDED = "ncu --set full of bench.py --profile, profiles/cape_kernel_pressure_1M.md"
-NCU_TRAFFIC = {"learned": 701_029_632, "plain": 728_342_784}
-NCU_ISSUE = {"learned": {"issue_active": 0.846, "tensor_pipe_active": 0.0086,
-                         "threads_per_warp_instruction": 28.24},
+NCU_TRAFFIC = {"learned": 697_144_832, "plain": 728_342_784}
+NCU_ISSUE = {"learned": {"issue_active": 0.847, "tensor_pipe_active": 0.0105,
+                         "threads_per_warp_instruction": 28.25},
              "plain": {"issue_active": 0.879, "tensor_pipe_active": 0.0,
                        "threads_per_warp_instruction": 27.11}}
 ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg (strided)
