@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(SEG_THREADS, 8) srh_seg_kernel(SrhArgs a) {
     if (threadIdx.x == 0) {
       mbar_expect_tx(&stage_bar, NARR * bytes);
       const float *src[5] = {gt, gtd, gu, gv, gp};
+#pragma unroll
       for (int k = 0; k < NARR; ++k)
         bulk_g2s(stage + k * COLS * nk, src[k] + g0, bytes, &stage_bar);
     }
