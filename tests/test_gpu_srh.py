@@ -316,6 +316,30 @@ def test_srh_fp32_level_parallel_kernel_short_columns():
             np.testing.assert_allclose(g, w, rtol=0, atol=1e-3)
 
 
+def test_srh_fp32_staged_and_direct_loads_agree():
+    """Float32 CUDA tensors on 16-byte boundaries take the level-parallel
+    kernel with its rows staged in shared memory by bulk copies (all full
+    blocks; the partial last block reads global memory); the same values one
+    float off a 16-byte boundary take the direct-load kernel for every
+    block.  Both run the same arithmetic on the same values: the same bits."""
+    torch = torch_cuda()
+    for args, vl in ((S.srh_c2(shape=(37, 41)), "model"), (S.pressure_srh(shape=(29, 33)), "pressure")):
+        dev = to_dev(*[np.asarray(x, np.float32) for x in args])
+        assert all(x.data_ptr() % 16 == 0 for x in dev)
+        off = []
+        for x in dev:
+            buf = torch.empty(x.numel() + 1, dtype=x.dtype, device=x.device)
+            y = buf[1:].view(x.shape)
+            y.copy_(x)
+            assert y.data_ptr() % 16 == 4
+            off.append(y)
+        a = X.calc_srh(*dev, depth=3000, vertical_lev=vl, output_var="all", precision="fp32")
+        b = X.calc_srh(*off, depth=3000, vertical_lev=vl, output_var="all", precision="fp32")
+        torch.cuda.synchronize()
+        for x, y in zip(a, b):
+            assert torch.equal(x, y)
+
+
 def test_srh_fp32_level_parallel_kernel_falls_back_on_irregular_columns():
     """Columns whose heights do not increase with level -- pressure rising
     with level, a NaN, a level below the previous one -- are redone by the
