@@ -8,7 +8,8 @@ xc_loopcape_ex_noalloc uses a static device array inside the library
 instead.  These tests call it through the C ABI, twice in a row, and check
 each result against xc_loopcape_ex with a caller-provided workspace (within
 the CAPE/CIN tolerance the other GPU tests use; the two run the same
-kernels), also at exactly XC_NOALLOC_MAX_COLUMNS columns.  They check that
+kernels), also at exactly XC_NOALLOC_MAX_COLUMNS columns, and one result
+directly against the oracle under the parity criteria of gpu_util.  They check that
 the calls make no allocation -- neither the library's own (its allocation
 counter, xc_alloc_count) nor torch's -- including in a fresh process under
 lazy module loading, and that a batch above the limit is refused with a
@@ -106,6 +107,28 @@ def _check_two_calls(d, n2, guess):
 def test_noalloc_matches_workspace_entry_point(dev_inputs, guess):
     d, n2 = dev_inputs
     _check_two_calls(d, n2, guess)
+
+
+def test_noalloc_against_the_oracle():
+    """The allocation-free entry point pinned to the oracle directly, not only
+    through xc_loopcape_ex: the plain solver against the FP32 oracle with the
+    parity criteria of the single-call tests, on 4,096 columns of pressure
+    levels, most-unstable parcels."""
+    import torch
+    from gpu_util import compare_cape, oracle_cols
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(64, 64), seed=12)
+    d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (plev, t, td, ps, ts, tds)]
+    n2 = ps.size
+    L = _lib.lib()
+    outs = _outputs(n2)
+    _lib.check(L.xc_loopcape_ex_noalloc(*_args(d, n2, _lib.XC_GUESS_PLAIN, outs),
+                                        torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    cape, cin, zout, mulvl, status = _numpy(outs)
+    args = (2, plev, t, td, ps, ts, tds, "most-unstable", "pseudo-liquid", 500.0, 500.0)
+    compare_cape({"cape": cape, "cin": cin, "mulvl": mulvl, "z_out": zout, "status": status},
+                 oracle_cols(*args), oracle_cols(*args, precision="f64"),
+                 what="noalloc vs oracle")
 
 
 def test_noalloc_at_the_column_limit():
