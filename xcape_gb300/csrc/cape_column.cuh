@@ -42,7 +42,7 @@ struct EnvT {
 };
 using Env = EnvT<float>;
 
-// FAST (the accelerated solvers, float only): pi from exp(RDDCP ln(p/P00)),
+// FAST (the accelerated solvers, float only): pi as 2^(RDDCP log2(p/P00)),
 // q from getqvs_fast and the two quotients from approximate divides.
 template <bool FAST = false, typename R = float>
 XC_HD EnvT<R> make_env(R pin, R tin, R tdin) {
@@ -52,9 +52,8 @@ XC_HD EnvT<R> make_env(R pin, R tin, R tdin) {
   e.td = XC_LIT(R, 273.15) + tdin;
   if constexpr (FAST) {
     static_assert(sizeof(R) == sizeof(float), "the accelerated environment is FP32");
-    float es;
-    e.pi = fast_exp(RDDCP * fast_log(e.p * RP00));
-    e.q = getqvs_fast(e.p, e.td, es);
+    e.pi = fast_exp2(RDDCP * fast_log2(e.p * RP00));
+    e.q = getqvs_fast(e.p, e.td);
     e.th = fast_div(e.t, e.pi);
     e.thv = fast_div(e.th * (1.0f + REPS * e.q), 1.0f + e.q);
   } else {
@@ -171,6 +170,9 @@ struct SolverState {
   // (SOLVE_ACCEL, SOLVE_LEARNED) (th2 - th1) / dp of the previous sub-step;
   // 0 before the first, so that the first guess is th1
   float rate = 0.0f;
+  // (SOLVE_ACCEL, SOLVE_LEARNED*) fast_rcp of the current level's sub-step
+  // dp, taken once per level for the rate
+  float rdp = 0.0f;
   bool saturated = false;   // (SOLVE_LEARNED_ALL) condensate at the end of the last sub-step
   // (SOLVE_LEARNED) the network's output at the parcel's LCL until the
   // parcel first saturates, NaN once used or when there is none
@@ -222,10 +224,10 @@ XC_HD bool network_increment(const float *w, float p1, float p2, float t1, float
 
 // d qsat / dT of qsat = QEPS es / (p - es), es = 611.2 exp(a (T - 273.15) / (T - b))
 // (getqvs: a = 17.67, b = 29.65; getqvi: a = 21.8745584, b = 7.66), from the
-// values the evaluation already has: qsat p / (p - es) * k / (T - b)^2 with
-// k = a (273.15 - b) and tb = T - b.
-XC_HD float dqsat_dt(float qsat, float p, float es, float tb, float k) {
-  return fast_div(qsat * p * k, (p - es) * tb * tb);
+// parts qsat_fast already has: qsat p / (p - es) * k / (T - b)^2 with
+// k = a (273.15 - b).
+XC_HD float dqsat_dt(float qsat, float p, const QsatParts &q, float k) {
+  return qsat * p * q.rpe * (k * q.rtb) * q.rtb;
 }
 
 // The map F of a sub-step (:435-463): th2 = F(x) for the guess x, with t2,
@@ -281,14 +283,22 @@ struct MapSlope {
   float dex, dqv, dql, dqi, qsat;
 };
 
-// The same map for the accelerated solvers: the approximate exp and divides
-// of getqvs_fast / getqvi_fast, the exponent over one common denominator
-// (one approximate divide), and the clamps as single min/max operations
-// (equal to the reference's compare-and-select for the non-NaN bounds used
-// here).  With slope set it also returns the map's derivatives at x
-// (MapSlope), differentiated through the saturation mixing ratio
-// (dqsat_dt), the liquid/ice split and the exponent, for the Newton step of
-// substep and for the parcel state at the Newton point.
+// The same map for the accelerated solvers: the approximate exp and
+// reciprocals of qsat_fast, the exponent over one common denominator (one
+// approximate divide), and the clamps as single min/max operations (equal to
+// the reference's compare-and-select for the non-NaN bounds used here).  The
+// means of the two ends (tbar, qvbar, ...) enter as sums with the factors
+// 1/2 folded into the constants: with tsum = t1 + t2,
+//   lhv = LV1 - LV2 tbar  -> 4 lhv = 4 LV1 - 2 LV2 tsum   (and lhs alike),
+//   rm = RD + RV qvbar    -> 2 rm = 2 RD + RV qvsum,
+//   cpm = CP + CPV qvbar + CPL qlbar (+ CPI qibar) -> 2 cpm, likewise,
+// so that the exponent's quotient
+//   [lhv (ql2 - ql1) + lhs (qi2 - qi1) + rm lp tbar] / (cpm tbar)
+// is [4 lhv (ql2 - ql1) + 4 lhs (qi2 - qi1) + 2 rm lp tsum] / (2 cpm tsum).
+// With slope set it also returns the map's derivatives at x (MapSlope),
+// differentiated through the saturation mixing ratio (dqsat_dt), the
+// liquid/ice split and the exponent, for the Newton step of substep and for
+// the parcel state at the Newton point.
 template <bool ICE>
 XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th1, float qv1,
                       float ql1, float qi1, float qt, bool slope, float &t2, float &qv2,
@@ -297,19 +307,18 @@ XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th
   float fliq, fice, qsat;
   float dq = 0.0f, dql = 0.0f, dqi = 0.0f;  // d/dt2 of qv2, ql2, qi2 (slope)
   if (ICE) {
-    fliq = fmaxf(fminf((t2 - 233.15f) / (273.15f - 233.15f), 1.0f), 0.0f);
+    fliq = fmaxf(fminf((t2 - 233.15f) * (1.0f / (273.15f - 233.15f)), 1.0f), 0.0f);
     fice = 1.0f - fliq;
     // both are evaluated: skipping the one of weight 0 outside the
     // 233.15-273.15 K ramp was slower (the lanes of a warp straddle it)
-    float esl, esi;
-    const float qvs = getqvs_fast(p2, t2, esl), qvi = getqvi_fast(p2, t2, esi);
+    QsatParts ql, qi;
+    const float qvs = qsat_fast<false>(p2, t2, ql), qvi = qsat_fast<true>(p2, t2, qi);
     qsat = fliq * qvs + fice * qvi;
     if (slope && qt > qsat) {
       // saturated: qv2 = qsat, ql2 = fliq (qt - qsat), qi2 = fice (qt - qsat)
       const float dfl = (t2 > 233.15f && t2 < 273.15f) ? 1.0f / (273.15f - 233.15f) : 0.0f;
-      dq = dfl * (qvs - qvi) +
-           fliq * dqsat_dt(qvs, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f)) +
-           fice * dqsat_dt(qvi, p2, esi, t2 - 7.66f, 21.8745584f * (273.15f - 7.66f));
+      dq = dfl * (qvs - qvi) + fliq * dqsat_dt(qvs, p2, ql, 17.67f * (273.15f - 29.65f)) +
+           fice * dqsat_dt(qvi, p2, qi, 21.8745584f * (273.15f - 7.66f));
       const float c = dfl * (qt - qsat);
       dql = c - fliq * dq;
       dqi = -c - fice * dq;
@@ -317,10 +326,10 @@ XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th
   } else {
     fliq = 1.0f;
     fice = 0.0f;
-    float esl;
-    qsat = getqvs_fast(p2, t2, esl);
+    QsatParts ql;
+    qsat = qsat_fast<false>(p2, t2, ql);
     if (slope && qt > qsat) {
-      dq = dqsat_dt(qsat, p2, esl, t2 - 29.65f, 17.67f * (273.15f - 29.65f));
+      dq = dqsat_dt(qsat, p2, ql, 17.67f * (273.15f - 29.65f));
       dql = -dq;
     }
   }
@@ -335,27 +344,31 @@ XC_HD float accel_map(float x, float p2, float pi2, float lp, float t1, float th
   ms.dql = dql;
   ms.dqi = dqi;
   ms.qsat = qsat;
-  const float tbar = 0.5f * (t1 + t2);
-  const float qvbar = 0.5f * (qv1 + qv2);
-  const float qlbar = 0.5f * (ql1 + ql2);
-  const float lhv = LV1 - LV2 * tbar;
-  const float rm = RD + RV * qvbar;
-  const float qibar = ICE ? 0.5f * (qi1 + qi2) : 0.0f;
-  const float cpm = ICE ? CP + CPV * qvbar + CPL * qlbar + CPI * qibar
-                        : CP + CPV * qvbar + CPL * qlbar;
-  float num = lhv * (ql2 - ql1) + rm * lp * tbar;
-  if (ICE) num += (LS1 - LS2 * tbar) * (qi2 - qi1);
-  const float den = cpm * tbar;
-  const float r = fast_div(num, den);
+  const float tsum = t1 + t2;
+  const float qvsum = qv1 + qv2;
+  const float gl = ql2 - ql1;
+  const float lhv4 = 4.0f * LV1 - 2.0f * LV2 * tsum;
+  const float rm2 = 2.0f * RD + RV * qvsum;
+  float cpm2 = 2.0f * CP + CPV * qvsum + CPL * (ql1 + ql2);
+  if (ICE) cpm2 += CPI * (qi1 + qi2);
+  float num = lhv4 * gl + rm2 * lp * tsum;
+  float lhs4 = 0.0f;
+  if (ICE) {
+    lhs4 = 4.0f * LS1 - 2.0f * LS2 * tsum;
+    num += lhs4 * (qi2 - qi1);
+  }
+  const float den = cpm2 * tsum;
+  const float rden = fast_rcp(den);
+  const float r = num * rden;
   if (slope) {
-    // d expo / d t2 = (num' - r den') / den, tbar' = 1/2
-    float dnum = lhv * dql - 0.5f * LV2 * (ql2 - ql1) + lp * (0.5f * RV * dq * tbar + 0.5f * rm);
-    float dcpm = CPV * dq + CPL * dql;
+    // d r / d t2 = (num' - r den') / den, tsum' = 1
+    float dnum = lhv4 * dql - 2.0f * LV2 * gl + lp * (RV * dq * tsum + rm2);
+    float dcpm2 = CPV * dq + CPL * dql;
     if (ICE) {
-      dnum += (LS1 - LS2 * tbar) * dqi - 0.5f * LS2 * (qi2 - qi1);
-      dcpm += CPI * dqi;
+      dnum += lhs4 * dqi - 2.0f * LS2 * (qi2 - qi1);
+      dcpm2 += CPI * dqi;
     }
-    ms.dex = fast_div(dnum - r * (0.5f * dcpm * tbar + 0.5f * cpm), den);
+    ms.dex = (dnum - r * (dcpm2 * tsum + cpm2)) * rden;
   }
   return th1 * fast_exp(r - RDDCP * lp);
 }
@@ -430,9 +443,10 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
   constexpr bool ACCEL_MATH = SOLVER != SOLVE_PLAIN;
   R pi2, lp;
   if constexpr (ACCEL_MATH) {
-    const float lnp2 = fast_log(p2);
+    const float l2p2 = fast_log2(p2);
+    const float lnp2 = l2p2 * LN2;
     lp = lnp2 - ss.lnp;
-    pi2 = fast_exp(RDDCP * (lnp2 - LN_P00));
+    pi2 = fast_exp2(fmaf(RDDCP, l2p2, -RDDCP * LG2_P00));
     ss.lnp = lnp2;
   } else {
     pi2 = xpow(p2 * (R)RP00, (R)RDDCP);
@@ -481,7 +495,7 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
     // a sub-step without a pressure drop (a level at the pressure of the
     // one below it, e.g. the surface exactly on a pressure level) has no
     // rate to extrapolate: 0/0 would make every later guess NaN
-    if (dp != 0.0f) ss.rate = fast_div(th2 - th1, dp);
+    if (dp != 0.0f) ss.rate = (th2 - th1) * ss.rdp;
   } else {
     if constexpr (SOLVER == SOLVE_LEARNED_ALL) {
       float dth_net;
@@ -662,8 +676,7 @@ XC_HD SourceSelT<R> select_source(const ColumnReader<T, GRID, R> &col, int ncl, 
           const R td = XC_LIT(R, 273.15) + tdin;
           R q, the;
           if constexpr (FAST) {
-            float es;
-            q = getqvs_fast(p, td, es);
+            q = getqvs_fast(p, td);
             the = getthe_fast(p, t, td, q);
           } else {
             q = getqvs(p, td);
@@ -858,12 +871,18 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID, R> &col, int ncl, float 
         nloop = 1 + (int)f;
         dp = dp / (R)nloop;
       }
+      if constexpr (SOLVER != SOLVE_PLAIN) ss.rdp = fast_rcp(dp);
       if (r.nsub + nloop > MAX_SUBSTEPS) {
         r.cape = 0.0f;
         r.cin = 0.0f;
         r.status |= COL_TOOMANYSTEPS;
         return r;
       }
+      // two sub-steps per pass of the loop on the device: the launch took 3%
+      // less time than with one
+#if defined(__CUDA_ARCH__)
+#pragma unroll 2
+#endif
       for (int n = 1; n <= nloop; ++n) {
         ++r.nsub;
         if (!substep<ICE, PSEUDO, SOLVER>(dp, p2, t2, th2, qv2, ql2, qi2, qt, r.niter, ss)) {

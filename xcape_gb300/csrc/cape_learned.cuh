@@ -405,6 +405,7 @@ __device__ CapeResult ascend_col_warp(const ColumnReader<T, GRID> &col, int ncl,
         nloop = 1 + (int)f;
         dp = dp / (float)nloop;
       }
+      ss.rdp = fast_rcp(dp);
       if (r.nsub + nloop > MAX_SUBSTEPS) {
         r.status |= COL_TOOMANYSTEPS;
         done = aborted = true;

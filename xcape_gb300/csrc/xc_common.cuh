@@ -79,7 +79,7 @@ XC_HD float getthe(float p, float t, float td, float q) {
 // quotients, the saturation mixing ratio and the exponent of their map, whose
 // contract is agreement with the FP64 run within tolerance rather than
 // bit-faithfulness to the FP32 Fortran.  On the device a times the PTX
-// reciprocal approximation; this and the two functions below use the
+// reciprocal approximation; this and the approximate functions below use the
 // flush-to-zero forms, which skip the handling of subnormal operands and
 // results: the quantities they see (pressures, temperatures, mixing ratios
 // and their ratios) are far from the subnormal range, where a result would
@@ -117,6 +117,43 @@ XC_HD float fast_log(float x) {
 #endif
 }
 
+// Base-2 forms of the approximate exp and log, for expressions whose factors
+// log2(e) and ln 2 fold into constants (ex2.approx / lg2.approx,
+// flush-to-zero); exp2f / log2f on the host.
+XC_HD float fast_exp2(float x) {
+#if defined(__CUDA_ARCH__)
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+#else
+  return exp2f(x);
+#endif
+}
+XC_HD float fast_log2(float x) {
+#if defined(__CUDA_ARCH__)
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+#else
+  return log2f(x);
+#endif
+}
+// The reciprocal that fast_div multiplies by; 1 / x on the host.
+XC_HD float fast_rcp(float x) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return 1.0f / x;
+#endif
+}
+
+constexpr float LOG2E = 1.4426950408889634f;
+constexpr float LN2 = 0.6931471805599453f;
+constexpr float LG2_P00 = 16.609640474436812f;  // log2(P00)
+constexpr float LG2_ES0 = 9.255500733148386f;   // log2(611.2)
+
 // getthe of the accelerated solvers' source selection: the same formula with
 // the approximate log, exp and divides (powf as exp of the log), a relative
 // error near 1e-6 of theta-e.  The host build computes exactly what getthe
@@ -128,23 +165,48 @@ XC_HD float getthe_fast(float p, float t, float td, float q) {
   } else {
     tlcl = 56.0f + fast_div(1.0f, fast_div(1.0f, td - 56.0f) + 0.00125f * fast_log(fast_div(t, td)));
   }
+#if defined(__CUDA_ARCH__)
+  // the two factors (P00/p)^a exp(b) as one power of two, 2^(a log2(P00/p) + b log2(e))
+  return t * fast_exp2(fmaf(0.2854f * (1.0f - 0.28f * q), fast_log2(fast_div(100000.0f, p)),
+                            (fast_div(3376.0f, tlcl) - 2.54f) * q * (1.0f + 0.81f * q) * LOG2E));
+#else
   return t * fast_exp(0.2854f * (1.0f - 0.28f * q) * fast_log(fast_div(100000.0f, p))) *
          fast_exp((fast_div(3376.0f, tlcl) - 2.54f) * q * (1.0f + 0.81f * q));
+#endif
 }
 
-// getqvs / getqvi of the accelerated solvers: the same formulas with the
-// approximate exp and divides (the host build computes exactly what getqvs /
-// getqvi do), also returning the saturation vapour pressure es for the
-// slope of the moist-adiabat map.
-XC_HD float getqvs_fast(float p, float t, float &es_out) {
-  const float es = 611.2f * fast_exp(fast_div(17.67f * (t - 273.15f), t - 29.65f));
-  es_out = es;
-  return fast_div(QEPS * es, p - es);
+// What the accelerated saturation mixing ratio computes on its way, kept for
+// the slope of the moist-adiabat map: es, 1 / (T - b) and 1 / (p - es).
+struct QsatParts {
+  float es, rtb, rpe;
+};
+
+// getqvs (ICE false: a = 17.67, b = 29.65) / getqvi (ICE true: a =
+// 21.8745584, b = 7.66) of the accelerated solvers: es = 611.2 exp(a (T -
+// 273.15) / (T - b)), qsat = QEPS es / (p - es), with the approximate
+// reciprocals and exp.  On the device the exponent is taken to base 2, with
+// a log2(e) folded into one constant and log2(611.2) added by the same
+// multiply-add.  The host build computes exactly what getqvs / getqvi do
+// (and the two reciprocals beside them).
+template <bool ICE>
+XC_HD float qsat_fast(float p, float t, QsatParts &q) {
+  constexpr float A = ICE ? 21.8745584f : 17.67f;
+  constexpr float B = ICE ? 7.66f : 29.65f;
+#if defined(__CUDA_ARCH__)
+  q.rtb = fast_rcp(t - B);
+  q.es = fast_exp2(fmaf((t - 273.15f) * (A * LOG2E), q.rtb, LG2_ES0));
+  q.rpe = fast_rcp(p - q.es);
+  return QEPS * q.es * q.rpe;
+#else
+  q.es = 611.2f * expf(A * (t - 273.15f) / (t - B));
+  q.rtb = 1.0f / (t - B);
+  q.rpe = 1.0f / (p - q.es);
+  return QEPS * q.es / (p - q.es);
+#endif
 }
-XC_HD float getqvi_fast(float p, float t, float &es_out) {
-  const float es = 611.2f * fast_exp(fast_div(21.8745584f * (t - 273.15f), t - 7.66f));
-  es_out = es;
-  return fast_div(QEPS * es, p - es);
+XC_HD float getqvs_fast(float p, float t) {
+  QsatParts q;
+  return qsat_fast<false>(p, t, q);
 }
 
 // Fortran MIN/MAX as gfortran lowers them for the reference build: the
