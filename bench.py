@@ -20,6 +20,7 @@ the same workload per step).  Under torchrun every rank processes its own
 equal share of columns (weak scaling, no collective on the data path).
 """
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -492,15 +493,20 @@ def run_ours(args):
     n2 = hi - lo
     P, T, TD, PS, TS, TDS = (torch.from_numpy(np.ascontiguousarray(a)).to(dev)
                              for a in (plev, t, td, ps, ts, tds))
-    outs = {src: [torch.empty(n2, dtype=torch.float32, device=dev) for _ in range(3)] +
-            [torch.empty(n2, dtype=torch.int32, device=dev)] for src, _ in SOURCES}
+    # outputs [source][n2] in one array each, as xc_loopcape_multi writes them
+    nsrc = len(SOURCES)
+    out_all = [torch.empty(nsrc * n2, dtype=torch.float32, device=dev) for _ in range(3)] + \
+        [torch.empty(nsrc * n2, dtype=torch.int32, device=dev)]
+    outs = {src: [x[j * n2:(j + 1) * n2] for x in out_all] for j, (src, _) in enumerate(SOURCES)}
+    src_codes = (ctypes.c_int * nsrc)(*[code for _, code in SOURCES])
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     ws_bytes = _lib.workspace_bytes(n2)
     wsbuf = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=dev)
     ws = wsbuf.data_ptr() + (-wsbuf.data_ptr()) % 256
     order = not args.no_order
-    launches_per_call = 4 if order else 1  # 3 ordering kernels + the lift
+    # per step: the 3 ordering kernels once, then one lift per source
+    launches_per_step = (3 if order else 0) + nsrc
 
     def launch(src_code, o, counters=None, g=None):
         cape, cin, zout, mulvl = o
@@ -513,8 +519,14 @@ def run_ours(args):
                                     sptr))
 
     def step():
-        for src, code in SOURCES:
-            launch(code, outs[src])
+        # both sources in one call: the columns are ordered once for both
+        cape, cin, zout, mulvl = out_all
+        _lib.check(L.xc_loopcape_multi(2, P.data_ptr(), T.data_ptr(), TD.data_ptr(), PS.data_ptr(),
+                                       TS.data_ptr(), TDS.data_ptr(), _lib.XC_F32, PINC, nsrc,
+                                       ctypes.cast(src_codes, ctypes.c_void_p), ML_DEPTH, ADIABAT,
+                                       None, NLEV, n2, guess, cape.data_ptr(), cin.data_ptr(),
+                                       mulvl.data_ptr(), zout.data_ptr(), None, None,
+                                       ws if order else None, ws_bytes if order else 0, sptr))
 
     if args.profile:
         step()
@@ -672,6 +684,8 @@ def run_ours(args):
         "issue_roofline": dict(NCU_ISSUE.get(args.guess, {}), source=f"recorded: {NCU_RECORDED}")
         if args.guess in NCU_ISSUE else None,
         "per_source_ms": per_src_ms,
+        "per_source_note": "one xc_loopcape_ex call per source, each ordering the columns itself; "
+                           "the timed step orders them once for both (xc_loopcape_multi)",
         "vs_plain": ({"plain_value": cols_all / (sum(plain_ms.values()) / 1e3),
                       "plain_per_source_ms": plain_ms,
                       "speedup": sum(plain_ms.values()) / sum(per_src_ms.values()),
@@ -694,7 +708,7 @@ def run_ours(args):
         "e2e": {"value": cols_all / e2e_dt, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "api": "xcape_gb300.calc_cape_sources(numpy, pinned), both sources in one call"},
-        "gpu_launches": args.steps * len(SOURCES) * launches_per_call,
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": clocks,
     }
     if not args.no_cpu_baseline and world == 1:

@@ -153,6 +153,22 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
                    float *cape, float *cin, int *mulvl, float *z_out, int *status,
                    long long *counters, void *workspace, size_t workspace_bytes, void *stream);
 
+/* xc_loopcape_ex for nsrc (1..3) sources of the same device-resident
+ * columns in one call: with a workspace the columns are ordered once, and
+ * every source's lift reads that order.  No counterpart in the reference,
+ * where each source is its own calc_cape call (src/xcape/core.py:130-235).
+ * sources [nsrc] holds XC_SOURCE_* codes; the outputs are [nsrc][n2]
+ * (source j's result of column i at j * n2 + i; status may be NULL) and
+ * equal those of nsrc xc_loopcape_ex calls.  counters, when given, sums the
+ * work of all the sources.  With XC_RETRY_FP64 the retries of every source
+ * follow all the lifts. */
+int xc_loopcape_multi(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                      const void *ts, const void *tds, int dtype, float pinc, int nsrc,
+                      const int *sources, float ml_depth, int adiabat, const int *start_3d, int nk,
+                      int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
+                      int *status, long long *counters, void *workspace, size_t workspace_bytes,
+                      void *stream);
+
 /* xc_loopcape_ex (natural column order, no counters) with the diagnostics
  * that getcape computes and discards -- the crossing pressure of its
  * buoyancy sign changes (CAPE_CODE_model_lev.f90:511, :526) and the parcel

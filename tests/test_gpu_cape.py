@@ -389,6 +389,67 @@ def test_calc_cape_sources_one_upload(guess, ring, monkeypatch):
             compare_cape(g, want, what=f"calc_cape_sources {name}")
 
 
+@pytest.mark.parametrize("guess", ["plain", "learned"])
+def test_loopcape_multi_device(guess):
+    """xc_loopcape_multi on device arrays (calc_cape_sources with CUDA
+    tensors): one ordering of the columns serves the three sources.  Each
+    source's outputs equal an xc_loopcape_ex call of its own bit for bit, the
+    work counters are the sum of the three calls' counters, and with
+    XC_RETRY_FP64 the retries, which reuse the ordering workspace, follow all
+    three lifts and give the single calls' results too."""
+    import ctypes
+    import torch
+    plev, t, td, ps, ts, tds = S.pressure_c1(shape=(96, 512), seed=8)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (plev, t, td, ps, ts, tds)]
+    names = ["mixed-layer", "surface", "most-unstable"]
+    gs = {"plain": _lib.XC_GUESS_PLAIN, "learned": _lib.XC_GUESS_LEARNED}[guess]
+    if guess == "learned":
+        from xcape_gb300 import guess as G
+        G.ensure_loaded()
+    got = X.calc_cape_sources(*dev, sources=names, vertical_lev="pressure", guess=guess)
+    for name in names:
+        single = X.calc_cape(*dev, source=name, vertical_lev="pressure", guess=guess)
+        for a, b in zip(got[name], single):
+            np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+    n2, nk = ps.size, t.shape[-1]
+    codes = [SOURCES[n] for n in names]
+    ws_bytes = _lib.workspace_bytes(n2)
+    wsbuf = torch.empty(ws_bytes + 256, dtype=torch.uint8, device="cuda")
+    ws = wsbuf.data_ptr() + (-wsbuf.data_ptr()) % 256
+    stream = torch.cuda.current_stream().cuda_stream
+    ptrs = [x.data_ptr() for x in dev]
+
+    def outputs(n):
+        return ([torch.empty(n, dtype=torch.float32, device="cuda") for _ in range(3)] +
+                [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)])
+
+    for g in (gs, gs | _lib.XC_RETRY_FP64):
+        cape, cin, zout, mulvl, status = outputs(3 * n2)
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        arr = (ctypes.c_int * 3)(*codes)
+        _lib.call("xc_loopcape_multi", 2, *ptrs, _lib.XC_F32, 500.0, 3,
+                  ctypes.cast(arr, ctypes.c_void_p), 500.0, 1, None, nk, n2, g, cape.data_ptr(),
+                  cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), status.data_ptr(),
+                  cnt.data_ptr(), ws, ws_bytes, stream)
+        total = torch.zeros(2, dtype=torch.int64, device="cuda")
+        for j, code in enumerate(codes):
+            o = outputs(n2)
+            c1 = torch.zeros(2, dtype=torch.int64, device="cuda")
+            _lib.call("xc_loopcape_ex", 2, *ptrs, _lib.XC_F32, 500.0, code, 500.0, 1, None, nk,
+                      n2, g, o[0].data_ptr(), o[1].data_ptr(), o[3].data_ptr(), o[2].data_ptr(),
+                      o[4].data_ptr(), c1.data_ptr(), ws, ws_bytes, stream)
+            total += c1
+            sl = slice(j * n2, (j + 1) * n2)
+            for a, b in zip((cape, cin, zout, mulvl, status), o):
+                np.testing.assert_array_equal(a[sl].cpu().numpy(), b.cpu().numpy())
+        np.testing.assert_array_equal(cnt.cpu().numpy(), total.cpu().numpy())
+    with pytest.raises(_lib.XcapeError, match="nsrc"):
+        _lib.call("xc_loopcape_multi", 2, *ptrs, _lib.XC_F32, 500.0, 4,
+                  ctypes.cast(arr, ctypes.c_void_p), 500.0, 1, None, nk, n2, gs, cape.data_ptr(),
+                  cin.data_ptr(), mulvl.data_ptr(), zout.data_ptr(), None, None, ws, ws_bytes,
+                  stream)
+
+
 def test_calc_cape_sources_arguments():
     plev, t, td, ps, ts, tds = S.pressure_c1(shape=(4, 8))
     with pytest.raises(ValueError, match="at most once"):

@@ -59,6 +59,8 @@ SIGNATURES = {
     + [_vp],
     "xc_loopcape_multi_host": [_i] + [_vp] * 6 + [_i, _f, _i, _vp, _f, _i, _vp, _i, _i, _i]
     + [_vp] * 5 + [_vp],
+    "xc_loopcape_multi": [_i] + [_vp] * 6 + [_i, _f, _i, _vp, _f, _i, _vp, _i, _i, _i] + [_vp] * 6
+    + [_vp, ctypes.c_size_t, _vp],
     "xc_loopcape_ex_noalloc": [_i] + [_vp] * 6 + [_i, _f, _i, _f, _i, _vp, _i, _i, _i]
     + [_vp] * 6 + [_vp],
     "xc_calc_srh": [_i] + [_vp] * 10 + [_i, _vp, _d, _d, _i, _i] + [_vp] * 5 + [_vp],

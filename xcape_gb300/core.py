@@ -306,8 +306,8 @@ def calc_cape_sources(p, t, td, ps, ts, tds, sources=("most-unstable", "mixed-la
     (src/xcape/core.py:130-235), so numpy inputs would cross to the device
     once per source; here they cross once (``xc_loopcape_multi_host``), and
     the columns are ordered once for all the sources.  CUDA tensors are used
-    in place, one launch per source.  ``guess`` and ``fp64_retry`` as in
-    ``calc_cape``.
+    in place (``xc_loopcape_multi``: one ordering, one launch per source).
+    ``guess`` and ``fp64_retry`` as in ``calc_cape``.
     """
     names = list(sources)
     if not names or len(set(names)) != len(names):
@@ -331,17 +331,15 @@ def calc_cape_sources(p, t, td, ps, ts, tds, sources=("most-unstable", "mixed-la
             status = b.empty(ns * b.n2, "i4")
     common = (grid, b.ptr(b.p), b.ptr(b.levels[0]), b.ptr(b.levels[1]), b.ptr(b.surface[0]),
               b.ptr(b.surface[1]), b.ptr(b.surface[2]), b.dtype, float(pinc))
+    import ctypes
+    arr = (ctypes.c_int * ns)(*codes)
     if b.torch:
         ws, ws_bytes = b.workspace(_lib.workspace_bytes(b.n2))
-        for j, code in enumerate(codes):
-            sl = slice(j * b.n2, (j + 1) * b.n2)
-            _lib.call("xc_loopcape_ex", *common, code, float(ml_depth), adi, None, b.nk, b.n2, gs,
-                      b.ptr(cape[sl]), b.ptr(cin[sl]), b.ptr(mulvl[sl]), b.ptr(zout[sl]),
-                      None if status is None else b.ptr(status[sl]), None, ws, ws_bytes,
-                      b.stream)
+        _lib.call("xc_loopcape_multi", *common, ns, ctypes.cast(arr, ctypes.c_void_p),
+                  float(ml_depth), adi, None, b.nk, b.n2, gs, b.ptr(cape), b.ptr(cin),
+                  b.ptr(mulvl), b.ptr(zout), None if status is None else b.ptr(status), None, ws,
+                  ws_bytes, b.stream)
     else:
-        import ctypes
-        arr = (ctypes.c_int * ns)(*codes)
         _lib.call("xc_loopcape_multi_host", *common, ns, ctypes.cast(arr, ctypes.c_void_p),
                   float(ml_depth), adi, None, b.nk, b.n2, gs, b.ptr(cape), b.ptr(cin),
                   b.ptr(mulvl), b.ptr(zout), None, None)

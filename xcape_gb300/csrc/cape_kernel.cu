@@ -139,13 +139,17 @@ __device__ __forceinline__ int order_bucket(const CapeArgs &a, long long i) {
   return start * ORDER_TD_BINS + bin;
 }
 
+// Neighbouring columns mostly fall in the same bucket, so the lanes of a warp
+// that share one add their count with a single atomic (warp-aggregated); the
+// blocks are whole warps, and lanes past n2 take part with bucket -1.
 template <typename T, int GRID>
 __global__ void order_bucket_kernel(CapeArgs a, unsigned short *bucket, unsigned *hist) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n2) return;
-  const int b = order_bucket<T, GRID>(a, i);
-  bucket[i] = (unsigned short)b;
-  atomicAdd(hist + b, 1u);
+  const bool in = i < a.n2;
+  const int b = in ? order_bucket<T, GRID>(a, i) : -1;
+  if (in) bucket[i] = (unsigned short)b;
+  const unsigned same = __match_any_sync(0xffffffffu, b);
+  if (in && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(hist + b, (unsigned)__popc(same));
 }
 
 // Exclusive scan of the ORDER_BUCKETS counters in place: one block of 1024
@@ -154,12 +158,18 @@ __global__ void __launch_bounds__(1024) order_scan_kernel(unsigned *hist) {
   constexpr int PER = ORDER_BUCKETS / 1024;
   __shared__ unsigned warp_tot[32];
   const int tid = threadIdx.x;
+  static_assert(PER % 4 == 0, "whole 16-byte loads per thread");
   unsigned v[PER], sum = 0;
 #pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    v[j] = hist[tid * PER + j];
-    sum += v[j];
+  for (int j = 0; j < PER; j += 4) {
+    const uint4 q = reinterpret_cast<const uint4 *>(hist + tid * PER)[j / 4];
+    v[j] = q.x;
+    v[j + 1] = q.y;
+    v[j + 2] = q.z;
+    v[j + 3] = q.w;
   }
+#pragma unroll
+  for (int j = 0; j < PER; ++j) sum += v[j];
   // inclusive scan of `sum` across the block
   unsigned x = sum;
   const int lane = tid & 31, w = tid >> 5;
@@ -182,18 +192,30 @@ __global__ void __launch_bounds__(1024) order_scan_kernel(unsigned *hist) {
   __syncthreads();
   unsigned run = x - sum + (w > 0 ? warp_tot[w - 1] : 0u);
 #pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    hist[tid * PER + j] = run;
-    run += v[j];
+  for (int j = 0; j < PER; j += 4) {
+    uint4 q;
+    q.x = run;
+    q.y = q.x + v[j];
+    q.z = q.y + v[j + 1];
+    q.w = q.z + v[j + 2];
+    run = q.w + v[j + 3];
+    reinterpret_cast<uint4 *>(hist + tid * PER)[j / 4] = q;
   }
 }
 
+// Lanes that share a bucket take consecutive places in it, in lane order,
+// from one atomic of their first lane.
 __global__ void order_scatter_kernel(const unsigned short *bucket, unsigned *offs, int *perm,
                                      long long n2) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n2) return;
-  const unsigned pos = atomicAdd(offs + bucket[i], 1u);
-  perm[pos] = (int)i;
+  const bool in = i < n2;
+  const int b = in ? (int)bucket[i] : -1;
+  const unsigned same = __match_any_sync(0xffffffffu, b);
+  const int lane = threadIdx.x & 31, first = __ffs(same) - 1;
+  unsigned base = 0;
+  if (in && lane == first) base = atomicAdd(offs + b, (unsigned)__popc(same));
+  base = __shfl_sync(0xffffffffu, base, first);
+  if (in) perm[base + __popc(same & ((1u << lane) - 1u))] = (int)i;
 }
 
 static size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -224,6 +246,8 @@ cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStre
   unsigned short *bucket = (unsigned short *)(b + round256(sizeof(unsigned) * ORDER_BUCKETS));
   *perm = pm;
   if (a.n2 <= 0) return cudaSuccess;
+  // the scan reads and writes the counters 16 bytes at a time
+  if (((uintptr_t)ws & 15) != 0) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * ORDER_BUCKETS, s);
   if (e != cudaSuccess) return e;
   const unsigned blocks = (unsigned)((a.n2 + 255) / 256);

@@ -255,6 +255,87 @@ struct Carver {
   }
 };
 
+// xc_loopcape_ex (nsrc 1) and xc_loopcape_multi: the lifts of nsrc sources
+// of the same device-resident columns, outputs [nsrc][n2].  With a workspace
+// the columns are ordered once, and every source's lift reads that order;
+// the FP64 retries, which reuse the workspace, come after all the lifts.
+int lift_sources(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                 const void *ts, const void *tds, int dtype, float pinc, int nsrc,
+                 const int *sources, float ml_depth, int adiabat, const int *start_3d, int nk,
+                 int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out, int *status,
+                 long long *counters, void *workspace, size_t workspace_bytes, void *stream) {
+  int rc = check_common(dtype, nk, n2);
+  if (rc) return rc;
+  for (int j = 0; j < nsrc; ++j) {
+    rc = check_cape_opts(pinc, sources[j], ml_depth, adiabat);
+    if (rc) return rc;
+  }
+  if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
+  if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
+  const bool retry = (guess & XC_RETRY_FP64) != 0;
+  guess &= ~XC_RETRY_FP64;
+  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_WARP)
+    return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
+  if (retry && !status) return fail(XC_ERR_INVALID, "XC_RETRY_FP64 needs the status array");
+  const float *guess_w = nullptr;
+  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY ||
+      guess == XC_GUESS_LEARNED_WARP) {
+    rc = guess_weights(&guess_w);
+    if (rc) return rc;
+  }
+  if (n2 == 0) return XC_OK;
+  if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
+    return fail(XC_ERR_INVALID, "NULL array argument");
+  xc::CapeArgs a;
+  a.grid = grid;
+  a.dtype = dtype;
+  a.p = p;
+  a.t = t3d;
+  a.td = td3d;
+  a.ps = ps;
+  a.ts = ts;
+  a.tds = tds;
+  a.start = grid == 1 ? nullptr : start_3d;
+  a.pinc = pinc;
+  a.ml_depth = ml_depth;
+  a.adiabat = adiabat;
+  a.nk = nk;
+  a.n2 = n2;
+  a.guess = guess;
+  a.counters = counters;
+  a.perm = nullptr;
+  a.guess_w = guess_w;
+  cudaError_t e = cudaSuccess;
+  if (workspace) {
+    if (workspace_bytes < xc::order_workspace_bytes(n2))
+      return fail(XC_ERR_INVALID, "workspace of %zu bytes is smaller than the %zu needed",
+                  workspace_bytes, xc::order_workspace_bytes(n2));
+    if (((size_t)workspace & 255) != 0) return fail(XC_ERR_INVALID, "workspace must be 256-byte aligned");
+    e = xc::launch_order(a, workspace, &a.perm, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
+  }
+  auto point = [&](int j) {
+    const size_t o = (size_t)j * (size_t)n2;
+    a.source = sources[j];
+    a.cape = cape + o;
+    a.cin = cin + o;
+    a.mulvl = mulvl + o;
+    a.z_out = z_out + o;
+    a.status = status ? status + o : nullptr;
+  };
+  for (int j = 0; j < nsrc; ++j) {
+    point(j);
+    e = xc::launch_cape(a, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+  }
+  for (int j = 0; retry && j < nsrc; ++j) {
+    point(j);
+    e = xc::launch_retry64(a, workspace, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "FP64 retry launch");
+  }
+  return XC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -290,67 +371,22 @@ int xc_loopcape_ex(int grid, const void *p, const void *t3d, const void *td3d, c
                    float ml_depth, int adiabat, const int *start_3d, int nk, int n2, int guess,
                    float *cape, float *cin, int *mulvl, float *z_out, int *status,
                    long long *counters, void *workspace, size_t workspace_bytes, void *stream) {
-  int rc = check_common(dtype, nk, n2);
-  if (rc) return rc;
-  rc = check_cape_opts(pinc, source, ml_depth, adiabat);
-  if (rc) return rc;
-  if (grid < 1 || grid > 3) return fail(XC_ERR_INVALID, "grid must be 1 (sigma), 2 (pressure, 1-D p) or 3 (pressure, 3-D p)");
-  if (grid == 3 && !start_3d) return fail(XC_ERR_INVALID, "grid 3 needs start_3d");
-  const bool retry = (guess & XC_RETRY_FP64) != 0;
-  guess &= ~XC_RETRY_FP64;
-  if (guess < XC_GUESS_PLAIN || guess > XC_GUESS_LEARNED_WARP)
-    return fail(XC_ERR_INVALID, "guess %d is not one of XC_GUESS_*", guess);
-  if (retry && !status) return fail(XC_ERR_INVALID, "XC_RETRY_FP64 needs the status array");
-  const float *guess_w = nullptr;
-  if (guess == XC_GUESS_LEARNED || guess == XC_GUESS_LEARNED_EVERY ||
-      guess == XC_GUESS_LEARNED_WARP) {
-    rc = guess_weights(&guess_w);
-    if (rc) return rc;
-  }
-  if (n2 == 0) return XC_OK;
-  if (!p || !t3d || !td3d || !ps || !ts || !tds || !cape || !cin || !mulvl || !z_out)
-    return fail(XC_ERR_INVALID, "NULL array argument");
-  xc::CapeArgs a;
-  a.grid = grid;
-  a.dtype = dtype;
-  a.p = p;
-  a.t = t3d;
-  a.td = td3d;
-  a.ps = ps;
-  a.ts = ts;
-  a.tds = tds;
-  a.start = grid == 1 ? nullptr : start_3d;
-  a.pinc = pinc;
-  a.source = source;
-  a.ml_depth = ml_depth;
-  a.adiabat = adiabat;
-  a.nk = nk;
-  a.n2 = n2;
-  a.guess = guess;
-  a.cape = cape;
-  a.cin = cin;
-  a.mulvl = mulvl;
-  a.z_out = z_out;
-  a.status = status;
-  a.counters = counters;
-  a.perm = nullptr;
-  a.guess_w = guess_w;
-  cudaError_t e = cudaSuccess;
-  if (workspace) {
-    if (workspace_bytes < xc::order_workspace_bytes(n2))
-      return fail(XC_ERR_INVALID, "workspace of %zu bytes is smaller than the %zu needed",
-                  workspace_bytes, xc::order_workspace_bytes(n2));
-    if (((size_t)workspace & 255) != 0) return fail(XC_ERR_INVALID, "workspace must be 256-byte aligned");
-    e = xc::launch_order(a, workspace, &a.perm, (cudaStream_t)stream);
-    if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
-  }
-  e = xc::launch_cape(a, (cudaStream_t)stream);
-  if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
-  if (retry) {
-    e = xc::launch_retry64(a, workspace, (cudaStream_t)stream);
-    if (e != cudaSuccess) return cuda_fail(e, "FP64 retry launch");
-  }
-  return XC_OK;
+  return lift_sources(grid, p, t3d, td3d, ps, ts, tds, dtype, pinc, 1, &source, ml_depth, adiabat,
+                      start_3d, nk, n2, guess, cape, cin, mulvl, z_out, status, counters,
+                      workspace, workspace_bytes, stream);
+}
+
+int xc_loopcape_multi(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
+                      const void *ts, const void *tds, int dtype, float pinc, int nsrc,
+                      const int *sources, float ml_depth, int adiabat, const int *start_3d, int nk,
+                      int n2, int guess, float *cape, float *cin, int *mulvl, float *z_out,
+                      int *status, long long *counters, void *workspace, size_t workspace_bytes,
+                      void *stream) {
+  if (nsrc < 1 || nsrc > 3) return fail(XC_ERR_INVALID, "nsrc=%d outside 1..3", nsrc);
+  if (!sources) return fail(XC_ERR_INVALID, "NULL sources");
+  return lift_sources(grid, p, t3d, td3d, ps, ts, tds, dtype, pinc, nsrc, sources, ml_depth,
+                      adiabat, start_3d, nk, n2, guess, cape, cin, mulvl, z_out, status, counters,
+                      workspace, workspace_bytes, stream);
 }
 
 int xc_loopcape_diag(int grid, const void *p, const void *t3d, const void *td3d, const void *ps,
