@@ -255,6 +255,43 @@ struct Carver {
   }
 };
 
+// Side streams of xc_loopcape_multi on each device (created on first use,
+// kept for the process): the second and third sources' lifts run on them,
+// beside the first source's on the caller's stream, so that a lift's last
+// blocks share the GPU with the next lift's first ones instead of running
+// alone.  The events that fork and join them are taken under fork_mu, so
+// that calls from several host threads each wait on their own records.
+struct SideStreams {
+  int dev = -1;
+  cudaStream_t s[2] = {nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+};
+std::mutex g_side_mu;
+std::vector<std::unique_ptr<SideStreams>> g_side;
+
+int side_streams(SideStreams **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_side_mu);
+  for (auto &x : g_side)
+    if (x->dev == dev) {
+      *out = x.get();
+      return XC_OK;
+    }
+  auto x = std::make_unique<SideStreams>();
+  x->dev = dev;
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+    e = cudaStreamCreateWithFlags(&x->s[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->join[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) return cuda_fail(e, "side streams of the multi-source lift");
+  *out = x.get();
+  g_side.push_back(std::move(x));
+  return XC_OK;
+}
+
 // xc_loopcape_ex (nsrc 1) and xc_loopcape_multi: the lifts of nsrc sources
 // of the same device-resident columns, outputs [nsrc][n2].  With a workspace
 // the columns are ordered once, and every source's lift reads that order;
@@ -323,10 +360,29 @@ int lift_sources(int grid, const void *p, const void *t3d, const void *td3d, con
     a.z_out = z_out + o;
     a.status = status ? status + o : nullptr;
   };
-  for (int j = 0; j < nsrc; ++j) {
-    point(j);
+  if (nsrc == 1) {
+    point(0);
     e = xc::launch_cape(a, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+  } else {
+    SideStreams *ss = nullptr;
+    rc = side_streams(&ss);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_side_mu);
+    const cudaStream_t s0 = (cudaStream_t)stream;
+    e = cudaEventRecord(ss->fork, s0);  // after the ordering
+    for (int j = 1; j < nsrc && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(ss->s[j - 1], ss->fork, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "forking the multi-source lift");
+    for (int j = 0; j < nsrc; ++j) {
+      point(j);
+      e = xc::launch_cape(a, j == 0 ? s0 : ss->s[j - 1]);
+      if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+    }
+    for (int j = 1; j < nsrc && e == cudaSuccess; ++j) {
+      e = cudaEventRecord(ss->join[j - 1], ss->s[j - 1]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s0, ss->join[j - 1], 0);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "joining the multi-source lift");
   }
   for (int j = 0; retry && j < nsrc; ++j) {
     point(j);
