@@ -324,20 +324,24 @@ def test_tall_columns(guess):
     assert np.all(d <= np.maximum(1.0, 1e-3 * want["cape"][ok])), d.max()
 
 
-@pytest.mark.parametrize("ring,chunks,streams", [(None, None, None), ("1", None, None),
-                                                  (None, "2", "1"), ("1", "3", "3")])
+@pytest.mark.parametrize("ring,chunks,streams,copies", [(None, None, None, None),
+                                                         ("1", None, None, "0"),
+                                                         (None, "2", "1", "3"),
+                                                         ("1", "3", "3", "7")])
 @pytest.mark.parametrize("guess", ["plain", "learned"])
-def test_host_path_chunks_match_device_path(guess, ring, chunks, streams, monkeypatch):
+def test_host_path_chunks_match_device_path(guess, ring, chunks, streams, copies, monkeypatch):
     """numpy inputs go through the pipelined host entry point (chunks of
     131,072+ columns, their inputs copied on one stream, their lifts on four
-    in turn); the results equal those of the device entry point on the same
+    in turn, their outputs moved into the caller's arrays by the copy
+    threads); the results equal those of the device entry point on the same
     arrays, bit for bit, whatever the pipelining: with XC_HOST_RING_BYTES=1
     the three chunks share two device slots, so the third reuses the first's
     buffers and staging; XC_HOST_CHUNKS and XC_HOST_STREAMS change the chunk
-    count and the compute streams."""
+    count and the compute streams, XC_HOST_COPY_THREADS the output copies'
+    split (0: the calling thread copies)."""
     import torch
     for name, val in (("XC_HOST_RING_BYTES", ring), ("XC_HOST_CHUNKS", chunks),
-                      ("XC_HOST_STREAMS", streams)):
+                      ("XC_HOST_STREAMS", streams), ("XC_HOST_COPY_THREADS", copies)):
         if val is not None:
             monkeypatch.setenv(name, val)
     plev, t, td, ps, ts, tds = S.pressure_c1(shape=(216, 1440))  # 311,040 columns: 3 chunks
