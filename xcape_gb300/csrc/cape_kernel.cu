@@ -152,27 +152,26 @@ __global__ void order_bucket_kernel(CapeArgs a, unsigned short *bucket, unsigned
   if (in && (threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(hist + b, (unsigned)__popc(same));
 }
 
-// Exclusive scan of the ORDER_BUCKETS counters in place: one block of 1024
-// threads, 16 consecutive counters per thread.
-__global__ void __launch_bounds__(1024) order_scan_kernel(unsigned *hist) {
-  constexpr int PER = ORDER_BUCKETS / 1024;
-  __shared__ unsigned warp_tot[32];
-  const int tid = threadIdx.x;
-  static_assert(PER % 4 == 0, "whole 16-byte loads per thread");
-  unsigned v[PER], sum = 0;
-#pragma unroll
-  for (int j = 0; j < PER; j += 4) {
-    const uint4 q = reinterpret_cast<const uint4 *>(hist + tid * PER)[j / 4];
-    v[j] = q.x;
-    v[j + 1] = q.y;
-    v[j + 2] = q.z;
-    v[j + 3] = q.w;
+// Exclusive scan of the ORDER_BUCKETS counters in place, by one block of
+// ORDER_SCAN_THREADS threads: small enough to start in the slot that one
+// retiring lift block frees on an SM (the host path orders a chunk while
+// the lifts of earlier chunks fill the GPU).  Each thread sums its
+// consecutive counters, the block scans the sums, and each thread writes
+// its counters' prefixes, 16 bytes at a time.
+constexpr int ORDER_SCAN_THREADS = 128;
+__global__ void __launch_bounds__(ORDER_SCAN_THREADS) order_scan_kernel(unsigned *hist) {
+  constexpr int PER = ORDER_BUCKETS / ORDER_SCAN_THREADS;
+  static_assert(PER % 4 == 0, "whole 16-byte accesses per thread");
+  __shared__ unsigned warp_tot[ORDER_SCAN_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  uint4 *h4 = reinterpret_cast<uint4 *>(hist + tid * PER);
+  unsigned sum = 0;
+  for (int j = 0; j < PER / 4; ++j) {
+    const uint4 q = h4[j];
+    sum += q.x + q.y + q.z + q.w;
   }
-#pragma unroll
-  for (int j = 0; j < PER; ++j) sum += v[j];
   // inclusive scan of `sum` across the block
   unsigned x = sum;
-  const int lane = tid & 31, w = tid >> 5;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
@@ -180,26 +179,17 @@ __global__ void __launch_bounds__(1024) order_scan_kernel(unsigned *hist) {
   }
   if (lane == 31) warp_tot[w] = x;
   __syncthreads();
-  if (w == 0) {
-    unsigned z = warp_tot[lane];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(0xffffffffu, z, o);
-      if (lane >= o) z += y;
-    }
-    warp_tot[lane] = z;
-  }
-  __syncthreads();
-  unsigned run = x - sum + (w > 0 ? warp_tot[w - 1] : 0u);
-#pragma unroll
-  for (int j = 0; j < PER; j += 4) {
-    uint4 q;
-    q.x = run;
-    q.y = q.x + v[j];
-    q.z = q.y + v[j + 1];
-    q.w = q.z + v[j + 2];
-    run = q.w + v[j + 3];
-    reinterpret_cast<uint4 *>(hist + tid * PER)[j / 4] = q;
+  unsigned run = x - sum;
+  for (int v = 0; v < w; ++v) run += warp_tot[v];
+  for (int j = 0; j < PER / 4; ++j) {
+    const uint4 q = h4[j];
+    uint4 r;
+    r.x = run;
+    r.y = r.x + q.x;
+    r.z = r.y + q.y;
+    r.w = r.z + q.z;
+    run = r.w + q.w;
+    h4[j] = r;
   }
 }
 
@@ -260,7 +250,7 @@ cudaError_t launch_order(const CapeArgs &a, void *ws, const int **perm, cudaStre
     else if (a.grid == 2) launch_bucket<double, 2>(a, bucket, hist, blocks, s);
     else launch_bucket<double, 3>(a, bucket, hist, blocks, s);
   }
-  order_scan_kernel<<<1, 1024, 0, s>>>(hist);
+  order_scan_kernel<<<1, ORDER_SCAN_THREADS, 0, s>>>(hist);
   order_scatter_kernel<<<blocks, 256, 0, s>>>(bucket, hist, pm, a.n2);
   return cudaGetLastError();
 }

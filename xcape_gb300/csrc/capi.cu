@@ -209,8 +209,20 @@ struct HostCtx {
   bool busy = false;
   cudaStream_t s[4] = {};  // kernels and output copies, chunks in turn over host_streams()
   cudaStream_t copy = nullptr;             // input copies, in chunk order
+  // the chunks' column orderings, at the device's highest stream priority:
+  // a chunk's ordering kernels then take the SM slots that earlier chunks'
+  // lift blocks free before more lift blocks do, and its lifts start sooner
+  cudaStream_t ord = nullptr;
   cudaEvent_t start = nullptr;
   cudaEvent_t loaded[HOST_CHUNKS] = {};    // slot k holds its chunk's inputs
+  cudaEvent_t ordered[HOST_CHUNKS] = {};   // slot k's columns are ordered
+  // the second and third sources' lifts of every chunk, beside the first
+  // source's on the chunk's compute stream (a chunk's lifts are about one
+  // wave of blocks each: run one after the other they doubled the time from
+  // the last chunk's inputs to its outputs); lifted[k][j] marks slot k's
+  // lift of source j + 1 done
+  cudaStream_t side[2] = {};
+  cudaEvent_t lifted[HOST_CHUNKS][2] = {};
   cudaEvent_t done[HOST_CHUNKS] = {};      // slot k's outputs are in its staging
   char *pinned = nullptr;                  // pinned output staging, grow-only
   size_t pinned_cap = 0;
@@ -257,8 +269,19 @@ struct HostCtxLease {
     for (int k = 0; k < 4 && e == cudaSuccess; ++k)
       if (!c->s[k]) e = cudaStreamCreateWithFlags(&c->s[k], cudaStreamNonBlocking);
     if (e == cudaSuccess && !c->copy) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    for (int j = 0; j < 2 && e == cudaSuccess; ++j)
+      if (!c->side[j]) e = cudaStreamCreateWithFlags(&c->side[j], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !c->ord) {
+      int least = 0, greatest = 0;
+      e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->ord, cudaStreamNonBlocking, greatest);
+    }
     for (int k = 0; k < HOST_CHUNKS && e == cudaSuccess; ++k) {
       if (!c->done[k]) e = cudaEventCreateWithFlags(&c->done[k], cudaEventDisableTiming);
+      if (e == cudaSuccess && !c->ordered[k])
+        e = cudaEventCreateWithFlags(&c->ordered[k], cudaEventDisableTiming);
+      for (int j = 0; j < 2 && e == cudaSuccess; ++j)
+        if (!c->lifted[k][j]) e = cudaEventCreateWithFlags(&c->lifted[k][j], cudaEventDisableTiming);
       if (e == cudaSuccess && !c->loaded[k])
         e = cudaEventCreateWithFlags(&c->loaded[k], cudaEventDisableTiming);
     }
@@ -775,6 +798,8 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
   for (int k = 0; k < nstream && e == cudaSuccess; ++k)
     e = cudaStreamWaitEvent(pl->s[k], pl->start, 0);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->copy, pl->start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->ord, pl->start, 0);
+  for (int j = 0; j < 2 && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(pl->side[j], pl->start, 0);
   if (e != cudaSuccess) return cuda_fail(e, "ordering the host path after the caller's stream");
   const char *hp = (const char *)p, *ht = (const char *)t3d, *htd = (const char *)td3d;
   const char *hps = (const char *)ps, *hts = (const char *)ts, *htds = (const char *)tds;
@@ -809,7 +834,7 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
     if (has_start) H2D(q.st, start_3d + c0, (size_t)nc * 4);
 #undef H2D
     if (e == cudaSuccess) e = cudaEventRecord(pl->loaded[k], pl->copy);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, pl->loaded[k], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->ord, pl->loaded[k], 0);
     if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
     xc::CapeArgs a;
     a.grid = grid;
@@ -830,7 +855,9 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
     a.counters = nullptr;
     a.perm = nullptr;
     a.guess_w = guess_w;
-    e = xc::launch_order(a, b + q.ord, &a.perm, s);
+    e = xc::launch_order(a, b + q.ord, &a.perm, pl->ord);
+    if (e == cudaSuccess) e = cudaEventRecord(pl->ordered[k], pl->ord);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, pl->ordered[k], 0);
     if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
     auto point = [&](int s_) {
       char *o = b + q.out;
@@ -841,11 +868,15 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
       a.z_out = (float *)(o + out_off(s_, 3));
       a.status = nout == 5 ? (int *)(o + out_off(s_, 4)) : nullptr;
     };
-    for (int s_ = 0; s_ < nsrc; ++s_) {
+    for (int s_ = 1; s_ < nsrc && e == cudaSuccess; ++s_)
+      e = cudaStreamWaitEvent(pl->side[s_ - 1], pl->ordered[k], 0);
+    for (int s_ = 0; s_ < nsrc && e == cudaSuccess; ++s_) {
       point(s_);
-      e = xc::launch_cape(a, s);
-      if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
+      e = xc::launch_cape(a, s_ == 0 ? s : pl->side[s_ - 1]);
+      if (e == cudaSuccess && s_ > 0) e = cudaEventRecord(pl->lifted[k][s_ - 1], pl->side[s_ - 1]);
+      if (e == cudaSuccess && s_ > 0) e = cudaStreamWaitEvent(s, pl->lifted[k][s_ - 1], 0);
     }
+    if (e != cudaSuccess) return cuda_fail(e, "cape kernel launch");
     // the FP64 retries come after every source's lift: each reuses the
     // ordering workspace, which the lifts read
     for (int s_ = 0; retry && s_ < nsrc; ++s_) {
