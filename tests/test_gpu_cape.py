@@ -331,7 +331,7 @@ def test_tall_columns(guess):
 @pytest.mark.parametrize("guess", ["plain", "learned"])
 def test_host_path_chunks_match_device_path(guess, ring, chunks, streams, copies, monkeypatch):
     """numpy inputs go through the pipelined host entry point (chunks of
-    131,072+ columns, their inputs copied on one stream, their lifts on four
+    131,072+ columns, their inputs copied on one stream, their lifts on two
     in turn, their outputs moved into the caller's arrays by the copy
     threads); the results equal those of the device entry point on the same
     arrays, bit for bit, whatever the pipelining: with XC_HOST_RING_BYTES=1

@@ -85,10 +85,10 @@ size_t host_ring_bytes() {
   return (size_t)4 << 30;
 }
 
-// Compute streams the host path's chunks take in turn: 4, or the
+// Compute streams the host path's chunks take in turn: 2, or the
 // environment's XC_HOST_STREAMS (1..4; it changes only how the work overlaps
-// on the GPU, never a result).  With more launches in flight, the tails of
-// the chunks' lifts overlap: 1 stream 174, 2 streams 242, 4 streams 248 M
+// on the GPU, never a result).  With the second source's lifts on a side
+// stream, 1, 2, 3 and 4 compute streams gave 389, 403, 394 and 388 M
 // columns/s end to end on 1M columns x 37 levels, two sources.
 int host_streams() {
   const char *e = getenv("XC_HOST_STREAMS");
@@ -96,7 +96,7 @@ int host_streams() {
     const int v = atoi(e);
     if (v >= 1 && v <= 4) return v;
   }
-  return 4;
+  return 2;
 }
 
 // Host threads that move the host path's outputs from pinned staging into
@@ -646,14 +646,16 @@ namespace {
 
 // The host-pointer CAPE path for nsrc sources of the same columns.  The
 // columns go through in chunks.  One stream copies the chunks' inputs in
-// order, once for all the sources; each chunk's ordering, its nsrc lifts and
-// its output copies run on one of host_streams() compute streams, in turn,
-// once its inputs are in, so copies overlap lifts and one chunk's last warps
-// overlap the next chunks' first.  Every chunk has its own device slot when the ring budget allows
-// (the usual case), and then the calling thread queues the whole call
-// without waiting.  Outputs come back into pinned staging (a copy into
-// pageable memory would block this thread) and are moved into the caller's
-// arrays at the end, or when a slot is reused.  The column ordering depends
+// order, once for all the sources; once a chunk's inputs are in, its
+// ordering runs on the priority stream, its first source's lift and its
+// output copies on one of host_streams() compute streams, in turn, and the
+// other sources' lifts on the side streams.  So copies overlap lifts and
+// one chunk's last warps overlap the next chunks' first.  Every chunk has
+// its own device slot when the ring budget allows (the usual case), and
+// then the calling thread queues the whole call without waiting.  Outputs
+// come back into pinned staging (a copy into pageable memory would block
+// this thread) and are moved into the caller's arrays by the copy threads
+// as the chunks land, or when a slot is reused.  The column ordering depends
 // only on the start level and the surface dewpoint, not on the source, so
 // one ordering per chunk serves every source.  Each column is still computed
 // by one thread and written to its own index, so neither the chunking nor
