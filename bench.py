@@ -48,9 +48,9 @@ CPU_SAMPLE = 131072      # columns per CPU-baseline measurement
 # share and active threads per warp instruction, from `ncu --set full`
 # captures of `bench.py --profile` (profiles/cape_kernel_pressure_1M.md).
 NCU_RECORDED = "ncu --set full of bench.py --profile, profiles/cape_kernel_pressure_1M.md"
-NCU_TRAFFIC = {"learned": 697_144_832, "plain": 728_342_784}
-NCU_ISSUE = {"learned": {"issue_active": 0.847, "tensor_pipe_active": 0.0105,
-                         "threads_per_warp_instruction": 28.25},
+NCU_TRAFFIC = {"learned": 689_983_744, "plain": 728_342_784}
+NCU_ISSUE = {"learned": {"issue_active": 0.811, "tensor_pipe_active": 0.0131,
+                         "threads_per_warp_instruction": 28.65},
              "plain": {"issue_active": 0.879, "tensor_pipe_active": 0.0,
                        "threads_per_warp_instruction": 27.11}}
 ACC_SAMPLE = 8192        # columns checked against the FP64 oracle in the CPU leg (strided)
