@@ -536,11 +536,13 @@ XC_HD bool substep(R dp, R &p2, R &t2, R &th2, R &qv2, R &ql2, R &qi2, R &qt, in
     }
   }
   if constexpr (SOLVER == SOLVE_LEARNED) {
-    if (ql2 + qi2 > 0.0f && ss.lcl_y == ss.lcl_y && dp != 0.0f) {
-      // the parcel has just saturated: the increment extrapolated into the
-      // next sub-step is the network's, not this sub-step's partial one
-      ss.rate = -GUESS_SLOPE_SCALE * ss.lcl_y * fast_div(lp, dp);
-      ss.lcl_y = NAN;
+    if (ss.lcl_y == ss.lcl_y) {  // the network's output not yet taken
+      if (ql2 + qi2 > 0.0f && dp != 0.0f) {
+        // the parcel has just saturated: the increment extrapolated into the
+        // next sub-step is the network's, not this sub-step's partial one
+        ss.rate = -GUESS_SLOPE_SCALE * ss.lcl_y * fast_div(lp, dp);
+        ss.lcl_y = NAN;
+      }
     }
   }
   if constexpr (SOLVER == SOLVE_LEARNED_ALL || SOLVER == SOLVE_LEARNED_WARP)
@@ -869,7 +871,11 @@ XC_HD CapeResult ascend_col(const ColumnReader<T, GRID, R> &col, int ncl, float 
           return r;
         }
         nloop = 1 + (int)f;
-        dp = dp / (R)nloop;
+        if constexpr (FAST) {
+          dp = dp * fast_rcp((float)nloop);
+        } else {
+          dp = dp / (R)nloop;
+        }
       }
       if constexpr (SOLVER != SOLVE_PLAIN) ss.rdp = fast_rcp(dp);
       if (r.nsub + nloop > MAX_SUBSTEPS) {
