@@ -385,21 +385,33 @@ def column_levels(plev, ps, ts):
 
 # XU (transcendental unit) lane operations of the accelerated solvers per unit
 # of work, counted from the column code (cape_column.cuh, xc_common.cuh): each
-# approximate exp (ex2), log (lg2) and divide (rcp) is one XU operation.
-#   environment of a level (make_env<true>): pi = exp(k ln p) 2, getqvs_fast
+# approximate exp (ex2), log (lg2) and reciprocal (rcp) is one XU operation.
+#   environment of a level (make_env<true>): pi = 2^(k log2 p) 2, qsat_fast
 #     3, theta and theta_v 2                                          -> 7
-#   ascent level: the environment + the two buoyancy divides          -> 9
-#   most-unstable level (p >= 500 hPa): getqvs_fast 3 + getthe_fast 9 -> 12
+#   ascent level: the environment, the two buoyancy divides, 1/dp and
+#     1/nloop                                                         -> 11
+#   most-unstable level (p >= 500 hPa): qsat_fast 3 + getthe_fast 8    -> 11
 #   mixed-layer pass level: the environment                           -> 7
-#   sub-step: ln p2, pi2, and the analytic slope's two divides        -> 4
+#   sub-step: log2 p2, pi2, the Newton step's reciprocal               -> 3
 #   iteration (accel_map, liquid): qsat 3, exponent 1, exp 1          -> 5
 #   step between iterations (secant quotient, root step)             -> 2
-XU_MODEL = {"ascent_level": 9, "mu_level": 12, "ml_level": 7, "substep": 4, "iteration": 5,
+XU_MODEL = {"ascent_level": 11, "mu_level": 11, "ml_level": 7, "substep": 3, "iteration": 5,
             "step": 2}
-# FP32 lane operations (FFMA, FADD, FMUL, FMNMX, FSETP and the multiplies of
-# the approximate functions) of the same code, per unit.
-FP32_MODEL = {"ascent_level": 30, "mu_level": 35, "ml_level": 25, "substep": 25,
-              "iteration": 45, "step": 12}
+# FP32 lane operations (FFMA, FADD, FMUL, FMNMX, FSETP, FSEL and the
+# multiplies of the approximate functions) of the same code, per unit:
+#   iteration (accel_map, liquid, without the slope): t2, qsat 7, the clamps
+#     5, the sums 3, lhv/rm/cpm 5, the exponent's quotient 5, the exp 3    -> 29
+#   sub-step: p2, log p, pi2 4; the guess 1; the convergence test 2; the
+#     Newton step 8; the Newton-point ending 16; the rate 3; the network's
+#     onset test 2; the slope of the first evaluation (saturated) 16       -> 52
+#   step between iterations: secant quotient 3, root step 6, test 2      -> 12
+#   ascent level: the environment 16, height 5, sub-step count and dp 13,
+#     buoyancy 9, areas and sums 20                                        -> 63
+#   most-unstable level: the level 4, qsat 7, getthe_fast 18, the maximum
+#     4                                                                    -> 33
+#   mixed-layer pass level: the environment 16, the averages 9             -> 25
+FP32_MODEL = {"ascent_level": 63, "mu_level": 33, "ml_level": 25, "substep": 52,
+              "iteration": 29, "step": 12}
 
 
 def model_ops(model, work, lev, source_code):
