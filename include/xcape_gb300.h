@@ -222,7 +222,12 @@ int xc_loopcape_ex_noalloc(int grid, const void *p, const void *t3d, const void 
  * columns go through in up to 8 chunks whose device buffers take at most
  * 4 GiB (at least two chunks' worth; the environment variable
  * XC_HOST_RING_BYTES sets another limit, in bytes); chunks beyond that
- * reuse buffers, which changes no result. */
+ * reuse buffers, which changes no result.  The outputs reach the caller's
+ * arrays through pinned staging, moved by a pool of host threads that the
+ * library starts on first use and keeps (XC_HOST_COPY_THREADS, 0..16,
+ * default 4; 0 moves them in the calling thread).  XC_HOST_CHUNKS (2..16,
+ * default 8) and XC_HOST_STREAMS (1..4, default 2) set the chunk count and
+ * the compute streams; none of these changes a result. */
 int xc_loopcape_ex_host(int grid, const void *p, const void *t3d, const void *td3d,
                         const void *ps, const void *ts, const void *tds, int dtype, float pinc,
                         int source, float ml_depth, int adiabat, const int *start_3d, int nk,
