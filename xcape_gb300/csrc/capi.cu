@@ -218,9 +218,8 @@ struct HostCtx {
   cudaEvent_t ordered[HOST_CHUNKS] = {};   // slot k's columns are ordered
   // the second and third sources' lifts of every chunk, beside the first
   // source's on the chunk's compute stream (a chunk's lifts are about one
-  // wave of blocks each: run one after the other they doubled the time from
-  // the last chunk's inputs to its outputs); lifted[k][j] marks slot k's
-  // lift of source j + 1 done
+  // wave of blocks each, and beside each other they share the SMs);
+  // lifted[k][j] marks slot k's lift of source j + 1 done
   cudaStream_t side[2] = {};
   cudaEvent_t lifted[HOST_CHUNKS][2] = {};
   cudaEvent_t done[HOST_CHUNKS] = {};      // slot k's outputs are in its staging
@@ -372,8 +371,9 @@ struct Carver {
 // kept for the process): the second and third sources' lifts run on them,
 // beside the first source's on the caller's stream, so that a lift's last
 // blocks share the GPU with the next lift's first ones instead of running
-// alone.  The events that fork and join them are taken under fork_mu, so
-// that calls from several host threads each wait on their own records.
+// alone.  The events that fork and join them are recorded and waited on
+// under g_side_mu, so that calls from several host threads each wait on
+// their own records.
 struct SideStreams {
   int dev = -1;
   cudaStream_t s[2] = {nullptr, nullptr};
