@@ -454,6 +454,26 @@ def test_loopcape_multi_device(guess):
                   stream)
 
 
+@pytest.mark.parametrize("adiabat", ["pseudo-liquid", "reversible-ice"])
+def test_loopcape_multi_device_sigma_f64(adiabat):
+    """xc_loopcape_multi on the sigma grid with float64 CUDA tensors (the
+    small CPU case, 64 x 64 columns x 40 levels): every source equals its
+    own calc_cape call bit for bit, with the plain and the learned solver."""
+    import torch
+    p, t, td, ps, ts, tds = S.sigma_c0()
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (p, t, td, ps, ts, tds)]
+    names = ["most-unstable", "mixed-layer", "surface"]
+    for guess in ("plain", "learned"):
+        got = X.calc_cape_sources(*dev, sources=names, adiabat=adiabat, vertical_lev="sigma",
+                                  guess=guess)
+        for name in names:
+            single = X.calc_cape(*dev, source=name, adiabat=adiabat, vertical_lev="sigma",
+                                 guess=guess)
+            assert len(got[name]) == len(single)
+            for a, b in zip(got[name], single):
+                np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
 def test_calc_cape_sources_arguments():
     plev, t, td, ps, ts, tds = S.pressure_c1(shape=(4, 8))
     with pytest.raises(ValueError, match="at most once"):
