@@ -215,6 +215,7 @@ struct HostCtx {
   cudaStream_t ord = nullptr;
   cudaEvent_t start = nullptr;
   cudaEvent_t loaded[HOST_CHUNKS] = {};    // slot k holds its chunk's inputs
+  cudaEvent_t surf[HOST_CHUNKS] = {};      // ... those the ordering reads (copied first)
   cudaEvent_t ordered[HOST_CHUNKS] = {};   // slot k's columns are ordered
   // the second and third sources' lifts of every chunk, beside the first
   // source's on the chunk's compute stream (a chunk's lifts are about one
@@ -279,6 +280,8 @@ struct HostCtxLease {
       if (!c->done[k]) e = cudaEventCreateWithFlags(&c->done[k], cudaEventDisableTiming);
       if (e == cudaSuccess && !c->ordered[k])
         e = cudaEventCreateWithFlags(&c->ordered[k], cudaEventDisableTiming);
+      if (e == cudaSuccess && !c->surf[k])
+        e = cudaEventCreateWithFlags(&c->surf[k], cudaEventDisableTiming);
       for (int j = 0; j < 2 && e == cudaSuccess; ++j)
         if (!c->lifted[k][j]) e = cudaEventCreateWithFlags(&c->lifted[k][j], cudaEventDisableTiming);
       if (e == cudaSuccess && !c->loaded[k])
@@ -823,20 +826,21 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
 #define H2D(off, src, bytes)                                                         \
     if (e == cudaSuccess)                                                            \
       e = cudaMemcpyAsync(b + (off), (src), (bytes), cudaMemcpyHostToDevice, pl->copy)
-    if (grid == 2) {
-      H2D(q.p, hp, (size_t)nk * es);
-    } else {
-      H2D(q.p, hp + off3, r3);
-    }
-    H2D(q.t, ht + off3, r3);
-    H2D(q.td, htd + off3, r3);
+    // first what the ordering reads (the surface values, the start levels,
+    // the 1-D pressures), so that the chunk's ordering runs while its
+    // profiles are still crossing
+    if (grid == 2) H2D(q.p, hp, (size_t)nk * es);
     H2D(q.ps, hps + off1, (size_t)nc * es);
     H2D(q.ts, hts + off1, (size_t)nc * es);
     H2D(q.tds, htds + off1, (size_t)nc * es);
     if (has_start) H2D(q.st, start_3d + c0, (size_t)nc * 4);
+    if (e == cudaSuccess) e = cudaEventRecord(pl->surf[k], pl->copy);
+    if (grid != 2) H2D(q.p, hp + off3, r3);
+    H2D(q.t, ht + off3, r3);
+    H2D(q.td, htd + off3, r3);
 #undef H2D
     if (e == cudaSuccess) e = cudaEventRecord(pl->loaded[k], pl->copy);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->ord, pl->loaded[k], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->ord, pl->surf[k], 0);
     if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
     xc::CapeArgs a;
     a.grid = grid;
@@ -860,6 +864,7 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
     e = xc::launch_order(a, b + q.ord, &a.perm, pl->ord);
     if (e == cudaSuccess) e = cudaEventRecord(pl->ordered[k], pl->ord);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, pl->ordered[k], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, pl->loaded[k], 0);
     if (e != cudaSuccess) return cuda_fail(e, "column ordering launch");
     auto point = [&](int s_) {
       char *o = b + q.out;
@@ -870,8 +875,10 @@ int host_lift(int grid, const void *p, const void *t3d, const void *td3d, const 
       a.z_out = (float *)(o + out_off(s_, 3));
       a.status = nout == 5 ? (int *)(o + out_off(s_, 4)) : nullptr;
     };
-    for (int s_ = 1; s_ < nsrc && e == cudaSuccess; ++s_)
+    for (int s_ = 1; s_ < nsrc && e == cudaSuccess; ++s_) {
       e = cudaStreamWaitEvent(pl->side[s_ - 1], pl->ordered[k], 0);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(pl->side[s_ - 1], pl->loaded[k], 0);
+    }
     for (int s_ = 0; s_ < nsrc && e == cudaSuccess; ++s_) {
       point(s_);
       e = xc::launch_cape(a, s_ == 0 ? s : pl->side[s_ - 1]);
